@@ -1,0 +1,99 @@
+// eg_internal.h -- device-side mesh object and shared helpers of libeulergpu.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "eulergpu.h"
+
+#define EG_MAX_NV 5
+#define EG_MAX_NF 16
+#define EG_MAX_NP 64
+#define EG_MAX_S 64
+
+// device status word bits (set with atomicOr by kernels, read by the host)
+#define EG_DEV_NEG_DENSITY 1u
+#define EG_DEV_NEG_PRESSURE 2u
+#define EG_DEV_NONFINITE 4u
+#define EG_DEV_LU_PIVOT 8u
+
+void eg_set_error(const char* fmt, ...);
+int eg_cuda_fail(cudaError_t e, const char* what);
+
+#define EG_CUDA(call)                                      \
+  do {                                                     \
+    cudaError_t _e = (call);                               \
+    if (_e != cudaSuccess) return eg_cuda_fail(_e, #call); \
+  } while (0)
+
+// Physics constants in the form the kernels read them.
+struct DevParams {
+  double gamma, gamma_1;
+  double Ma, aoa, rho_free, p_free, E_free;
+  double r_in, rho_in, M_in;
+  double R, cv;
+};
+
+// Per-element face table entry: which face-flux slot a local face reads and
+// from which side.  slot < I: interface slot; slot >= I: boundary slot.
+struct EFace {
+  int32_t slot;
+  int32_t side;    // 0: element is elementL (or boundary owner), 1: elementR
+  int32_t orient;  // nbrperm column for side 1
+  int32_t pad;
+};
+
+// phase ids of the device timers (eg_timings fields)
+enum { EG_PHASE_FACE = 0, EG_PHASE_ELEMENT = 1, EG_PHASE_NORM = 2, EG_PHASE_OTHER = 3, EG_NPHASE = 4 };
+
+struct TimerState;  // event pool (eg_timing.cu)
+
+struct eg_mesh {
+  // sizes
+  int dim, E, Np, Nf, S, F, I, B, nbc, norient, nv;
+  int64_t ndof;
+  eg_params params;
+  DevParams dp;
+  cudaStream_t stream;
+  // operator (device)
+  double* Q;        // [dim][Np(j)][Np(i)]: Q[k][j][i] = Q_k(i, j)
+  double* w;        // [Np]
+  double* interp;   // [F][Nf][S]
+  int32_t* perm;    // [F][S]
+  int32_t* nbrperm; // [norient][Nf]
+  double* wface;    // [Nf]
+  double* lift;     // [F][Np][Nf]: sum_s [perm[f][s]==j] interp[f][i][s] * wface[i]
+  // mesh (device)
+  double* dxidx;    // [E][Np][dim][dim]
+  double* jac;      // [E][Np]
+  double* Minv;     // [E][Np] = jac / w
+  int32_t* ifaces;  // [I][5]
+  double* nrm_face; // [I][Nf][dim]
+  int32_t* bfaces;  // [B][2]
+  int32_t* bc_of_b; // [B] boundary condition of each boundary face
+  double* coords_bndry; // [B][Nf][dim]
+  double* nrm_bndry;    // [B][Nf][dim]
+  double* qg_bndry;     // [B][Nf][nv] Dirichlet states (time-independent, set at creation)
+  EFace* eface;     // [E][F]
+  // work buffers (device)
+  double* fflux;    // [(I+B)][Nf][nv] face fluxes times wface
+  double* q_dev;    // [ndof] staging for host inputs
+  double* res_dev;  // [ndof] staging for host outputs
+  unsigned int* status;   // device status word
+  double* red;      // reduction scratch
+  unsigned int* h_status; // pinned host mirror
+  double* h_red;          // pinned host scalar
+  cudaStream_t own_stream;  // the library's stream (stream may be a caller's)
+  TimerState* timer;        // phase timers (null until enabled)
+  int64_t launches;         // kernel launches since creation
+};
+
+// phase timers: bracket a group of launches on m->stream
+void eg_phase_begin(eg_mesh* m, int phase);
+void eg_phase_end(eg_mesh* m, int phase, int nlaunch);
+void eg_timer_free(eg_mesh* m);
+
+// kernels entry points used across translation units
+int eg_residual_device(eg_mesh* m, const double* q, double* res);
+int eg_check_status(eg_mesh* m);

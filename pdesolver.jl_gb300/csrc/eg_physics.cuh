@@ -1,0 +1,268 @@
+// eg_physics.cuh -- point functions of the Euler equations on the device.
+//
+// Scalar-generic (T = double, float, or a forward-mode derivative carrier) so
+// the Jacobian kernels differentiate the same arithmetic the residual uses.
+// Formulas follow the reference:
+//   calcPressure      src/solver/euler/euler_funcs.jl:856-911
+//   calcEulerFlux     src/solver/euler/euler_funcs.jl:512-540, 749-773
+//   RoeSolver/calcSAT src/solver/euler/bc_solvers.jl:29-425
+//   calcEulerFlux_IR  src/solver/euler/bc_solvers.jl:725-884
+//   logavg            src/solver/euler/bc_solvers.jl:942-956
+#pragma once
+#include <cuda_runtime.h>
+
+namespace eg {
+
+// ---------------------------------------------------------------------------
+// derivative carrier: value + N directional derivatives
+template <typename R, int N>
+struct Fwd {
+  R v;
+  R d[N];
+  __host__ __device__ Fwd() {}
+  __host__ __device__ Fwd(R x) : v(x) {  // NOLINT: implicit from constants
+#pragma unroll
+    for (int i = 0; i < N; ++i) d[i] = R(0);
+  }
+};
+
+#define EG_FWD_BIN(OP, VAL, DER)                                                             \
+  template <typename R, int N>                                                               \
+  __host__ __device__ __forceinline__ Fwd<R, N> operator OP(const Fwd<R, N>& a,              \
+                                                            const Fwd<R, N>& b) {            \
+    Fwd<R, N> r;                                                                             \
+    r.v = VAL;                                                                               \
+    _Pragma("unroll") for (int i = 0; i < N; ++i) r.d[i] = DER;                              \
+    return r;                                                                                \
+  }
+EG_FWD_BIN(+, a.v + b.v, a.d[i] + b.d[i])
+EG_FWD_BIN(-, a.v - b.v, a.d[i] - b.d[i])
+EG_FWD_BIN(*, a.v * b.v, a.d[i] * b.v + a.v * b.d[i])
+#undef EG_FWD_BIN
+
+template <typename R, int N>
+__host__ __device__ __forceinline__ Fwd<R, N> operator/(const Fwd<R, N>& a, const Fwd<R, N>& b) {
+  Fwd<R, N> r;
+  R ib = R(1) / b.v;
+  r.v = a.v * ib;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = (a.d[i] - r.v * b.d[i]) * ib;
+  return r;
+}
+template <typename R, int N>
+__host__ __device__ __forceinline__ Fwd<R, N> operator-(const Fwd<R, N>& a) {
+  Fwd<R, N> r;
+  r.v = -a.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = -a.d[i];
+  return r;
+}
+// mixed with plain scalars
+template <typename R, int N>
+__host__ __device__ __forceinline__ Fwd<R, N> operator*(const Fwd<R, N>& a, R b) {
+  Fwd<R, N> r;
+  r.v = a.v * b;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * b;
+  return r;
+}
+template <typename R, int N>
+__host__ __device__ __forceinline__ Fwd<R, N> operator*(R b, const Fwd<R, N>& a) { return a * b; }
+template <typename R, int N>
+__host__ __device__ __forceinline__ Fwd<R, N> operator+(const Fwd<R, N>& a, R b) { Fwd<R, N> r = a; r.v = a.v + b; return r; }
+template <typename R, int N>
+__host__ __device__ __forceinline__ Fwd<R, N> operator+(R b, const Fwd<R, N>& a) { Fwd<R, N> r = a; r.v = b + a.v; return r; }
+template <typename R, int N>
+__host__ __device__ __forceinline__ Fwd<R, N> operator-(const Fwd<R, N>& a, R b) { Fwd<R, N> r = a; r.v = a.v - b; return r; }
+template <typename R, int N>
+__host__ __device__ __forceinline__ Fwd<R, N> operator-(R b, const Fwd<R, N>& a) { return Fwd<R, N>(b) - a; }
+template <typename R, int N>
+__host__ __device__ __forceinline__ Fwd<R, N> operator/(const Fwd<R, N>& a, R b) { return a * (R(1) / b); }
+template <typename R, int N>
+__host__ __device__ __forceinline__ Fwd<R, N> operator/(R a, const Fwd<R, N>& b) { return Fwd<R, N>(a) / b; }
+
+template <typename R, int N>
+__host__ __device__ __forceinline__ Fwd<R, N> sqrt(const Fwd<R, N>& a) {
+  Fwd<R, N> r;
+  r.v = ::sqrt(a.v);
+  R h = R(0.5) / r.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * h;
+  return r;
+}
+template <typename R, int N>
+__host__ __device__ __forceinline__ Fwd<R, N> log(const Fwd<R, N>& a) {
+  Fwd<R, N> r;
+  r.v = ::log(a.v);
+  R ia = R(1) / a.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * ia;
+  return r;
+}
+template <typename R, int N>
+__host__ __device__ __forceinline__ Fwd<R, N> absval(const Fwd<R, N>& a) { return a.v < R(0) ? -a : a; }
+template <typename R, int N>
+__host__ __device__ __forceinline__ Fwd<R, N> maxval(const Fwd<R, N>& a, const Fwd<R, N>& b) { return (a.v >= b.v) ? a : b; }
+template <typename R, int N>
+__host__ __device__ __forceinline__ R val(const Fwd<R, N>& a) { return a.v; }
+
+__host__ __device__ __forceinline__ double absval(double a) { return fabs(a); }
+__host__ __device__ __forceinline__ float absval(float a) { return fabsf(a); }
+__host__ __device__ __forceinline__ double maxval(double a, double b) { return fmax(a, b); }
+__host__ __device__ __forceinline__ float maxval(float a, float b) { return fmaxf(a, b); }
+__host__ __device__ __forceinline__ double val(double a) { return a; }
+__host__ __device__ __forceinline__ float val(float a) { return a; }
+using ::sqrt;
+using ::log;
+
+// gas constants as seen by the kernels
+struct Gas {
+  double gamma, gamma_1;
+};
+
+// ---------------------------------------------------------------------------
+template <int DIM, typename T>
+__device__ __forceinline__ T pressure(const Gas& g, const T* q) {
+  if (DIM == 2) return g.gamma_1 * (q[3] - 0.5 * (q[1] * q[1] + q[2] * q[2]) / q[0]);
+  return g.gamma_1 * (q[4] - 0.5 * (q[1] * q[1] + q[2] * q[2] + q[3] * q[3]) / q[0]);
+}
+
+// F . dir for the Euler equations (conservative variables)
+template <int DIM, typename T, typename Tn>
+__device__ __forceinline__ void euler_flux(const Gas& g, const T* q, const Tn* dir, T* F) {
+  T press = pressure<DIM>(g, q);
+  if (DIM == 2) {
+    T U = (q[1] * dir[0] + q[2] * dir[1]) / q[0];
+    F[0] = q[0] * U;
+    F[1] = q[1] * U + dir[0] * press;
+    F[2] = q[2] * U + dir[1] * press;
+    F[3] = (q[3] + press) * U;
+  } else {
+    T U = (q[1] * dir[0] + q[2] * dir[1] + q[3] * dir[2]) / q[0];
+    F[0] = q[0] * U;
+    F[1] = q[1] * U + dir[0] * press;
+    F[2] = q[2] * U + dir[1] * press;
+    F[3] = q[3] * U + dir[2] * press;
+    F[4] = (q[4] + press) * U;
+  }
+}
+
+// Roe flux: F(qL).n + 0.5 (|A_hat| - A_hat)(qL - qR), eigenvalue floors 0.025
+template <int DIM, typename T, typename Tn>
+__device__ __forceinline__ void roe_flux(const Gas& g, const T* q, const T* qg, const Tn* nrm, T* flux) {
+  constexpr int NV = DIM + 2;
+  const double gamma = g.gamma, gami = g.gamma_1;
+  const double sat_V = 0.025;
+  // Roe averages
+  T fac = 1.0 / q[0];
+  T uL = q[1] * fac, vL = q[2] * fac;
+  T wL = (DIM == 3) ? q[3] * fac : T(0.0);
+  T phi = 0.5 * (uL * uL + vL * vL + wL * wL);
+  T HL = gamma * q[NV - 1] * fac - gami * phi;
+  fac = 1.0 / qg[0];
+  T uR = qg[1] * fac, vR = qg[2] * fac;
+  T wR = (DIM == 3) ? qg[3] * fac : T(0.0);
+  phi = 0.5 * (uR * uR + vR * vR + wR * wR);
+  T HR = gamma * qg[NV - 1] * fac - gami * phi;
+  T sqL = sqrt(q[0]);
+  T sqR = sqrt(qg[0]);
+  fac = 1.0 / (sqL + sqR);
+  T u = (sqL * uL + sqR * uR) * fac;
+  T v = (sqL * vL + sqR * vR) * fac;
+  T w = (DIM == 3) ? (sqL * wL + sqR * wR) * fac : T(0.0);
+  T H = (sqL * HL + sqR * HR) * fac;
+  T dq[NV];
+#pragma unroll
+  for (int i = 0; i < NV; ++i) dq[i] = q[i] - qg[i];
+  // SAT
+  Tn nx = nrm[0], ny = nrm[1];
+  Tn nz = (DIM == 3) ? nrm[2] : Tn(0.0);
+  Tn dA = sqrt(nx * nx + ny * ny + nz * nz);
+  T Un = u * nx + v * ny + w * nz;
+  phi = 0.5 * (u * u + v * v + w * w);
+  T a = sqrt(gami * (H - phi));
+  T lambda1 = Un + dA * a;
+  T lambda2 = Un - dA * a;
+  T lambda3 = Un;
+  T rhoA = absval(Un) + dA * a;
+  lambda1 = 0.5 * (maxval(absval(lambda1), sat_V * rhoA) - lambda1);
+  lambda2 = 0.5 * (maxval(absval(lambda2), sat_V * rhoA) - lambda2);
+  lambda3 = 0.5 * (maxval(absval(lambda3), sat_V * rhoA) - lambda3);
+  T dqE, dqN;
+  if (DIM == 2) {
+    dqE = phi * dq[0] - u * dq[1] - v * dq[2] + dq[3];
+    dqN = -Un * dq[0] + nx * dq[1] + ny * dq[2];
+  } else {
+    dqE = phi * dq[0] - u * dq[1] - v * dq[2] - w * dq[3] + dq[4];
+    dqN = -Un * dq[0] + nx * dq[1] + ny * dq[2] + nz * dq[3];
+  }
+  T t1 = 0.5 * (lambda1 + lambda2) - lambda3;
+  T t2 = gami / (a * a);
+  Tn t3 = 1.0 / (dA * dA);
+  T t4 = 0.5 * (lambda1 - lambda2) / (dA * a);
+  // sat = l3 dq + t1 (t2 E1dq + t3 E2dq) + t4 (E3dq + gami E4dq)
+  T c1 = t1 * t2 * dqE + t4 * dqN;        // coefficient of (1, u, v, w, H)
+  T c2 = t1 * t3 * dqN + t4 * gami * dqE; // coefficient of (0, nx, ny, nz, Un)
+  T ef[NV];
+  euler_flux<DIM>(g, q, nrm, ef);
+  flux[0] = ef[0] + lambda3 * dq[0] + c1;
+  flux[1] = ef[1] + lambda3 * dq[1] + c1 * u + c2 * nx;
+  flux[2] = ef[2] + lambda3 * dq[2] + c1 * v + c2 * ny;
+  if (DIM == 3) flux[3] = ef[3] + lambda3 * dq[3] + c1 * w + c2 * nz;
+  flux[NV - 1] = ef[NV - 1] + lambda3 * dq[NV - 1] + c1 * H + c2 * Un;
+}
+
+// logarithmic mean with the 5-term series below u = 1e-3
+template <typename T>
+__device__ __forceinline__ T logavg(const T& aL, const T& aR) {
+  T xi = aL / aR;
+  T f = (xi - 1.0) / (xi + 1.0);
+  T u = f * f;
+  T F;
+  if (val(u) < 1e-3) {
+    F = 1.0 + u * (1.0 / 3.0 + u * (1.0 / 5.0 + u * (1.0 / 7.0 + u * (1.0 / 9.0))));
+  } else {
+    F = (log(xi) * 0.5) / f;
+  }
+  return (aL + aR) / (2.0 * F);
+}
+
+// Ismail-Roe flux: shared averages, then NDIR directions dir[d*DIM + k]
+template <int DIM, typename T>
+struct IRAvg {
+  T rho_hat, u_hat, v_hat, w_hat, p1_hat, h_hat;
+};
+
+template <int DIM, typename T>
+__device__ __forceinline__ IRAvg<DIM, T> ir_average(const Gas& g, const T* qL, const T* qR) {
+  const double gamma = g.gamma, gamma_1 = g.gamma_1;
+  T pL = pressure<DIM>(g, qL), pR = pressure<DIM>(g, qR);
+  T z1L = sqrt(qL[0] / pL), z1R = sqrt(qR[0] / pR);
+  T zpL = sqrt(qL[0] * pL), zpR = sqrt(qR[0] * pR);
+  T iz = 1.0 / (z1L + z1R);
+  IRAvg<DIM, T> r;
+  T lp = logavg(zpL, zpR);
+  r.rho_hat = 0.5 * (z1L + z1R) * lp;
+  r.u_hat = (z1L * qL[1] / qL[0] + z1R * qR[1] / qR[0]) * iz;
+  r.v_hat = (z1L * qL[2] / qL[0] + z1R * qR[2] / qR[0]) * iz;
+  r.w_hat = (DIM == 3) ? (z1L * qL[3] / qL[0] + z1R * qR[3] / qR[0]) * iz : T(0.0);
+  r.p1_hat = (zpL + zpR) * iz;
+  T p2_hat = ((gamma + 1) / (2 * gamma)) * lp / logavg(z1L, z1R) + (gamma_1 / (2 * gamma)) * (zpL + zpR) * iz;
+  r.h_hat = gamma * p2_hat / (r.rho_hat * gamma_1) +
+            0.5 * (r.u_hat * r.u_hat + r.v_hat * r.v_hat + r.w_hat * r.w_hat);
+  return r;
+}
+
+template <int DIM, typename T, typename Tn>
+__device__ __forceinline__ void ir_dir(const IRAvg<DIM, T>& a, const Tn* n, T* F) {
+  constexpr int NV = DIM + 2;
+  Tn nz = (DIM == 3) ? n[2] : Tn(0.0);
+  T mv_n = a.rho_hat * (n[0] * a.u_hat + n[1] * a.v_hat + nz * a.w_hat);
+  F[0] = mv_n;
+  F[1] = mv_n * a.u_hat + n[0] * a.p1_hat;
+  F[2] = mv_n * a.v_hat + n[1] * a.p1_hat;
+  if (DIM == 3) F[3] = mv_n * a.w_hat + nz * a.p1_hat;
+  F[NV - 1] = mv_n * a.h_hat;
+}
+
+}  // namespace eg

@@ -1,0 +1,338 @@
+// eg_residual.cu -- evalResidual on the device.
+//
+// Reference: src/solver/euler/euler.jl:111-175 (evalResidual), with the fused
+// per-element / per-face forms of euler_funcs.jl:158-205
+// (calcVolumeIntegrals_nopre), flux.jl:79-123 (calcFaceIntegral_nopre) and
+// bc.jl:290-329 (calcBoundaryFlux_nopre).
+//
+// Two launches per evaluation:
+//   k_face_flux   one thread per (face, face node): interpolate both sides
+//                 from the stencil (SBP interp/perm/nbrperm), numerical flux
+//                 (Roe / Ismail-Roe; boundary: Roe against the precomputed
+//                 Dirichlet state).  Each interface flux is computed once.
+//   k_element     one thread per (element, node): Euler flux in the
+//                 parametric directions into shared memory, then
+//                 res_j = sum_k sum_i Q_k(i,j) F_k,i (weak form Q^T F) and the
+//                 face terms -(+) sum_i lift_f(j,i) F_face,i for the elementL
+//                 (elementR) side.  No atomics: every residual entry is written
+//                 by exactly one thread, so results are deterministic.
+// The split-form (Hadamard) volume term of volume_integral_type 2 lives in
+// eg_split.cu.
+#include <cstdio>
+
+#include "eg_internal.h"
+#include "eg_kernels.cuh"
+#include "eg_physics.cuh"
+
+using eg::Gas;
+
+namespace {
+
+template <int DIM>
+__global__ void k_face_flux(DevMesh md, const double* __restrict__ q, double* __restrict__ fflux) {
+  constexpr int NV = DIM + 2;
+  const int Nf = md.Nf, S = md.S, Np = md.Np;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (md.I + md.B) * Nf) return;
+  const int slot = t / Nf, i = t - slot * Nf;
+  const Gas g{md.gamma, md.gamma_1};
+  double qL[NV], qR[NV], fl[NV];
+#pragma unroll
+  for (int c = 0; c < NV; ++c) { qL[c] = 0.0; qR[c] = 0.0; }
+  if (slot < md.I) {
+    const int* itf = md.ifaces + 5 * slot;
+    const int eL = itf[0], eR = itf[1], fL = itf[2], fR = itf[3], o = itf[4];
+    const int iR = md.nbrperm[o * Nf + i];
+    const double* cL = md.interp + ((size_t)fL * Nf + i) * S;
+    const double* cR = md.interp + ((size_t)fR * Nf + iR) * S;
+    const int* pL = md.perm + fL * S;
+    const int* pR = md.perm + fR * S;
+    for (int s = 0; s < S; ++s) {
+      const double a = cL[s], b = cR[s];
+      const double* xa = q + ((size_t)eL * Np + pL[s]) * NV;
+      const double* xb = q + ((size_t)eR * Np + pR[s]) * NV;
+#pragma unroll
+      for (int c = 0; c < NV; ++c) {
+        qL[c] = fma(a, xa[c], qL[c]);
+        qR[c] = fma(b, xb[c], qR[c]);
+      }
+    }
+    double nrm[DIM];
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) nrm[k] = md.nrm_face[((size_t)slot * Nf + i) * DIM + k];
+    if (md.face_flux == EG_FLUX_ROE) {
+      eg::roe_flux<DIM>(g, qL, qR, nrm, fl);
+    } else {
+      auto av = eg::ir_average<DIM>(g, qL, qR);
+      eg::ir_dir<DIM>(av, nrm, fl);
+    }
+  } else {
+    const int b = slot - md.I;
+    const int e = md.bfaces[2 * b], f = md.bfaces[2 * b + 1];
+    const double* cL = md.interp + ((size_t)f * Nf + i) * S;
+    const int* pL = md.perm + f * S;
+    for (int s = 0; s < S; ++s) {
+      const double a = cL[s];
+      const double* xa = q + ((size_t)e * Np + pL[s]) * NV;
+#pragma unroll
+      for (int c = 0; c < NV; ++c) qL[c] = fma(a, xa[c], qL[c]);
+    }
+    double nrm[DIM];
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) nrm[k] = md.nrm_bndry[((size_t)b * Nf + i) * DIM + k];
+#pragma unroll
+    for (int c = 0; c < NV; ++c) qR[c] = md.qg_bndry[((size_t)b * Nf + i) * NV + c];
+    eg::roe_flux<DIM>(g, qL, qR, nrm, fl);
+  }
+  double* out = fflux + (size_t)t * NV;
+#pragma unroll
+  for (int c = 0; c < NV; ++c) out[c] = fl[c];
+}
+
+// Shared-memory layout of k_element: Q[dim][Np][Np] | lift[F][Np][Nf] | Fbuf
+template <int DIM>
+__global__ void k_element(DevMesh md, const double* __restrict__ q,
+                          const double* __restrict__ fflux, double* __restrict__ res,
+                          unsigned int* __restrict__ status, int epb) {
+  constexpr int NV = DIM + 2;
+  constexpr int F = DIM + 1;
+  extern __shared__ double smem[];
+  const int Np = md.Np, Nf = md.Nf;
+  double* sQ = smem;
+  double* sL = sQ + DIM * Np * Np;
+  double* sF = sL + F * Np * Nf;
+  for (int k = threadIdx.x; k < DIM * Np * Np; k += blockDim.x) sQ[k] = md.Q[k];
+  for (int k = threadIdx.x; k < F * Np * Nf; k += blockDim.x) sL[k] = md.lift[k];
+  const int le = threadIdx.x / Np, j = threadIdx.x - le * Np;
+  const int e = blockIdx.x * epb + le;
+  const bool active = (le < epb) && (e < md.E);
+  const Gas g{md.gamma, md.gamma_1};
+  double* Fe = sF + (size_t)le * DIM * Np * NV;  // [k][i][c]
+  if (active) {
+    double qj[NV];
+    const double* src = q + ((size_t)e * Np + j) * NV;
+#pragma unroll
+    for (int c = 0; c < NV; ++c) qj[c] = src[c];
+    const double p = eg::pressure<DIM>(g, qj);
+    if (!(qj[0] > 0.0)) atomicOr(status, EG_DEV_NEG_DENSITY);
+    if (!(p > 0.0)) atomicOr(status, EG_DEV_NEG_PRESSURE);
+    const double* dx = md.dxidx + ((size_t)e * Np + j) * DIM * DIM;  // [p(x)][k(xi)]
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+      double dir[DIM];
+#pragma unroll
+      for (int pp = 0; pp < DIM; ++pp) dir[pp] = dx[pp * DIM + k];
+      eg::euler_flux<DIM>(g, qj, dir, Fe + ((size_t)k * Np + j) * NV);
+    }
+  }
+  __syncthreads();
+  if (!active) return;
+  double acc[NV];
+#pragma unroll
+  for (int c = 0; c < NV; ++c) acc[c] = 0.0;
+  // volume: (Q_k^T F_k)_j = sum_i Q_k(i, j) F_k,i ; sQ[k][j][i] = Q_k(i, j)
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) {
+    const double* qrow = sQ + ((size_t)k * Np + j) * Np;
+    const double* Fk = Fe + (size_t)k * Np * NV;
+    for (int i = 0; i < Np; ++i) {
+      const double a = qrow[i];
+#pragma unroll
+      for (int c = 0; c < NV; ++c) acc[c] = fma(a, Fk[i * NV + c], acc[c]);
+    }
+  }
+  // faces: elementL side subtracts, elementR side adds (SBP face integrate)
+#pragma unroll
+  for (int f = 0; f < F; ++f) {
+    const EFace ef = md.eface[(size_t)e * F + f];
+    const double* fl = fflux + (size_t)ef.slot * Nf * NV;
+    const double* lrow = sL + ((size_t)f * Np + j) * Nf;
+    if (ef.side == 0) {
+      for (int i = 0; i < Nf; ++i) {
+        const double a = -lrow[i];
+#pragma unroll
+        for (int c = 0; c < NV; ++c) acc[c] = fma(a, fl[i * NV + c], acc[c]);
+      }
+    } else {
+      const int* nb = md.nbrperm + ef.orient * Nf;
+      for (int i = 0; i < Nf; ++i) {
+        const double a = lrow[nb[i]];
+#pragma unroll
+        for (int c = 0; c < NV; ++c) acc[c] = fma(a, fl[i * NV + c], acc[c]);
+      }
+    }
+  }
+  double* dst = res + ((size_t)e * Np + j) * NV;
+#pragma unroll
+  for (int c = 0; c < NV; ++c) dst[c] = acc[c];
+}
+
+// sum of r^2 * M^{+-1} per block, then one block reduces the partials in a
+// fixed order (deterministic).
+template <int NT>
+__global__ void k_norm_partial(const double* __restrict__ r, const double* __restrict__ Minv,
+                               int64_t nnode, int nv, int strongres, double* __restrict__ part) {
+  __shared__ double sh[NT];
+  double s = 0.0;
+  for (int64_t n = blockIdx.x * (int64_t)NT + threadIdx.x; n < nnode; n += (int64_t)gridDim.x * NT) {
+    const double mi = Minv[n];
+    const double fac = strongres ? mi : 1.0 / mi;
+    double t = 0.0;
+    for (int c = 0; c < nv; ++c) {
+      const double x = r[n * nv + c];
+      t = fma(x, x, t);
+    }
+    s = fma(t, fac, s);
+  }
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = NT / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+template <int NT>
+__global__ void k_norm_final(const double* __restrict__ part, int n, double* __restrict__ out) {
+  __shared__ double sh[NT];
+  double s = 0.0;
+  for (int k = threadIdx.x; k < n; k += NT) s += part[k];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = NT / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[0] = sqrt(sh[0]);
+}
+
+}  // namespace
+
+DevMesh dev_mesh(const eg_mesh* m) {
+  DevMesh d;
+  d.E = m->E; d.Np = m->Np; d.Nf = m->Nf; d.S = m->S; d.I = m->I; d.B = m->B;
+  d.gamma = m->dp.gamma; d.gamma_1 = m->dp.gamma_1;
+  d.face_flux = m->params.face_flux;
+  d.Q = m->Q; d.interp = m->interp; d.perm = m->perm; d.nbrperm = m->nbrperm;
+  d.lift = m->lift; d.dxidx = m->dxidx; d.ifaces = m->ifaces; d.nrm_face = m->nrm_face;
+  d.bfaces = m->bfaces; d.nrm_bndry = m->nrm_bndry; d.qg_bndry = m->qg_bndry;
+  d.eface = m->eface; d.Minv = m->Minv; d.w = m->w; d.jac = m->jac;
+  return d;
+}
+
+int element_launch_shape(const eg_mesh* m, int* epb, int* threads, size_t* smem) {
+  const int nv = m->nv;
+  int e = 256 / m->Np;
+  if (e < 1) e = 1;
+  *epb = e;
+  *threads = e * m->Np;
+  *smem = sizeof(double) * ((size_t)m->dim * m->Np * m->Np + (size_t)m->F * m->Np * m->Nf +
+                            (size_t)e * m->dim * m->Np * nv);
+  return EG_OK;
+}
+
+int eg_launch_residual(eg_mesh* m, const double* q, double* res) {
+  DevMesh md = dev_mesh(m);
+  const int nf_threads = (m->I + m->B) * m->Nf;
+  if (nf_threads > 0) {
+    const int nt = 128;
+    eg_phase_begin(m, EG_PHASE_FACE);
+    if (m->dim == 2)
+      k_face_flux<2><<<(nf_threads + nt - 1) / nt, nt, 0, m->stream>>>(md, q, m->fflux);
+    else
+      k_face_flux<3><<<(nf_threads + nt - 1) / nt, nt, 0, m->stream>>>(md, q, m->fflux);
+    eg_phase_end(m, EG_PHASE_FACE, 1);
+  }
+  eg_phase_begin(m, EG_PHASE_ELEMENT);
+  if (m->params.volume_integral_type == 2) {
+    int st = eg_launch_split_element(m, q, res);
+    eg_phase_end(m, EG_PHASE_ELEMENT, 1);
+    return st;
+  }
+  int epb, threads;
+  size_t smem;
+  element_launch_shape(m, &epb, &threads, &smem);
+  const int blocks = (m->E + epb - 1) / epb;
+  if (m->dim == 2)
+    k_element<2><<<blocks, threads, smem, m->stream>>>(md, q, m->fflux, res, m->status, epb);
+  else
+    k_element<3><<<blocks, threads, smem, m->stream>>>(md, q, m->fflux, res, m->status, epb);
+  eg_phase_end(m, EG_PHASE_ELEMENT, 1);
+  return EG_OK;
+}
+
+int eg_launch_norm(eg_mesh* m, const double* r, int strongres, double* out_dev) {
+  const int64_t nnode = (int64_t)m->E * m->Np;
+  int blocks = (int)((nnode + 255) / 256);
+  if (blocks > 1024) blocks = 1024;
+  eg_phase_begin(m, EG_PHASE_NORM);
+  k_norm_partial<256><<<blocks, 256, 0, m->stream>>>(r, m->Minv, nnode, m->nv, strongres, m->red);
+  k_norm_final<256><<<1, 256, 0, m->stream>>>(m->red, blocks, out_dev);
+  eg_phase_end(m, EG_PHASE_NORM, 2);
+  return EG_OK;
+}
+
+int eg_check_status(eg_mesh* m) {
+  unsigned int s = *m->h_status;
+  if (s & EG_DEV_NEG_DENSITY) {
+    eg_set_error("negative density");
+    return EG_ERR_NEG_DENSITY;
+  }
+  if (s & EG_DEV_NEG_PRESSURE) {
+    eg_set_error("negative pressure");
+    return EG_ERR_NEG_PRESSURE;
+  }
+  if (s & EG_DEV_NONFINITE) {
+    eg_set_error("non-finite value");
+    return EG_ERR_NONFINITE;
+  }
+  if (s & EG_DEV_LU_PIVOT) {
+    eg_set_error("zero pivot in block LU");
+    return EG_ERR_LU_PIVOT;
+  }
+  return EG_OK;
+}
+
+extern "C" int eg_eval_residual(eg_mesh* m, const double* q, double* res, double t, int32_t mem) {
+  (void)t;  // the implemented boundary states are time-independent
+  if (!m || !q || !res) {
+    eg_set_error("eg_eval_residual: NULL argument");
+    return EG_ERR_INVALID;
+  }
+  const size_t bytes = sizeof(double) * (size_t)m->ndof;
+  const double* qd = q;
+  double* rd = res;
+  if (mem == EG_MEM_HOST) {
+    EG_CUDA(cudaMemcpyAsync(m->q_dev, q, bytes, cudaMemcpyHostToDevice, m->stream));
+    qd = m->q_dev;
+    rd = m->res_dev;
+  }
+  EG_CUDA(cudaMemsetAsync(m->status, 0, sizeof(unsigned int), m->stream));
+  int st = eg_launch_residual(m, qd, rd);
+  if (st != EG_OK) return st;
+  EG_CUDA(cudaGetLastError());
+  EG_CUDA(cudaMemcpyAsync(m->h_status, m->status, sizeof(unsigned int), cudaMemcpyDeviceToHost, m->stream));
+  if (mem == EG_MEM_HOST)
+    EG_CUDA(cudaMemcpyAsync(res, rd, bytes, cudaMemcpyDeviceToHost, m->stream));
+  EG_CUDA(cudaStreamSynchronize(m->stream));
+  return eg_check_status(m);
+}
+
+extern "C" int eg_calc_norm(eg_mesh* m, const double* r, int32_t strongres, int32_t mem, double* out) {
+  if (!m || !r || !out) {
+    eg_set_error("eg_calc_norm: NULL argument");
+    return EG_ERR_INVALID;
+  }
+  const double* rd = r;
+  if (mem == EG_MEM_HOST) {
+    EG_CUDA(cudaMemcpyAsync(m->res_dev, r, sizeof(double) * (size_t)m->ndof, cudaMemcpyHostToDevice, m->stream));
+    rd = m->res_dev;
+  }
+  eg_launch_norm(m, rd, strongres, m->red + 2048);
+  EG_CUDA(cudaGetLastError());
+  EG_CUDA(cudaMemcpyAsync(m->h_red, m->red + 2048, sizeof(double), cudaMemcpyDeviceToHost, m->stream));
+  EG_CUDA(cudaStreamSynchronize(m->stream));
+  *out = m->h_red[0];
+  return EG_OK;
+}

@@ -1,0 +1,157 @@
+// eg_split.cu -- entropy-conservative Hadamard split-form volume integral.
+//
+// Reference: calcVolumeIntegralsSplitFormCurvilinear
+// (src/solver/euler/euler_funcs.jl:295-362) with calcSCurvilinear
+// (src/Utils/curvilinear.jl:17-41):
+//   S_x[j,k,d] = 1/2 sum_m (dxidx[m,d,j] Q_m(j,k) - dxidx[m,d,k] Q_m(k,j))
+//   res_j -= 2 sum_d S_x[j,k,d] F_IR,d(q_j, q_k),  res_k += same   (k < j)
+// The IR flux is linear in its direction, so sum_d S_x[j,k,d] F_IR,d equals
+// one IR flux in the direction n_jk = S_x[j,k,:]; each pair (j,k) costs one
+// Ismail-Roe average and one projection.
+//
+// k_split_element: a CTA owns `epb` elements.  Phase 1: all threads walk the
+// element pairs, writing G_jk = 2 F_IR(q_j, q_k; n_jk) to shared memory.
+// Phase 2: thread (element, j) sums its row with the antisymmetry signs, adds
+// the face terms (same lift as the weak form) and writes res_j once.
+#include "eg_internal.h"
+#include "eg_kernels.cuh"
+#include "eg_physics.cuh"
+
+using eg::Gas;
+
+namespace {
+
+template <int DIM>
+__global__ void k_split_element(DevMesh md, const double* __restrict__ q,
+                                const double* __restrict__ fflux, double* __restrict__ res,
+                                unsigned int* __restrict__ status, int epb) {
+  constexpr int NV = DIM + 2;
+  constexpr int F = DIM + 1;
+  extern __shared__ double smem[];
+  const int Np = md.Np, Nf = md.Nf;
+  const int P = Np * (Np - 1) / 2;
+  double* sQ = smem;                          // [DIM][Np][Np]
+  double* sL = sQ + DIM * Np * Np;            // [F][Np][Nf]
+  double* sq = sL + F * Np * Nf;              // [epb][Np][NV]
+  double* sG = sq + (size_t)epb * Np * NV;    // [epb][P][NV]
+  short2* sPair = reinterpret_cast<short2*>(sG + (size_t)epb * P * NV);  // [P]
+  for (int k = threadIdx.x; k < DIM * Np * Np; k += blockDim.x) sQ[k] = md.Q[k];
+  for (int k = threadIdx.x; k < F * Np * Nf; k += blockDim.x) sL[k] = md.lift[k];
+  for (int j = threadIdx.x; j < Np; j += blockDim.x)
+    for (int k = 0; k < j; ++k) sPair[j * (j - 1) / 2 + k] = make_short2((short)j, (short)k);
+  const int e0 = blockIdx.x * epb;
+  const int nloc = min(epb, md.E - e0);
+  for (int t = threadIdx.x; t < nloc * Np * NV; t += blockDim.x)
+    sq[t] = q[(size_t)e0 * Np * NV + t];
+  __syncthreads();
+  const Gas g{md.gamma, md.gamma_1};
+  // ---- phase 1: pair fluxes
+  for (int t = threadIdx.x; t < nloc * P; t += blockDim.x) {
+    const int le = t / P, pidx = t - le * P;
+    const short2 jk = sPair[pidx];
+    const int j = jk.x, k = jk.y;
+    const int e = e0 + le;
+    const double* dxj = md.dxidx + ((size_t)e * Np + j) * DIM * DIM;  // [x][xi]
+    const double* dxk = md.dxidx + ((size_t)e * Np + k) * DIM * DIM;
+    double n[DIM];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      double s = 0.0;
+#pragma unroll
+      for (int m = 0; m < DIM; ++m) {
+        // Q_m(j,k) = sQ[m][k][j]; Q_m(k,j) = sQ[m][j][k]
+        s = fma(dxj[d * DIM + m], sQ[((size_t)m * Np + k) * Np + j], s);
+        s = fma(-dxk[d * DIM + m], sQ[((size_t)m * Np + j) * Np + k], s);
+      }
+      n[d] = s;  // 2 * S_x[j,k,d]
+    }
+    const double* qj = sq + ((size_t)le * Np + j) * NV;
+    const double* qk = sq + ((size_t)le * Np + k) * NV;
+    auto av = eg::ir_average<DIM>(g, qj, qk);
+    double Fp[NV];
+    eg::ir_dir<DIM>(av, n, Fp);
+    double* G = sG + ((size_t)le * P + pidx) * NV;
+#pragma unroll
+    for (int c = 0; c < NV; ++c) G[c] = Fp[c];
+  }
+  __syncthreads();
+  // ---- phase 2: rows + faces
+  const int le = threadIdx.x / Np, j = threadIdx.x - le * Np;
+  const int e = e0 + le;
+  if (le >= epb || e >= md.E) return;
+  const double* qj = sq + ((size_t)le * Np + j) * NV;
+  const double pj = eg::pressure<DIM>(g, qj);
+  if (!(qj[0] > 0.0)) atomicOr(status, EG_DEV_NEG_DENSITY);
+  if (!(pj > 0.0)) atomicOr(status, EG_DEV_NEG_PRESSURE);
+  double acc[NV];
+#pragma unroll
+  for (int c = 0; c < NV; ++c) acc[c] = 0.0;
+  const double* Ge = sG + (size_t)le * P * NV;
+  for (int k = 0; k < j; ++k) {          // pair (j, k): res_j -= G
+    const double* G = Ge + (size_t)(j * (j - 1) / 2 + k) * NV;
+#pragma unroll
+    for (int c = 0; c < NV; ++c) acc[c] -= G[c];
+  }
+  for (int k = j + 1; k < Np; ++k) {     // pair (k, j): res_j += G
+    const double* G = Ge + (size_t)(k * (k - 1) / 2 + j) * NV;
+#pragma unroll
+    for (int c = 0; c < NV; ++c) acc[c] += G[c];
+  }
+#pragma unroll
+  for (int f = 0; f < F; ++f) {
+    const EFace ef = md.eface[(size_t)e * F + f];
+    const double* fl = fflux + (size_t)ef.slot * Nf * NV;
+    const double* lrow = sL + ((size_t)f * Np + j) * Nf;
+    if (ef.side == 0) {
+      for (int i = 0; i < Nf; ++i) {
+        const double a = -lrow[i];
+#pragma unroll
+        for (int c = 0; c < NV; ++c) acc[c] = fma(a, fl[i * NV + c], acc[c]);
+      }
+    } else {
+      const int* nb = md.nbrperm + ef.orient * Nf;
+      for (int i = 0; i < Nf; ++i) {
+        const double a = lrow[nb[i]];
+#pragma unroll
+        for (int c = 0; c < NV; ++c) acc[c] = fma(a, fl[i * NV + c], acc[c]);
+      }
+    }
+  }
+  double* dst = res + ((size_t)e * Np + j) * NV;
+#pragma unroll
+  for (int c = 0; c < NV; ++c) dst[c] = acc[c];
+}
+
+}  // namespace
+
+int eg_launch_split_element(eg_mesh* m, const double* q, double* res) {
+  DevMesh md = dev_mesh(m);
+  const int Np = m->Np, nv = m->nv;
+  const int P = Np * (Np - 1) / 2;
+  int epb = 256 / Np;
+  if (epb < 1) epb = 1;
+  auto smem_of = [&](int e) {
+    return sizeof(double) * ((size_t)m->dim * Np * Np + (size_t)m->F * Np * m->Nf +
+                             (size_t)e * Np * nv + (size_t)e * P * nv) +
+           sizeof(short2) * (size_t)P;
+  };
+  while (epb > 1 && smem_of(epb) > 160 * 1024) --epb;
+  const size_t smem = smem_of(epb);
+  const int threads = epb * Np;
+  const int blocks = (m->E + epb - 1) / epb;
+  static bool attr_set[4] = {false, false, false, false};
+  if (m->dim == 2) {
+    if (!attr_set[2]) {
+      cudaFuncSetAttribute(k_split_element<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+      attr_set[2] = true;
+    }
+    k_split_element<2><<<blocks, threads, smem, m->stream>>>(md, q, m->fflux, res, m->status, epb);
+  } else {
+    if (!attr_set[3]) {
+      cudaFuncSetAttribute(k_split_element<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+      attr_set[3] = true;
+    }
+    k_split_element<3><<<blocks, threads, smem, m->stream>>>(md, q, m->fflux, res, m->status, epb);
+  }
+  return EG_OK;
+}

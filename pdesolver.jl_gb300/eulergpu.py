@@ -1,0 +1,200 @@
+"""Python mirror of the reference's physics-module interface over the C ABI.
+
+The reference's Euler module is driven through
+
+* ``evalResidual(mesh, sbp, eqn, opts, t)``  (src/solver/euler/euler.jl:111)
+* ``evalJacobian(mesh, sbp, eqn, opts, assembler, t)`` (evalJacobian.jl:6)
+* ``calcNorm(eqn, res_vec; strongres)``      (src/Utils/Utils.jl:427)
+
+Here ``mesh`` is a :class:`pdesolver_gb300.mesh.Mesh`, ``sbp`` its operator,
+``eqn`` an :class:`EulerData` holding ``q``/``res`` in the reference layout
+(``q[E, Np, nv]`` row-major == Julia ``q[nv, Np, E]``) and ``opts`` a dict with
+the reference's option keys.  Every call goes to libeulergpu.so; there is no
+CPU fallback: if the library is missing or no GPU is visible the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+
+_LIB = None
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libeulergpu.so")
+
+
+class EulerGPUError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{abi.STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+def library():
+    """Load the in-tree libeulergpu.so (built by build.py); raise if absent."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"libeulergpu.so not built ({LIB_PATH}); run the build step")
+        lib = C.CDLL(LIB_PATH)
+        _declare(lib)
+        _LIB = lib
+    return _LIB
+
+
+def _declare(lib):
+    vp = C.c_void_p
+    dp = C.POINTER(C.c_double)
+    lib.eg_version.restype = C.c_int
+    lib.eg_last_error.restype = C.c_char_p
+    lib.eg_mesh_create.argtypes = [C.POINTER(abi.EgMeshDesc), C.POINTER(abi.EgParams), C.POINTER(vp)]
+    lib.eg_mesh_destroy.argtypes = [vp]
+    lib.eg_mesh_num_dof.argtypes = [vp]
+    lib.eg_mesh_num_dof.restype = C.c_int64
+    lib.eg_eval_residual.argtypes = [vp, vp, vp, C.c_double, C.c_int32]
+    lib.eg_calc_norm.argtypes = [vp, vp, C.c_int32, C.c_int32, dp]
+    lib.eg_mesh_set_stream.argtypes = [vp, vp]
+    lib.eg_eval_residual_async.argtypes = [vp, vp, vp]
+    lib.eg_sync.argtypes = [vp]
+    lib.eg_set_timing.argtypes = [vp, C.c_int32]
+    lib.eg_get_timings.argtypes = [vp, C.POINTER(Timings)]
+    lib.eg_reset_timings.argtypes = [vp]
+
+
+class Timings(C.Structure):
+    """eg_timings: per-phase device milliseconds (reference Timings buckets)."""
+    _fields_ = [("t_face_flux", C.c_double), ("t_element", C.c_double), ("t_norm", C.c_double),
+                ("t_other", C.c_double), ("launches", C.c_int64), ("timed", C.c_int64)]
+
+
+def check(status):
+    if status != abi.EG_OK:
+        raise EulerGPUError(status, library().eg_last_error().decode())
+
+
+FLUX_NAMES = {"RoeFlux": abi.EG_FLUX_ROE, "IRFlux": abi.EG_FLUX_IR}
+
+
+def params_from_opts(opts: dict) -> abi.EgParams:
+    """Translate reference option keys (read_input.jl) into eg_params."""
+    return abi.EgParams.make(
+        gamma=opts.get("gamma", 1.4), Ma=opts.get("Ma", 0.5), aoa_deg=opts.get("aoa", 0.0),
+        M_in=opts.get("vortex_M_in", 0.5),
+        face_flux=FLUX_NAMES[opts.get("Flux_name", "RoeFlux")],
+        volume_integral_type=opts.get("volume_integral_type", 1),
+        volume_flux=FLUX_NAMES[opts.get("Volume_flux_name", "IRFlux")],
+        p_free=opts.get("p_free"))
+
+
+class GPUMesh:
+    """Owner of one eg_mesh (device copy of mesh + operator + parameters)."""
+
+    def __init__(self, mesh, opts: dict):
+        self.lib = library()
+        self.mesh = mesh
+        self.opts = dict(opts)
+        self.desc = abi.MeshDesc(mesh)
+        self.params = params_from_opts(opts)
+        h = C.c_void_p()
+        check(self.lib.eg_mesh_create(C.byref(self.desc.desc), C.byref(self.params), C.byref(h)))
+        self.handle = h
+        self.ndof = int(self.lib.eg_mesh_num_dof(h))
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.eg_mesh_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- array helpers -----------------------------------------------------
+    @staticmethod
+    def _ptr(a):
+        """(pointer, mem flag) of a numpy array (host) or a CUDA tensor."""
+        if isinstance(a, np.ndarray):
+            if not (a.flags.c_contiguous and a.dtype == np.float64):
+                raise ValueError("expected a C-contiguous float64 array")
+            return C.c_void_p(a.ctypes.data), abi.EG_MEM_HOST
+        # torch tensor on the device
+        if a.dtype.__repr__() != "torch.float64" or not a.is_contiguous():
+            raise ValueError("expected a contiguous float64 tensor")
+        if a.device.type != "cuda":
+            return C.c_void_p(a.data_ptr()), abi.EG_MEM_HOST
+        return C.c_void_p(a.data_ptr()), abi.EG_MEM_DEVICE
+
+    def eval_residual(self, q, res, t=0.0):
+        pq, mq = self._ptr(q)
+        pr, mr = self._ptr(res)
+        if mq != mr:
+            raise ValueError("q and res must both be host or both be device arrays")
+        check(self.lib.eg_eval_residual(self.handle, pq, pr, t, mq))
+        return res
+
+    def set_stream(self, stream_handle):
+        """run this mesh's work on a caller's CUDA stream (int handle; 0 = own)."""
+        check(self.lib.eg_mesh_set_stream(self.handle, C.c_void_p(stream_handle or None)))
+
+    def eval_residual_async(self, q_dev, res_dev):
+        """enqueue R(q) with device tensors, no host synchronisation."""
+        check(self.lib.eg_eval_residual_async(self.handle, C.c_void_p(q_dev.data_ptr()),
+                                              C.c_void_p(res_dev.data_ptr())))
+
+    def sync(self):
+        check(self.lib.eg_sync(self.handle))
+
+    def set_timing(self, on=True):
+        check(self.lib.eg_set_timing(self.handle, int(on)))
+
+    def timings(self):
+        t = Timings()
+        check(self.lib.eg_get_timings(self.handle, C.byref(t)))
+        return t
+
+    def reset_timings(self):
+        check(self.lib.eg_reset_timings(self.handle))
+
+    def calc_norm(self, r, strongres=True):
+        pr, mr = self._ptr(r)
+        out = C.c_double()
+        check(self.lib.eg_calc_norm(self.handle, pr, int(strongres), mr, C.byref(out)))
+        return out.value
+
+
+class EulerData:
+    """The fields of the reference's EulerData the hot path touches."""
+
+    def __init__(self, mesh, opts):
+        self.q = np.zeros((mesh.numEl, mesh.numNodesPerElement, mesh.numDofPerNode))
+        self.res = np.zeros_like(self.q)
+        self.M = np.repeat(mesh.M[:, :, None], mesh.numDofPerNode, axis=2)
+        self.Minv = 1.0 / self.M
+        self.gpu = GPUMesh(mesh, opts)
+
+    @property
+    def q_vec(self):
+        return self.q.reshape(-1)
+
+    @property
+    def res_vec(self):
+        return self.res.reshape(-1)
+
+
+def createObjects(mesh, opts):
+    """(mesh, sbp, eqn, opts) tuple as the reference's createObjects returns."""
+    return mesh, mesh.sbp, EulerData(mesh, opts), opts
+
+
+def evalResidual(mesh, sbp, eqn, opts, t=0.0):
+    """eqn.res <- R(eqn.q) on the GPU (weak form; reference euler.jl:111)."""
+    eqn.gpu.eval_residual(eqn.q, eqn.res, t)
+
+
+def calcNorm(eqn, res_vec, strongres=False):
+    """SBP norm of a residual vector (reference Utils.jl:427)."""
+    r = np.ascontiguousarray(np.asarray(res_vec, dtype=np.float64).reshape(eqn.q.shape))
+    return eqn.gpu.calc_norm(r, strongres)

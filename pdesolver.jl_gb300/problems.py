@@ -1,0 +1,90 @@
+"""The synthetic workloads the hot path is measured on (seeded).
+
+* ``config1``: FP64 isentropic vortex, quarter annulus r in [1,3],
+  16x16 (r, theta) quads split into 512 triangles, SBP-Omega p=2, Roe faces,
+  vortex (rho_in = 2, M_in = 0.5) as state and Dirichlet data; state =
+  vortex * (1 + N(0, 1e-3)) with seed 1.
+* ``config2``: same annulus at 64x64 (8192 triangles), SBP-Gamma p=3, Roe;
+  start = free stream (rho 1, Ma = 0.5, aoa 0) * (1 + U(-0.01, 0.01)), seed 2.
+* ``config3``: unit cube 24^3 hexes -> 6 tets each (82,944), warped, SBP
+  diagonal-E p=2 tets, Ismail-Roe split-form volume and IR faces, Mach 0.5
+  free stream with density * (1 + N(0, 0.01)), seed 4.
+
+Initial/boundary states restate the reference's calcIsentropicVortex
+(src/solver/euler/common_funcs.jl:25-79, with M_in a parameter) and
+calcFreeStream (common_funcs.jl:312-345).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import mesh as _mesh
+from . import sbp as _sbp
+
+R_GAS = 287.058   # read_input.jl:141
+
+
+def vortex_state(coords, gamma=1.4, M_in=0.5, r_in=1.0, rho_in=2.0):
+    x, y = coords[..., 0], coords[..., 1]
+    r = np.sqrt(x * x + y * y)
+    theta = np.arctan2(y, x)
+    tmp1 = ((gamma - 1) / 2) * M_in * M_in
+    rho = rho_in * (1 + tmp1 * (1 - (r_in * r_in) / (r * r))) ** (1 / (gamma - 1))
+    p = (1 / gamma) * (rho / rho_in) ** gamma
+    a = np.sqrt(gamma * p / rho)
+    M = np.sqrt((2 / (gamma - 1)) * (rho_in / rho) ** (gamma - 1) * (1 + tmp1) - 2 / (gamma - 1))
+    U = M * a
+    cv = R_GAS / (gamma - 1)
+    e = cv * p / (rho * R_GAS)
+    q = np.zeros(coords.shape[:-1] + (4,))
+    q[..., 0] = rho
+    q[..., 1] = rho * (U * np.sin(theta))
+    q[..., 2] = rho * (-U * np.cos(theta))
+    q[..., 3] = rho * e + 0.5 * rho * U * U
+    return q
+
+
+def free_stream(dim, shape, gamma=1.4, Ma=0.5, aoa=0.0, rho=1.0, p_free=None):
+    p_free = 1.0 / gamma if p_free is None else p_free
+    q = np.zeros(shape + (dim + 2,))
+    q[..., 0] = rho
+    q[..., 1] = rho * Ma * np.cos(aoa)
+    if dim == 2:
+        q[..., 2] = rho * Ma * np.sin(aoa)
+    else:
+        q[..., 3] = -rho * Ma * np.sin(aoa)
+    q[..., dim + 1] = p_free / (gamma - 1) + 0.5 * rho * Ma * Ma
+    return q
+
+
+def config1(n=16, p=2, family="omega", seed=1):
+    op = _sbp.get_operator(2, family, p)
+    ms = _mesh.annulus(op, n, n, bc=_mesh.BC_VORTEX)
+    opts = {"gamma": 1.4, "Ma": 0.5, "aoa": 0.0, "vortex_M_in": 0.5, "Flux_name": "RoeFlux",
+            "volume_integral_type": 1}
+    rng = np.random.default_rng(seed)
+    q = vortex_state(ms.coords, M_in=0.5)
+    q = q * (1.0 + rng.normal(0.0, 1e-3, size=q.shape))
+    return ms, opts, np.ascontiguousarray(q)
+
+
+def config2(n=64, p=3, family="gamma", seed=2, M_in=0.5):
+    op = _sbp.get_operator(2, family, p)
+    ms = _mesh.annulus(op, n, n, bc=_mesh.BC_VORTEX)
+    opts = {"gamma": 1.4, "Ma": M_in, "aoa": 0.0, "vortex_M_in": M_in, "Flux_name": "RoeFlux",
+            "volume_integral_type": 1}
+    rng = np.random.default_rng(seed)
+    q = free_stream(2, ms.coords.shape[:2], Ma=M_in)
+    q = q * (1.0 + rng.uniform(-0.01, 0.01, size=q.shape))
+    return ms, opts, np.ascontiguousarray(q)
+
+
+def config3(n=24, p=2, seed=4, warp=0.05, warp_seed=3):
+    op = _sbp.get_operator(3, "diage", p)
+    ms = _mesh.cube(op, n, warp=warp, seed=warp_seed, bc=_mesh.BC_FREESTREAM)
+    opts = {"gamma": 1.4, "Ma": 0.5, "aoa": 0.0, "Flux_name": "IRFlux",
+            "volume_integral_type": 2, "Volume_flux_name": "IRFlux"}
+    rng = np.random.default_rng(seed)
+    q = free_stream(3, ms.coords.shape[:2], Ma=0.5)
+    q[..., 0] *= 1.0 + rng.normal(0.0, 0.01, size=q.shape[:2])
+    return ms, opts, np.ascontiguousarray(q)

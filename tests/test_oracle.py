@@ -1,0 +1,236 @@
+"""Known-answer tests pinning the CPU oracle to the reference's own tests.
+
+Each case restates a check from PDESolver.jl's test suite (file:line in the
+test names' docstrings) against the oracle's C++ point functions and
+residual.  CPU only.
+"""
+import ctypes as C
+import math
+
+import numpy as np
+import pytest
+
+from pdesolver_gb300 import abi, mesh, problems, sbp
+from conftest import oracle_residual
+
+
+def _p(**kw):
+    return abi.EgParams.make(**kw)
+
+
+def _flux(oracle, fn, dim, *args):
+    P = _p()
+    F = np.zeros(dim + 2)
+    arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in args]
+    getattr(oracle, fn)(C.byref(P), dim, *[abi.dptr(a) for a in arrs], abi.dptr(F))
+    return F
+
+
+def roe(oracle, qL, qR, n):
+    return _flux(oracle, "oracle_roe_flux", len(n), qL, qR, n)
+
+
+def euler(oracle, q, n):
+    return _flux(oracle, "oracle_euler_flux", len(n), q, n)
+
+
+def ir(oracle, qL, qR, n):
+    P = _p()
+    dim = len(n)
+    F = np.zeros(dim + 2)
+    a, b, d = (np.ascontiguousarray(x, dtype=np.float64) for x in (qL, qR, n))
+    oracle.oracle_ir_flux(C.byref(P), dim, abi.dptr(a), abi.dptr(b), abi.dptr(d), 1, abi.dptr(F))
+    return F
+
+
+def test_pressure_and_euler_flux(oracle):
+    """test/euler/test_lowlevel.jl:509-516: p([1,2,3,7]) = 0.2 and the Euler
+    flux in direction [1,0] is [2, 4.2, 6, 14.4] (atol 1e-14)."""
+    P = _p()
+    q = np.array([1.0, 2.0, 3.0, 7.0])
+    assert math.isclose(oracle.oracle_pressure(C.byref(P), 2, abi.dptr(q)), 0.2, rel_tol=1e-14)
+    np.testing.assert_allclose(euler(oracle, q, [1.0, 0.0]), [2.0, 4.2, 6.0, 14.4], atol=1e-14)
+
+
+def test_isentropic_vortex_known_answer(oracle):
+    """test/euler/test_lowlevel.jl:644-649: vortex at (1,0) with the
+    reference's inner Mach 0.95 is [2.000, 0.000, -1.3435, 2.236960] (1e-4)."""
+    P = _p(M_in=0.95)
+    x = np.array([1.0, 0.0])
+    q = np.zeros(4)
+    oracle.oracle_vortex(C.byref(P), abi.dptr(x), abi.dptr(q))
+    np.testing.assert_allclose(q, [2.0, 0.0, -1.3435, 2.236960], atol=1e-4)
+
+
+def test_roe_consistency(oracle):
+    """test/euler/test_lowlevel.jl:547-614: Roe(q, q) equals the Euler flux,
+    including at the exact vortex state used as boundary data."""
+    rng = np.random.default_rng(0)
+    q = np.array([1.0, 2.0, 3.0, 7.0])
+    for _ in range(5):
+        n = rng.normal(size=2)
+        np.testing.assert_allclose(roe(oracle, q, q, n), euler(oracle, q, n), rtol=1e-14, atol=1e-14)
+    P = _p(M_in=0.95)
+    qv = np.zeros(4)
+    oracle.oracle_vortex(C.byref(P), abi.dptr(np.array([1.0, 0.0])), abi.dptr(qv))
+    n = np.array([0.3, -0.7])
+    np.testing.assert_allclose(roe(oracle, qv, qv, n), euler(oracle, qv, n), rtol=1e-13, atol=1e-14)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_roe_upwinding_and_antisymmetry(oracle, dim):
+    """test/euler/test_flux.jl:314-365: supersonic states upwind fully, the
+    flux is antisymmetric under (qL, qR, n) -> (qR, qL, -n) (atol 1e-13),
+    also with an indefinite flux Jacobian."""
+    if dim == 2:
+        qL, n = np.array([1.0, 2.0, 3.0, 7.0]), np.array([1.0, 0.0])
+    else:
+        qL, n = np.array([1.0, 2.0, 3.0, 4.0, 15.0]), np.array([1.0, 0.0, 0.0])
+    qR = qL + 1
+    assert np.linalg.norm(roe(oracle, qL, qR, n) - euler(oracle, qL, n)) < 1e-13
+    f = roe(oracle, qR, qL, n)
+    assert np.linalg.norm(f - euler(oracle, qR, n)) < 1e-13
+    assert np.linalg.norm(f + roe(oracle, qL, qR, -n)) < 1e-13
+    if dim == 2:
+        qL = np.array([1.0, 1.0, 1.0, 7.0])
+    else:
+        qL = np.array([1.0, 1.0, 1.0, 1.0, 15.0])
+    qR = qL + 1
+    assert np.linalg.norm(roe(oracle, qL, qR, n) + roe(oracle, qR, qL, -n)) < 1e-13
+
+
+def _logmean_test(aL, aR):
+    # independent log mean of test/euler/test_flux.jl:4-16 (series below 1e-2)
+    xi = aL / aR
+    f = (xi - 1) / (xi + 1)
+    u = f * f
+    if u < 1e-2:
+        F = 1.0 + u / 3.0 + u * u / 5.0 + u * u * u / 7.0
+    else:
+        F = math.log(xi) / 2.0 / f
+    return (aL + aR) / (2 * F)
+
+
+def _ir_flux_test(qL, qR, nrm, gamma=1.4):
+    # independent slow IR flux of test/euler/test_flux.jl:87-117
+    g1 = gamma - 1
+    pL = g1 * (qL[3] - 0.5 * (qL[1] ** 2 + qL[2] ** 2) / qL[0])
+    pR = g1 * (qR[3] - 0.5 * (qR[1] ** 2 + qR[2] ** 2) / qR[0])
+    z5_ln = _logmean_test(math.sqrt(qL[0] * pL), math.sqrt(qR[0] * pR))
+    rho_hat = 0.5 * (math.sqrt(qL[0] / pL) + math.sqrt(qR[0] / pR)) * z5_ln
+    z1L, z1R = math.sqrt(qL[0] / pL), math.sqrt(qR[0] / pR)
+    z1_avg = 0.5 * (z1L + z1R)
+    u_hat = 0.5 * (z1L * qL[1] / qL[0] + z1R * qR[1] / qR[0]) / z1_avg
+    v_hat = 0.5 * (z1L * qL[2] / qL[0] + z1R * qR[2] / qR[0]) / z1_avg
+    p1_hat = 0.5 * (math.sqrt(qL[0] * pL) + math.sqrt(qR[0] * pR)) / z1_avg
+    z1_ln = _logmean_test(z1L, z1R)
+    p2_hat = ((gamma + 1) * z5_ln / (2 * gamma * z1_ln)
+              + g1 * 0.5 * (math.sqrt(qL[0] * pL) + math.sqrt(qR[0] * pR)) / (2 * gamma * z1_avg))
+    h_hat = gamma * p2_hat / (rho_hat * g1) + 0.5 * (u_hat ** 2 + v_hat ** 2)
+    fx = np.array([rho_hat * u_hat, rho_hat * u_hat ** 2 + p1_hat, rho_hat * u_hat * v_hat,
+                   rho_hat * u_hat * h_hat])
+    fy = np.array([rho_hat * v_hat, rho_hat * u_hat * v_hat, rho_hat * v_hat ** 2 + p1_hat,
+                   rho_hat * v_hat * h_hat])
+    return fx * nrm[0] + fy * nrm[1]
+
+
+def test_ir_flux_properties(oracle):
+    """test/euler/test_flux.jl:26-165: IR flux symmetric, antisymmetric in n,
+    consistent with the Euler flux, multi-direction == single direction, and
+    equal to an independent slow implementation at 1e-12."""
+    qL = np.array([1.0, 2.0, 3.0, 7.0])
+    qR = qL + 1
+    n = np.array([1.0, 1.0])
+    np.testing.assert_allclose(ir(oracle, qL, qR, n), ir(oracle, qR, qL, n), atol=1e-12)
+    np.testing.assert_allclose(ir(oracle, qL, qR, n), -ir(oracle, qR, qL, -n), atol=1e-12)
+    np.testing.assert_allclose(ir(oracle, qL, qL, n), euler(oracle, qL, n), rtol=1e-12)
+    nrm = np.array([1.0, 2.0])
+    np.testing.assert_allclose(ir(oracle, qL, qR, nrm), _ir_flux_test(qL, qR, nrm), atol=1e-12)
+    # multi-direction
+    P = _p()
+    rng = np.random.default_rng(1)
+    dirs = np.ascontiguousarray(rng.uniform(size=(2, 2)))
+    Fm = np.zeros((2, 4))
+    oracle.oracle_ir_flux(C.byref(P), 2, abi.dptr(qL), abi.dptr(qR), abi.dptr(dirs), 2, abi.dptr(Fm))
+    for d in range(2):
+        np.testing.assert_allclose(Fm[d], ir(oracle, qL, qR, dirs[d]), rtol=1e-14)
+
+
+def test_logavg(oracle):
+    """bc_solvers.jl:942-956: log mean is symmetric, exact at aL == aR, and
+    continuous across the series threshold (test_jac.jl:2001-2050 probes it)."""
+    assert math.isclose(oracle.oracle_logavg(2.0, 2.0), 2.0, rel_tol=1e-15)
+    for a, b in [(1.0, 1.5), (3.0, 0.2), (1.0, 1.0001)]:
+        assert math.isclose(oracle.oracle_logavg(a, b), oracle.oracle_logavg(b, a), rel_tol=1e-14)
+        assert math.isclose(oracle.oracle_logavg(a, b), (a - b) / math.log(a / b), rel_tol=1e-12)
+    # both sides of u = 1e-3: xi with f^2 = 1e-3
+    f = math.sqrt(1e-3)
+    xi = (1 + f) / (1 - f)
+    lo = oracle.oracle_logavg(xi * (1 - 1e-9), 1.0)
+    hi = oracle.oracle_logavg(xi * (1 + 1e-9), 1.0)
+    assert abs(hi - lo) < 1e-8
+
+
+def test_freestream_residual_roundoff(oracle):
+    """test/euler/test_lowlevel.jl:763-818: a uniform flow with free-stream
+    boundary data has zero residual at round-off."""
+    for fam, p in [("omega", 2), ("gamma", 3)]:
+        op = sbp.get_operator(2, fam, p)
+        ms = mesh.annulus(op, 4, 4, bc=mesh.BC_FREESTREAM)
+        desc = abi.MeshDesc(ms)
+        P = _p(Ma=0.5, aoa_deg=10.0)
+        q = problems.free_stream(2, ms.coords.shape[:2], Ma=0.5, aoa=10.0 * math.pi / 180)
+        res = oracle_residual(oracle, desc, P, np.ascontiguousarray(q))
+        assert np.abs(res).max() < 1e-13
+
+
+def test_freestream_residual_roundoff_tet_split_form(oracle):
+    """Free-stream preservation of the Ismail-Roe split form on warped
+    (curvilinear) tetrahedra: the discrete metric identities hold."""
+    op = sbp.get_operator(3, "diage", 2)
+    ms = mesh.cube(op, 2, warp=0.05, seed=3, bc=mesh.BC_FREESTREAM)
+    desc = abi.MeshDesc(ms)
+    P = _p(Ma=0.5, aoa_deg=5.0, face_flux=abi.EG_FLUX_IR, volume_integral_type=2)
+    q = problems.free_stream(3, ms.coords.shape[:2], Ma=0.5, aoa=5.0 * math.pi / 180)
+    res = oracle_residual(oracle, desc, P, np.ascontiguousarray(q))
+    assert np.abs(res).max() < 1e-12
+
+
+def test_split_form_conservation(oracle):
+    """test/euler/test_flux.jl:195-200: with S skew-symmetric and F
+    symmetric, 1^T (volume split-form residual) = 0 per element.  Faces are
+    made inert by evaluating with all boundary/interface fluxes identical,
+    so the check is on the total over the mesh: sum(res) = boundary flux."""
+    op = sbp.get_operator(3, "diage", 2)
+    ms = mesh.cube(op, 2, warp=0.05, seed=3, bc=mesh.BC_FREESTREAM)
+    desc = abi.MeshDesc(ms)
+    P = _p(Ma=0.5, face_flux=abi.EG_FLUX_IR, volume_integral_type=2)
+    rng = np.random.default_rng(7)
+    q = problems.free_stream(3, ms.coords.shape[:2], Ma=0.5)
+    q[..., 0] *= 1 + rng.normal(0, 0.01, size=q.shape[:2])
+    q = np.ascontiguousarray(q)
+    res = oracle_residual(oracle, desc, P, q)
+    # conservation: interior contributions cancel; the total equals minus the
+    # integrated boundary flux, computed here independently
+    tot = res.sum(axis=(0, 1))
+    bflux = np.zeros(5)
+    from pdesolver_gb300.problems import free_stream
+    qg = free_stream(3, (1,), Ma=0.5)[0]
+    for b, (e, f) in enumerate(ms.bndryfaces):
+        for i in range(op.numfacenodes):
+            qf = op.interp[f, i] @ q[e, op.perm[f]]
+            bflux += op.wface[i] * roe(oracle, qf, qg, ms.nrm_bndry[b, i])
+    np.testing.assert_allclose(tot, -bflux, rtol=1e-11, atol=1e-13)
+
+
+def test_calc_norm(oracle):
+    """calcNorm (Utils.jl:427-449) with M and M^-1 weights."""
+    op = sbp.get_operator(2, "omega", 2)
+    ms = mesh.annulus(op, 3, 3)
+    desc = abi.MeshDesc(ms)
+    r = np.random.default_rng(3).normal(size=(ms.numEl, op.numnodes, 4))
+    M = ms.M[:, :, None]
+    assert math.isclose(oracle.oracle_calc_norm(C.byref(desc.desc), abi.dptr(r), 0),
+                        math.sqrt(np.sum(r * r * M)), rel_tol=1e-13)
+    assert math.isclose(oracle.oracle_calc_norm(C.byref(desc.desc), abi.dptr(r), 1),
+                        math.sqrt(np.sum(r * r / M)), rel_tol=1e-13)
