@@ -80,6 +80,31 @@ class Mesh:
         return self.sbp.w[None, :] / self.jac
 
 
+def save_npz(path, ms, **extra):
+    """Write a mesh and its SBP operator (all arrays, bit-exact) to an npz."""
+    op = ms.sbp
+    arrs = {f"mesh_{f.name}": getattr(ms, f.name) for f in dataclasses.fields(ms)
+            if isinstance(getattr(ms, f.name), np.ndarray)}
+    arrs.update({f"sbp_{f.name}": getattr(op, f.name) for f in dataclasses.fields(op)
+                 if isinstance(getattr(op, f.name), np.ndarray)})
+    meta = np.array([ms.dim, op.p, int(op.sparse_face)], dtype=np.int64)
+    np.savez_compressed(path, meta=meta, meta_family=np.array(op.family),
+                        meta_name=np.array(ms.name), **arrs, **extra)
+
+
+def load_npz(path):
+    """Inverse of save_npz: (mesh, other arrays)."""
+    z = np.load(path)
+    dim, p, sparse = (int(v) for v in z["meta"])
+    opf = {f.name: z[f"sbp_{f.name}"] for f in dataclasses.fields(SBPOperator)
+           if f"sbp_{f.name}" in z}
+    op = SBPOperator(dim=dim, p=p, family=str(z["meta_family"]), sparse_face=bool(sparse), **opf)
+    mf = {f.name: z[f"mesh_{f.name}"] for f in dataclasses.fields(Mesh) if f"mesh_{f.name}" in z}
+    ms = Mesh(dim=dim, sbp=op, name=str(z["meta_name"]), **mf)
+    extra = {k: z[k] for k in z.files if not k.startswith(("mesh_", "sbp_", "meta"))}
+    return ms, extra
+
+
 def _metrics_from_jacobian(J):
     """J[..., p, k] = dx_p/dxi_k -> (dxidx[..., p(x), k(xi)], jac)."""
     det = np.linalg.det(J)
@@ -94,61 +119,57 @@ def _face_key(verts):
     return tuple(sorted(int(v) for v in verts))
 
 
-def _connect(elverts, faces_local, sbp, coords_node_fn, face_points_fn, tag_fn,
-             bc_of_tag):
-    """Build interfaces / boundary faces and the geometric node matchings."""
-    E = elverts.shape[0]
-    table = {}
-    ifaces, bfaces = [], []
-    for e in range(E):
-        for f, lv in enumerate(faces_local):
-            key = _face_key(elverts[e, list(lv)])
-            if key in table:
-                eo, fo = table.pop(key)
-                ifaces.append((eo, e, fo, f))
-            else:
-                table[key] = (e, f)
-    for key, (e, f) in sorted(table.items(), key=lambda kv: kv[1]):
-        bfaces.append((e, f))
+def _connect(elverts, faces_local, sbp, face_pts_all, tags_of_faces, bc_of_tag):
+    """Interfaces, boundary faces and the geometric face-node matchings.
+
+    face_pts_all[e, f, i, :] are the physical coordinates of face node i of
+    local face f of element e.  Vectorised over all faces.
+    """
+    E, F = elverts.shape[0], len(faces_local)
     Nf = sbp.numfacenodes
-    perms = []
-    iface = np.zeros((len(ifaces), 5), dtype=np.int32)
-    for n, (eL, eR, fL, fR) in enumerate(ifaces):
-        xL = face_points_fn(eL, fL)
-        xR = face_points_fn(eR, fR)
-        perm = []
-        for i in range(Nf):
-            d = np.linalg.norm(xR - xL[i], axis=1)
-            j = int(np.argmin(d))
-            if d[j] > 1e-9 * max(1.0, np.abs(xL).max()):
-                raise RuntimeError("mesh: face nodes of neighbours do not match")
-            perm.append(j)
-        perm = tuple(perm)
-        if perm not in perms:
-            perms.append(perm)
-        iface[n] = (eL, eR, fL, fR, perms.index(perm))
-    nbrperm = np.array(perms if perms else [tuple(range(Nf))], dtype=np.int32)
-    tags = np.array([tag_fn(face_points_fn(e, f)) for e, f in bfaces], dtype=np.int32)
+    keys = np.sort(np.stack([elverts[:, list(lv)] for lv in faces_local], axis=1), axis=2)
+    keys = keys.reshape(E * F, -1)
+    order = np.lexsort(keys.T[::-1])
+    ks = keys[order]
+    same = np.all(ks[1:] == ks[:-1], axis=1)
+    first = np.nonzero(same)[0]
+    a, b = order[first], order[first + 1]          # element-face ids sharing a face
+    pair_lo = np.minimum(a, b)
+    pair_hi = np.maximum(a, b)
+    srt = np.argsort(pair_lo, kind="stable")
+    pair_lo, pair_hi = pair_lo[srt], pair_hi[srt]
+    matched = np.zeros(E * F, dtype=bool)
+    matched[pair_lo] = True
+    matched[pair_hi] = True
+    bids = np.nonzero(~matched)[0]
+    eL, fL = pair_lo // F, pair_lo % F
+    eR, fR = pair_hi // F, pair_hi % F
+    xL = face_pts_all[eL, fL]                      # [I, Nf, d]
+    xR = face_pts_all[eR, fR]
+    dist = np.linalg.norm(xL[:, :, None, :] - xR[:, None, :, :], axis=3)   # [I, Nf, Nf]
+    perm = np.argmin(dist, axis=2)
+    scale = max(1.0, float(np.abs(face_pts_all).max()))
+    if np.any(np.take_along_axis(dist, perm[:, :, None], 2) > 1e-9 * scale):
+        raise RuntimeError("mesh: face nodes of neighbours do not match")
+    uperm, orient = np.unique(perm, axis=0, return_inverse=True)
+    iface = np.stack([eL, eR, fL, fR, orient.reshape(-1)], axis=1).astype(np.int32)
+    nbrperm = uperm.astype(np.int32) if len(uperm) else np.arange(Nf, dtype=np.int32)[None]
+    be, bf = bids // F, bids % F
+    tags = np.asarray(tags_of_faces(be, bf), dtype=np.int32)
     bc = np.array([bc_of_tag(t) for t in tags], dtype=np.int32)
-    order = np.lexsort((np.arange(len(bfaces)), tags, bc))
-    bfaces = np.array(bfaces, dtype=np.int32).reshape(-1, 2)[order]
-    tags = tags[order]
-    bc = bc[order]
+    o = np.lexsort((np.arange(len(bids)), tags, bc))
+    bfaces = np.stack([be, bf], axis=1).astype(np.int32)[o]
+    tags, bc = tags[o], bc[o]
     bc_types = np.unique(bc).astype(np.int32)
     offsets = np.searchsorted(bc, bc_types).tolist() + [len(bc)]
     return iface, nbrperm, bfaces, np.array(offsets, dtype=np.int32), bc_types, tags
 
 
-def _face_geometry(sbp, dxidx_face_fn, faces, coords_fn):
-    """scaled normals and coordinates at the face nodes of (element, face)."""
-    Nf, d = sbp.numfacenodes, sbp.dim
-    nrm = np.zeros((len(faces), Nf, d))
-    crd = np.zeros((len(faces), Nf, d))
-    for n, (e, f) in enumerate(faces):
-        Dx = dxidx_face_fn(e, f)          # [Nf, d(x), d(xi)]
-        nrm[n] = np.einsum("k,ipk->ip", sbp.normals[f], Dx)
-        crd[n] = coords_fn(e, f)
-    return nrm, crd
+def _face_normals(sbp, dxidx_face_all, faces):
+    """scaled normals n_f . dxidx at the face nodes of (element, face) rows."""
+    e, f = faces[:, 0], faces[:, 1]
+    Dx = dxidx_face_all[e, f]                      # [n, Nf, d(x), d(xi)]
+    return np.einsum("nk,nipk->nip", sbp.normals[f], Dx)
 
 
 def annulus(sbp: SBPOperator, nr: int, ntheta: int, r_in=1.0, r_out=3.0,
@@ -181,25 +202,25 @@ def annulus(sbp: SBPOperator, nr: int, ntheta: int, r_in=1.0, r_out=3.0,
     dxidx = np.repeat(dx[:, None], Np, axis=1)
     jac = np.repeat(jac_e[:, None], Np, axis=1)
 
-    def face_pts(e, f):
-        return np.einsum("nv,vp->np", _bary_tri(sbp.face_xi[f]), X[e])
+    Nf = sbp.numfacenodes
+    fpts = np.stack([np.einsum("nv,evp->enp", _bary_tri(sbp.face_xi[f]), X) for f in range(3)], 1)
 
-    def tag_fn(pts):
-        rr = np.linalg.norm(pts, axis=1)
-        if np.allclose(rr, r_in, atol=1e-9 * r_out) or np.all(rr < r_in + 1e-9):
-            return 0
-        if np.all(np.abs(pts[:, 1]) < 1e-12):
-            return 2
-        if np.all(np.abs(pts[:, 0]) < 1e-12):
-            return 3
-        return 1
+    def tags_of(be, bf):
+        pts = fpts[be, bf]                          # [nb, Nf, 2]
+        rr = np.linalg.norm(pts, axis=2)
+        t = np.ones(len(be), dtype=np.int32)
+        t[np.all(np.abs(pts[:, :, 0]) < 1e-12, axis=1)] = 3
+        t[np.all(np.abs(pts[:, :, 1]) < 1e-12, axis=1)] = 2
+        t[np.all(rr < r_in + 1e-9 * r_out, axis=1)] = 0
+        return t
 
-    iface, nbrperm, bfaces, offs, bct, tags = _connect(
-        elverts, TRI_FACES, sbp, None, face_pts, tag_fn, lambda t: bc)
-    nrm_f, crd_f = _face_geometry(sbp, lambda e, f: np.repeat(dx[e][None], sbp.numfacenodes, 0),
-                                  iface[:, [0, 2]], face_pts)
-    nrm_b, crd_b = _face_geometry(sbp, lambda e, f: np.repeat(dx[e][None], sbp.numfacenodes, 0),
-                                  bfaces, face_pts)
+    iface, nbrperm, bfaces, offs, bct, tags = _connect(elverts, TRI_FACES, sbp, fpts, tags_of,
+                                                       lambda t: bc)
+    dxf = np.repeat(np.repeat(dx[:, None, None], 3, axis=1), Nf, axis=2)   # [E, F, Nf, 2, 2]
+    nrm_f = _face_normals(sbp, dxf, iface[:, [0, 2]])
+    crd_f = fpts[iface[:, 0], iface[:, 2]]
+    nrm_b = _face_normals(sbp, dxf, bfaces)
+    crd_b = fpts[bfaces[:, 0], bfaces[:, 1]]
     return Mesh(2, sbp, coords, dxidx, jac, iface, nbrperm, nrm_f, crd_f, bfaces, offs,
                 bct, crd_b, nrm_b, tags, name=f"annulus{nr}x{ntheta}")
 
@@ -299,28 +320,28 @@ def cube(sbp: SBPOperator, n: int, warp=0.05, seed=3, bc=BC_FREESTREAM) -> Mesh:
     coords, Jn = geom(allE, sbp.nodes)
     dxidx, jac = _metrics_from_jacobian(Jn)
 
-    def face_pts(e, f):
-        x, _ = geom(np.array([e]), sbp.face_xi[f])
-        return x[0]
+    fpts, fdx = [], []
+    for f in range(4):
+        xf, Jf = geom(allE, sbp.face_xi[f])
+        fpts.append(xf)
+        fdx.append(_metrics_from_jacobian(Jf)[0])
+    fpts = np.stack(fpts, 1)                        # [E, 4, Nf, 3]
+    fdx = np.stack(fdx, 1)                          # [E, 4, Nf, 3, 3]
 
-    def face_dx(e, f):
-        _, Jf = geom(np.array([e]), sbp.face_xi[f])
-        d, _ = _metrics_from_jacobian(Jf[0])
-        return d
+    def tags_of(be, bf):
+        # classify by the unwarped face (centroid of the element's vertices)
+        fv = np.array(TET_FACES)[bf]                # [nb, 3]
+        c = X[be[:, None], fv].mean(axis=1)         # [nb, 3]
+        dist = np.minimum(np.abs(c), np.abs(1 - c))
+        ax = np.argmin(dist, axis=1)
+        hi = np.abs(1 - c[np.arange(len(be)), ax]) < np.abs(c[np.arange(len(be)), ax])
+        return 2 * ax + hi.astype(np.int32)
 
-    def tag_fn(pts):
-        # classify by the unwarped face: use the face centroid of the
-        # element's vertices instead (robust to the warp)
-        return -1
-
-    iface, nbrperm, bfaces, offs, bct, tags = _connect(
-        elverts, TET_FACES, sbp, None, face_pts, tag_fn, lambda t: bc)
-    # geometric tags from the unwarped vertex positions
-    for n_, (e, f) in enumerate(bfaces):
-        c = X[e, list(TET_FACES[f])].mean(axis=0)
-        ax = int(np.argmin(np.minimum(np.abs(c), np.abs(1 - c))))
-        tags[n_] = 2 * ax + (1 if abs(1 - c[ax]) < abs(c[ax]) else 0)
-    nrm_f, crd_f = _face_geometry(sbp, face_dx, iface[:, [0, 2]], face_pts)
-    nrm_b, crd_b = _face_geometry(sbp, face_dx, bfaces, face_pts)
+    iface, nbrperm, bfaces, offs, bct, tags = _connect(elverts, TET_FACES, sbp, fpts, tags_of,
+                                                       lambda t: bc)
+    nrm_f = _face_normals(sbp, fdx, iface[:, [0, 2]])
+    crd_f = fpts[iface[:, 0], iface[:, 2]]
+    nrm_b = _face_normals(sbp, fdx, bfaces)
+    crd_b = fpts[bfaces[:, 0], bfaces[:, 1]]
     return Mesh(3, sbp, coords, dxidx, jac, iface, nbrperm, nrm_f, crd_f, bfaces, offs,
                 bct, crd_b, nrm_b, tags, name=f"cube{n}")

@@ -1,8 +1,9 @@
 """Regenerates the committed golden residual fixtures from the CPU oracle.
 
 Run from the repository root: ``python tests/golden/make_golden.py``.
-Each fixture holds the seeded input state and the oracle's residual for a
-small case of each discretisation on the hot path:
+Each fixture holds every input bit-exactly (SBP operator, mesh arrays,
+options, seeded state) and the oracle's residual, for a small case of each
+discretisation on the hot path:
   c1:       512-triangle vortex annulus, SBP-Omega p=2, Roe (full config 1)
   gamma3:   8x8 annulus (128 triangles), SBP-Gamma p=3, Roe
   tet2:     warped 2^3 cube (48 tets), diagonal-E p=2, IR split form + IR faces
@@ -18,7 +19,15 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 import __graft_entry__ as graft  # noqa: E402
 
 graft.load_package()
-from pdesolver_gb300 import abi, build, eulergpu, problems  # noqa: E402
+import json  # noqa: E402
+
+from pdesolver_gb300 import abi, build, eulergpu, mesh, problems  # noqa: E402
+
+
+def load(name):
+    """(mesh, opts, q, res) of a committed fixture."""
+    ms, extra = mesh.load_npz(os.path.join(HERE, f"residual_{name}.npz"))
+    return ms, json.loads(str(extra["opts"])), extra["q"], extra["res"]
 
 
 def cases():
@@ -40,7 +49,8 @@ def main():
     lib = C.CDLL(build.build_oracle())
     for name, (ms, opts, q) in cases():
         res = oracle_residual(lib, ms, opts, q)
-        np.savez_compressed(os.path.join(HERE, f"residual_{name}.npz"), q=q, res=res)
+        mesh.save_npz(os.path.join(HERE, f"residual_{name}.npz"), ms, q=q, res=res,
+                      opts=np.array(json.dumps(opts)))
         print(name, q.shape, float(np.abs(res).max()))
 
 

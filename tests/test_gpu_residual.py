@@ -29,11 +29,12 @@ def gpu_residual(ms, opts, q):
 
 @pytest.mark.parametrize("name", ["c1", "gamma3", "tet2"])
 def test_residual_matches_golden(gpu_lib, name):
-    from test_golden import CASES
-    ms, opts, q = CASES[name]
-    gold = np.load(os.path.join(HERE, f"residual_{name}.npz"))
-    res, _ = gpu_residual(ms, opts, np.ascontiguousarray(gold["q"]))
-    assert rel_err(res, gold["res"]) <= TOL
+    """GPU residual on the fixture's bit-exact inputs vs the committed oracle
+    residual."""
+    from test_golden import GEN
+    ms, opts, q, gold = GEN.load(name)
+    res, _ = gpu_residual(ms, opts, np.ascontiguousarray(q))
+    assert rel_err(res, gold) <= TOL
 
 
 @pytest.mark.parametrize("fam,p", [("omega", 1), ("omega", 2), ("omega", 3), ("omega", 4),
