@@ -151,10 +151,10 @@ int eg_calc_norm(eg_mesh* mesh, const double* r, int32_t strongres, int32_t mem,
 
 /* ---- streams, asynchronous launch and phase timers ---------------------- */
 
-/* Run this mesh's work on `stream` (a cudaStream_t; NULL restores the
-   library's own stream).  Lets a caller order library work with its own
-   kernels and CUDA events. */
-int eg_mesh_set_stream(eg_mesh* mesh, void* stream);
+/* Run this mesh's work on `stream` (a cudaStream_t; NULL is CUDA's default
+   stream), or on the library's own stream when use_own != 0.  Lets a caller
+   order library work with its own kernels and CUDA events. */
+int eg_mesh_set_stream(eg_mesh* mesh, void* stream, int32_t use_own);
 
 /* evalResidual with device pointers, enqueued on the mesh stream without a
    host synchronisation; the density/pressure checks are reported by the next

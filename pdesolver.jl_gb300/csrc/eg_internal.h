@@ -64,6 +64,9 @@ struct eg_mesh {
   int32_t* nbrperm; // [norient][Nf]
   double* wface;    // [Nf]
   double* lift;     // [F][Np][Nf]: sum_s [perm[f][s]==j] interp[f][i][s] * wface[i]
+  double* liftS;    // [F][Nf][S]: interp[f][i][s] * wface[i]
+  int32_t* nbrinv;  // [norient][Nf]: inverse permutations of nbrperm
+  int sparse_face;  // interp is the identity on every face (diagonal-E operators)
   // mesh (device)
   double* dxidx;    // [E][Np][dim][dim]
   double* jac;      // [E][Np]

@@ -23,7 +23,65 @@ struct DevMesh {
   const double* Minv;     // [E][Np]
   const double* w;        // [Np]
   const double* jac;      // [E][Np]
+  const double* liftS;    // [F][Nf][S]: interp[f][i][s] * wface[i]
+  const int* nbrinv;      // [norient][Nf]: inverse of nbrperm
+  const double* wface;    // [Nf]
+  int sparse_face;        // face nodes are volume nodes (interp = identity)
 };
+
+// Face terms of the SBP weak form added into a shared-memory residual
+// sres[epb][Np][NV] of the CTA's elements e0 .. e0+nloc-1 (reference
+// interiorfaceintegrate! / boundaryintegrate! with Subtract: elementL and
+// boundary faces subtract, elementR adds).  One pass per local face; in a
+// pass thread t handles (element, stencil node) so only stencil nodes do
+// work, and no two threads touch the same entry (deterministic, no atomics).
+template <int DIM>
+__device__ __forceinline__ void face_lift_smem(const DevMesh& md, const double* __restrict__ fflux,
+                                               double* sres, const double* sLift, const int* sPerm,
+                                               int e0, int nloc) {
+  constexpr int NV = DIM + 2;
+  constexpr int F = DIM + 1;
+  const int Np = md.Np, Nf = md.Nf, S = md.S;
+#pragma unroll 1
+  for (int f = 0; f < F; ++f) {
+    for (int t = threadIdx.x; t < nloc * S; t += blockDim.x) {
+      const int le = t / S, s = t - le * S;
+      const EFace ef = md.eface[(size_t)(e0 + le) * F + f];
+      const double* fl = fflux + (size_t)ef.slot * Nf * NV;
+      double acc[NV];
+#pragma unroll
+      for (int c = 0; c < NV; ++c) acc[c] = 0.0;
+      if (md.sparse_face) {
+        const int i = ef.side ? md.nbrinv[ef.orient * Nf + s] : s;
+        const double a = md.wface[s];
+#pragma unroll
+        for (int c = 0; c < NV; ++c) acc[c] = a * fl[i * NV + c];
+      } else if (ef.side == 0) {
+        for (int i = 0; i < Nf; ++i) {
+          const double a = sLift[(f * Nf + i) * S + s];
+#pragma unroll
+          for (int c = 0; c < NV; ++c) acc[c] = fma(a, fl[i * NV + c], acc[c]);
+        }
+      } else {
+        const int* nb = md.nbrperm + ef.orient * Nf;
+        for (int i = 0; i < Nf; ++i) {
+          const double a = sLift[(f * Nf + nb[i]) * S + s];
+#pragma unroll
+          for (int c = 0; c < NV; ++c) acc[c] = fma(a, fl[i * NV + c], acc[c]);
+        }
+      }
+      double* r = sres + ((size_t)le * Np + sPerm[f * S + s]) * NV;
+      if (ef.side == 0) {
+#pragma unroll
+        for (int c = 0; c < NV; ++c) r[c] -= acc[c];
+      } else {
+#pragma unroll
+        for (int c = 0; c < NV; ++c) r[c] += acc[c];
+      }
+    }
+    __syncthreads();
+  }
+}
 
 DevMesh dev_mesh(const eg_mesh* m);
 int eg_launch_residual(eg_mesh* m, const double* q, double* res);

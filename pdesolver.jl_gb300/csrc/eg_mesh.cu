@@ -82,7 +82,8 @@ static void freestream_state(const DevParams& p, int dim, double* sol) {
 
 static void free_mesh(eg_mesh* m) {
   if (!m) return;
-  void* bufs[] = {m->Q, m->w, m->interp, m->perm, m->nbrperm, m->wface, m->lift, m->dxidx,
+  void* bufs[] = {m->Q, m->w, m->interp, m->perm, m->nbrperm, m->wface, m->lift, m->liftS,
+                  m->nbrinv, m->dxidx,
                   m->jac, m->Minv, m->ifaces, m->nrm_face, m->bfaces, m->bc_of_b,
                   m->coords_bndry, m->nrm_bndry, m->qg_bndry, m->eface, m->fflux,
                   m->q_dev, m->res_dev, m->status, m->red};
@@ -242,6 +243,19 @@ extern "C" int eg_mesh_create(const eg_mesh_desc* d, const eg_params* params, eg
       for (int s = 0; s < S; ++s)
         lift[((size_t)f * Np + d->perm[f * S + s]) * Nf + i] +=
             d->interp[((size_t)f * Nf + i) * S + s] * d->wface[i];
+  std::vector<double> liftS((size_t)F * Nf * S);
+  for (int f = 0; f < F; ++f)
+    for (int i = 0; i < Nf; ++i)
+      for (int s = 0; s < S; ++s)
+        liftS[((size_t)f * Nf + i) * S + s] = d->interp[((size_t)f * Nf + i) * S + s] * d->wface[i];
+  std::vector<int32_t> nbrinv((size_t)m->norient * Nf);
+  for (int o = 0; o < m->norient; ++o)
+    for (int i = 0; i < Nf; ++i) nbrinv[(size_t)o * Nf + d->nbrperm[o * Nf + i]] = i;
+  m->sparse_face = (S == Nf);
+  for (int f = 0; f < F && m->sparse_face; ++f)
+    for (int i = 0; i < Nf; ++i)
+      for (int s = 0; s < S; ++s)
+        if (d->interp[((size_t)f * Nf + i) * S + s] != (i == s ? 1.0 : 0.0)) m->sparse_face = 0;
   // Dirichlet states at the boundary face nodes
   std::vector<double> qg((size_t)B * Nf * nv, 0.0);
   for (int b = 0; b < B; ++b)
@@ -266,6 +280,8 @@ extern "C" int eg_mesh_create(const eg_mesh_desc* d, const eg_params* params, eg
   UP(nbrperm, d->nbrperm, (size_t)m->norient * Nf, "nbrperm");
   UP(wface, d->wface, (size_t)Nf, "wface");
   UP(lift, lift.data(), lift.size(), "lift");
+  UP(liftS, liftS.data(), liftS.size(), "liftS");
+  UP(nbrinv, nbrinv.data(), nbrinv.size(), "nbrinv");
   UP(dxidx, d->dxidx, (size_t)E * Np * dim * dim, "dxidx");
   UP(jac, d->jac, (size_t)E * Np, "jac");
   UP(Minv, minv.data(), minv.size(), "Minv");

@@ -130,15 +130,17 @@ __device__ __forceinline__ T pressure(const Gas& g, const T* q) {
 // F . dir for the Euler equations (conservative variables)
 template <int DIM, typename T, typename Tn>
 __device__ __forceinline__ void euler_flux(const Gas& g, const T* q, const Tn* dir, T* F) {
-  T press = pressure<DIM>(g, q);
+  const T r = 1.0 / q[0];
   if (DIM == 2) {
-    T U = (q[1] * dir[0] + q[2] * dir[1]) / q[0];
+    T press = g.gamma_1 * (q[3] - 0.5 * (q[1] * q[1] + q[2] * q[2]) * r);
+    T U = (q[1] * dir[0] + q[2] * dir[1]) * r;
     F[0] = q[0] * U;
     F[1] = q[1] * U + dir[0] * press;
     F[2] = q[2] * U + dir[1] * press;
     F[3] = (q[3] + press) * U;
   } else {
-    T U = (q[1] * dir[0] + q[2] * dir[1] + q[3] * dir[2]) / q[0];
+    T press = g.gamma_1 * (q[4] - 0.5 * (q[1] * q[1] + q[2] * q[2] + q[3] * q[3]) * r);
+    T U = (q[1] * dir[0] + q[2] * dir[1] + q[3] * dir[2]) * r;
     F[0] = q[0] * U;
     F[1] = q[1] * U + dir[0] * press;
     F[2] = q[2] * U + dir[1] * press;
@@ -147,26 +149,29 @@ __device__ __forceinline__ void euler_flux(const Gas& g, const T* q, const Tn* d
   }
 }
 
-// Roe flux: F(qL).n + 0.5 (|A_hat| - A_hat)(qL - qR), eigenvalue floors 0.025
+// Roe flux: F(qL).n + 0.5 (|A_hat| - A_hat)(qL - qR), eigenvalue floors 0.025.
+// Arranged to spend few FP64 divisions (the scarce resource on GB300): one
+// reciprocal per state density, 1/(sqL+sqR), 1/(n.n), 1/(H - phi) (= gami/a^2)
+// and 1/(dA a); the Euler flux of qL reuses 1/rho_L.
 template <int DIM, typename T, typename Tn>
 __device__ __forceinline__ void roe_flux(const Gas& g, const T* q, const T* qg, const Tn* nrm, T* flux) {
   constexpr int NV = DIM + 2;
   const double gamma = g.gamma, gami = g.gamma_1;
   const double sat_V = 0.025;
   // Roe averages
-  T fac = 1.0 / q[0];
-  T uL = q[1] * fac, vL = q[2] * fac;
-  T wL = (DIM == 3) ? q[3] * fac : T(0.0);
-  T phi = 0.5 * (uL * uL + vL * vL + wL * wL);
-  T HL = gamma * q[NV - 1] * fac - gami * phi;
-  fac = 1.0 / qg[0];
-  T uR = qg[1] * fac, vR = qg[2] * fac;
-  T wR = (DIM == 3) ? qg[3] * fac : T(0.0);
-  phi = 0.5 * (uR * uR + vR * vR + wR * wR);
-  T HR = gamma * qg[NV - 1] * fac - gami * phi;
+  const T rL = 1.0 / q[0];
+  T uL = q[1] * rL, vL = q[2] * rL;
+  T wL = (DIM == 3) ? q[3] * rL : T(0.0);
+  T phiL = 0.5 * (uL * uL + vL * vL + wL * wL);
+  T HL = gamma * q[NV - 1] * rL - gami * phiL;
+  const T rR = 1.0 / qg[0];
+  T uR = qg[1] * rR, vR = qg[2] * rR;
+  T wR = (DIM == 3) ? qg[3] * rR : T(0.0);
+  T phiR = 0.5 * (uR * uR + vR * vR + wR * wR);
+  T HR = gamma * qg[NV - 1] * rR - gami * phiR;
   T sqL = sqrt(q[0]);
   T sqR = sqrt(qg[0]);
-  fac = 1.0 / (sqL + sqR);
+  T fac = 1.0 / (sqL + sqR);
   T u = (sqL * uL + sqR * uR) * fac;
   T v = (sqL * vL + sqR * vR) * fac;
   T w = (DIM == 3) ? (sqL * wL + sqR * wR) * fac : T(0.0);
@@ -177,14 +182,17 @@ __device__ __forceinline__ void roe_flux(const Gas& g, const T* q, const T* qg, 
   // SAT
   Tn nx = nrm[0], ny = nrm[1];
   Tn nz = (DIM == 3) ? nrm[2] : Tn(0.0);
-  Tn dA = sqrt(nx * nx + ny * ny + nz * nz);
+  Tn n2 = nx * nx + ny * ny + nz * nz;
+  Tn dA = sqrt(n2);
   T Un = u * nx + v * ny + w * nz;
-  phi = 0.5 * (u * u + v * v + w * w);
-  T a = sqrt(gami * (H - phi));
-  T lambda1 = Un + dA * a;
-  T lambda2 = Un - dA * a;
+  T phi = 0.5 * (u * u + v * v + w * w);
+  T Hp = H - phi;
+  T a = sqrt(gami * Hp);
+  T dAa = dA * a;
+  T lambda1 = Un + dAa;
+  T lambda2 = Un - dAa;
   T lambda3 = Un;
-  T rhoA = absval(Un) + dA * a;
+  T rhoA = absval(Un) + dAa;
   lambda1 = 0.5 * (maxval(absval(lambda1), sat_V * rhoA) - lambda1);
   lambda2 = 0.5 * (maxval(absval(lambda2), sat_V * rhoA) - lambda2);
   lambda3 = 0.5 * (maxval(absval(lambda3), sat_V * rhoA) - lambda3);
@@ -197,19 +205,20 @@ __device__ __forceinline__ void roe_flux(const Gas& g, const T* q, const T* qg, 
     dqN = -Un * dq[0] + nx * dq[1] + ny * dq[2] + nz * dq[3];
   }
   T t1 = 0.5 * (lambda1 + lambda2) - lambda3;
-  T t2 = gami / (a * a);
-  Tn t3 = 1.0 / (dA * dA);
-  T t4 = 0.5 * (lambda1 - lambda2) / (dA * a);
+  T t2 = 1.0 / Hp;                 // gami / a^2
+  Tn t3 = 1.0 / n2;                // 1 / dA^2
+  T t4 = 0.5 * (lambda1 - lambda2) / dAa;
   // sat = l3 dq + t1 (t2 E1dq + t3 E2dq) + t4 (E3dq + gami E4dq)
   T c1 = t1 * t2 * dqE + t4 * dqN;        // coefficient of (1, u, v, w, H)
   T c2 = t1 * t3 * dqN + t4 * gami * dqE; // coefficient of (0, nx, ny, nz, Un)
-  T ef[NV];
-  euler_flux<DIM>(g, q, nrm, ef);
-  flux[0] = ef[0] + lambda3 * dq[0] + c1;
-  flux[1] = ef[1] + lambda3 * dq[1] + c1 * u + c2 * nx;
-  flux[2] = ef[2] + lambda3 * dq[2] + c1 * v + c2 * ny;
-  if (DIM == 3) flux[3] = ef[3] + lambda3 * dq[3] + c1 * w + c2 * nz;
-  flux[NV - 1] = ef[NV - 1] + lambda3 * dq[NV - 1] + c1 * H + c2 * Un;
+  // Euler flux of qL in direction n, reusing 1/rho_L
+  T pL = gami * (q[NV - 1] - 0.5 * (q[1] * q[1] + q[2] * q[2] + ((DIM == 3) ? q[3] * q[3] : T(0.0))) * rL);
+  T UL = (q[1] * nx + q[2] * ny + ((DIM == 3) ? q[3] * nz : T(0.0))) * rL;
+  flux[0] = q[0] * UL + lambda3 * dq[0] + c1;
+  flux[1] = q[1] * UL + nx * pL + lambda3 * dq[1] + c1 * u + c2 * nx;
+  flux[2] = q[2] * UL + ny * pL + lambda3 * dq[2] + c1 * v + c2 * ny;
+  if (DIM == 3) flux[3] = q[3] * UL + nz * pL + lambda3 * dq[3] + c1 * w + c2 * nz;
+  flux[NV - 1] = (q[NV - 1] + pL) * UL + lambda3 * dq[NV - 1] + c1 * H + c2 * Un;
 }
 
 // logarithmic mean with the 5-term series below u = 1e-3

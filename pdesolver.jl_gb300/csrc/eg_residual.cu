@@ -89,7 +89,9 @@ __global__ void k_face_flux(DevMesh md, const double* __restrict__ q, double* __
   for (int c = 0; c < NV; ++c) out[c] = fl[c];
 }
 
-// Shared-memory layout of k_element: Q[dim][Np][Np] | lift[F][Np][Nf] | Fbuf
+// Shared-memory layout of k_element:
+//   Q[dim][Np][Np] | liftS[F][Nf][S] | perm[F][S] (ints, padded) | Fbuf[epb][dim][Np][NV]
+//   | sres[epb][Np][NV]
 template <int DIM>
 __global__ void k_element(DevMesh md, const double* __restrict__ q,
                           const double* __restrict__ fflux, double* __restrict__ res,
@@ -97,15 +99,20 @@ __global__ void k_element(DevMesh md, const double* __restrict__ q,
   constexpr int NV = DIM + 2;
   constexpr int F = DIM + 1;
   extern __shared__ double smem[];
-  const int Np = md.Np, Nf = md.Nf;
+  const int Np = md.Np, Nf = md.Nf, S = md.S;
   double* sQ = smem;
   double* sL = sQ + DIM * Np * Np;
-  double* sF = sL + F * Np * Nf;
+  int* sPerm = reinterpret_cast<int*>(sL + F * Nf * S);
+  double* sF = sL + F * Nf * S + (F * S + 1) / 2;
+  double* sres = sF + (size_t)epb * DIM * Np * NV;
   for (int k = threadIdx.x; k < DIM * Np * Np; k += blockDim.x) sQ[k] = md.Q[k];
-  for (int k = threadIdx.x; k < F * Np * Nf; k += blockDim.x) sL[k] = md.lift[k];
+  for (int k = threadIdx.x; k < F * Nf * S; k += blockDim.x) sL[k] = md.liftS[k];
+  for (int k = threadIdx.x; k < F * S; k += blockDim.x) sPerm[k] = md.perm[k];
+  const int e0 = blockIdx.x * epb;
+  const int nloc = min(epb, md.E - e0);
   const int le = threadIdx.x / Np, j = threadIdx.x - le * Np;
-  const int e = blockIdx.x * epb + le;
-  const bool active = (le < epb) && (e < md.E);
+  const int e = e0 + le;
+  const bool active = le < nloc;
   const Gas g{md.gamma, md.gamma_1};
   double* Fe = sF + (size_t)le * DIM * Np * NV;  // [k][i][c]
   if (active) {
@@ -126,45 +133,30 @@ __global__ void k_element(DevMesh md, const double* __restrict__ q,
     }
   }
   __syncthreads();
-  if (!active) return;
-  double acc[NV];
+  if (active) {
+    double acc[NV];
 #pragma unroll
-  for (int c = 0; c < NV; ++c) acc[c] = 0.0;
-  // volume: (Q_k^T F_k)_j = sum_i Q_k(i, j) F_k,i ; sQ[k][j][i] = Q_k(i, j)
+    for (int c = 0; c < NV; ++c) acc[c] = 0.0;
+    // volume: (Q_k^T F_k)_j = sum_i Q_k(i, j) F_k,i ; sQ[k][j][i] = Q_k(i, j)
 #pragma unroll
-  for (int k = 0; k < DIM; ++k) {
-    const double* qrow = sQ + ((size_t)k * Np + j) * Np;
-    const double* Fk = Fe + (size_t)k * Np * NV;
-    for (int i = 0; i < Np; ++i) {
-      const double a = qrow[i];
+    for (int k = 0; k < DIM; ++k) {
+      const double* qrow = sQ + ((size_t)k * Np + j) * Np;
+      const double* Fk = Fe + (size_t)k * Np * NV;
+      for (int i = 0; i < Np; ++i) {
+        const double a = qrow[i];
 #pragma unroll
-      for (int c = 0; c < NV; ++c) acc[c] = fma(a, Fk[i * NV + c], acc[c]);
-    }
-  }
-  // faces: elementL side subtracts, elementR side adds (SBP face integrate)
-#pragma unroll
-  for (int f = 0; f < F; ++f) {
-    const EFace ef = md.eface[(size_t)e * F + f];
-    const double* fl = fflux + (size_t)ef.slot * Nf * NV;
-    const double* lrow = sL + ((size_t)f * Np + j) * Nf;
-    if (ef.side == 0) {
-      for (int i = 0; i < Nf; ++i) {
-        const double a = -lrow[i];
-#pragma unroll
-        for (int c = 0; c < NV; ++c) acc[c] = fma(a, fl[i * NV + c], acc[c]);
-      }
-    } else {
-      const int* nb = md.nbrperm + ef.orient * Nf;
-      for (int i = 0; i < Nf; ++i) {
-        const double a = lrow[nb[i]];
-#pragma unroll
-        for (int c = 0; c < NV; ++c) acc[c] = fma(a, fl[i * NV + c], acc[c]);
+        for (int c = 0; c < NV; ++c) acc[c] = fma(a, Fk[i * NV + c], acc[c]);
       }
     }
-  }
-  double* dst = res + ((size_t)e * Np + j) * NV;
+    double* r = sres + ((size_t)le * Np + j) * NV;
 #pragma unroll
-  for (int c = 0; c < NV; ++c) dst[c] = acc[c];
+    for (int c = 0; c < NV; ++c) r[c] = acc[c];
+  }
+  __syncthreads();
+  face_lift_smem<DIM>(md, fflux, sres, sL, sPerm, e0, nloc);
+  // coalesced copy of the CTA's residual block
+  for (int t = threadIdx.x; t < nloc * Np * NV; t += blockDim.x)
+    res[(size_t)e0 * Np * NV + t] = sres[t];
 }
 
 // sum of r^2 * M^{+-1} per block, then one block reduces the partials in a
@@ -218,6 +210,7 @@ DevMesh dev_mesh(const eg_mesh* m) {
   d.lift = m->lift; d.dxidx = m->dxidx; d.ifaces = m->ifaces; d.nrm_face = m->nrm_face;
   d.bfaces = m->bfaces; d.nrm_bndry = m->nrm_bndry; d.qg_bndry = m->qg_bndry;
   d.eface = m->eface; d.Minv = m->Minv; d.w = m->w; d.jac = m->jac;
+  d.liftS = m->liftS; d.nbrinv = m->nbrinv; d.wface = m->wface; d.sparse_face = m->sparse_face;
   return d;
 }
 
@@ -227,8 +220,9 @@ int element_launch_shape(const eg_mesh* m, int* epb, int* threads, size_t* smem)
   if (e < 1) e = 1;
   *epb = e;
   *threads = e * m->Np;
-  *smem = sizeof(double) * ((size_t)m->dim * m->Np * m->Np + (size_t)m->F * m->Np * m->Nf +
-                            (size_t)e * m->dim * m->Np * nv);
+  *smem = sizeof(double) * ((size_t)m->dim * m->Np * m->Np + (size_t)m->F * m->Nf * m->S +
+                            (size_t)(m->F * m->S + 1) / 2 + (size_t)e * m->dim * m->Np * nv +
+                            (size_t)e * m->Np * nv);
   return EG_OK;
 }
 
@@ -254,6 +248,12 @@ int eg_launch_residual(eg_mesh* m, const double* q, double* res) {
   size_t smem;
   element_launch_shape(m, &epb, &threads, &smem);
   const int blocks = (m->E + epb - 1) / epb;
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_element<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_element<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    attr_set = true;
+  }
   if (m->dim == 2)
     k_element<2><<<blocks, threads, smem, m->stream>>>(md, q, m->fflux, res, m->status, epb);
   else

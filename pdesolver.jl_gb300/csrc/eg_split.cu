@@ -30,13 +30,17 @@ __global__ void k_split_element(DevMesh md, const double* __restrict__ q,
   extern __shared__ double smem[];
   const int Np = md.Np, Nf = md.Nf;
   const int P = Np * (Np - 1) / 2;
+  const int S = md.S;
   double* sQ = smem;                          // [DIM][Np][Np]
-  double* sL = sQ + DIM * Np * Np;            // [F][Np][Nf]
-  double* sq = sL + F * Np * Nf;              // [epb][Np][NV]
+  double* sL = sQ + DIM * Np * Np;            // [F][Nf][S]
+  int* sPerm = reinterpret_cast<int*>(sL + F * Nf * S);
+  double* sq = sL + F * Nf * S + (F * S + 1) / 2;  // [epb][Np][NV]
   double* sG = sq + (size_t)epb * Np * NV;    // [epb][P][NV]
-  short2* sPair = reinterpret_cast<short2*>(sG + (size_t)epb * P * NV);  // [P]
+  double* sres = sG + (size_t)epb * P * NV;   // [epb][Np][NV]
+  short2* sPair = reinterpret_cast<short2*>(sres + (size_t)epb * Np * NV);  // [P]
   for (int k = threadIdx.x; k < DIM * Np * Np; k += blockDim.x) sQ[k] = md.Q[k];
-  for (int k = threadIdx.x; k < F * Np * Nf; k += blockDim.x) sL[k] = md.lift[k];
+  for (int k = threadIdx.x; k < F * Nf * S; k += blockDim.x) sL[k] = md.liftS[k];
+  for (int k = threadIdx.x; k < F * S; k += blockDim.x) sPerm[k] = md.perm[k];
   for (int j = threadIdx.x; j < Np; j += blockDim.x)
     for (int k = 0; k < j; ++k) sPair[j * (j - 1) / 2 + k] = make_short2((short)j, (short)k);
   const int e0 = blockIdx.x * epb;
@@ -75,51 +79,37 @@ __global__ void k_split_element(DevMesh md, const double* __restrict__ q,
     for (int c = 0; c < NV; ++c) G[c] = Fp[c];
   }
   __syncthreads();
-  // ---- phase 2: rows + faces
-  const int le = threadIdx.x / Np, j = threadIdx.x - le * Np;
-  const int e = e0 + le;
-  if (le >= epb || e >= md.E) return;
-  const double* qj = sq + ((size_t)le * Np + j) * NV;
-  const double pj = eg::pressure<DIM>(g, qj);
-  if (!(qj[0] > 0.0)) atomicOr(status, EG_DEV_NEG_DENSITY);
-  if (!(pj > 0.0)) atomicOr(status, EG_DEV_NEG_PRESSURE);
-  double acc[NV];
+  // ---- phase 2: rows, then faces, then one coalesced store
+  {
+    const int le = threadIdx.x / Np, j = threadIdx.x - le * Np;
+    if (le < nloc) {
+      const double* qj = sq + ((size_t)le * Np + j) * NV;
+      const double pj = eg::pressure<DIM>(g, qj);
+      if (!(qj[0] > 0.0)) atomicOr(status, EG_DEV_NEG_DENSITY);
+      if (!(pj > 0.0)) atomicOr(status, EG_DEV_NEG_PRESSURE);
+      double acc[NV];
 #pragma unroll
-  for (int c = 0; c < NV; ++c) acc[c] = 0.0;
-  const double* Ge = sG + (size_t)le * P * NV;
-  for (int k = 0; k < j; ++k) {          // pair (j, k): res_j -= G
-    const double* G = Ge + (size_t)(j * (j - 1) / 2 + k) * NV;
+      for (int c = 0; c < NV; ++c) acc[c] = 0.0;
+      const double* Ge = sG + (size_t)le * P * NV;
+      for (int k = 0; k < j; ++k) {          // pair (j, k): res_j -= G
+        const double* G = Ge + (size_t)(j * (j - 1) / 2 + k) * NV;
 #pragma unroll
-    for (int c = 0; c < NV; ++c) acc[c] -= G[c];
-  }
-  for (int k = j + 1; k < Np; ++k) {     // pair (k, j): res_j += G
-    const double* G = Ge + (size_t)(k * (k - 1) / 2 + j) * NV;
-#pragma unroll
-    for (int c = 0; c < NV; ++c) acc[c] += G[c];
-  }
-#pragma unroll
-  for (int f = 0; f < F; ++f) {
-    const EFace ef = md.eface[(size_t)e * F + f];
-    const double* fl = fflux + (size_t)ef.slot * Nf * NV;
-    const double* lrow = sL + ((size_t)f * Np + j) * Nf;
-    if (ef.side == 0) {
-      for (int i = 0; i < Nf; ++i) {
-        const double a = -lrow[i];
-#pragma unroll
-        for (int c = 0; c < NV; ++c) acc[c] = fma(a, fl[i * NV + c], acc[c]);
+        for (int c = 0; c < NV; ++c) acc[c] -= G[c];
       }
-    } else {
-      const int* nb = md.nbrperm + ef.orient * Nf;
-      for (int i = 0; i < Nf; ++i) {
-        const double a = lrow[nb[i]];
+      for (int k = j + 1; k < Np; ++k) {     // pair (k, j): res_j += G
+        const double* G = Ge + (size_t)(k * (k - 1) / 2 + j) * NV;
 #pragma unroll
-        for (int c = 0; c < NV; ++c) acc[c] = fma(a, fl[i * NV + c], acc[c]);
+        for (int c = 0; c < NV; ++c) acc[c] += G[c];
       }
+      double* r = sres + ((size_t)le * Np + j) * NV;
+#pragma unroll
+      for (int c = 0; c < NV; ++c) r[c] = acc[c];
     }
   }
-  double* dst = res + ((size_t)e * Np + j) * NV;
-#pragma unroll
-  for (int c = 0; c < NV; ++c) dst[c] = acc[c];
+  __syncthreads();
+  face_lift_smem<DIM>(md, fflux, sres, sL, sPerm, e0, nloc);
+  for (int t = threadIdx.x; t < nloc * Np * NV; t += blockDim.x)
+    res[(size_t)e0 * Np * NV + t] = sres[t];
 }
 
 }  // namespace
@@ -131,8 +121,9 @@ int eg_launch_split_element(eg_mesh* m, const double* q, double* res) {
   int epb = 256 / Np;
   if (epb < 1) epb = 1;
   auto smem_of = [&](int e) {
-    return sizeof(double) * ((size_t)m->dim * Np * Np + (size_t)m->F * Np * m->Nf +
-                             (size_t)e * Np * nv + (size_t)e * P * nv) +
+    return sizeof(double) * ((size_t)m->dim * Np * Np + (size_t)m->F * m->Nf * m->S +
+                             (size_t)(m->F * m->S + 1) / 2 + (size_t)e * Np * nv +
+                             (size_t)e * P * nv + (size_t)e * Np * nv) +
            sizeof(short2) * (size_t)P;
   };
   while (epb > 1 && smem_of(epb) > 160 * 1024) --epb;

@@ -105,10 +105,10 @@ extern "C" int eg_reset_timings(eg_mesh* m) {
   return EG_OK;
 }
 
-extern "C" int eg_mesh_set_stream(eg_mesh* m, void* stream) {
+extern "C" int eg_mesh_set_stream(eg_mesh* m, void* stream, int32_t use_own) {
   if (!m) return EG_ERR_INVALID;
   EG_CUDA(cudaStreamSynchronize(m->stream));
-  m->stream = stream ? (cudaStream_t)stream : m->own_stream;
+  m->stream = use_own ? m->own_stream : (cudaStream_t)stream;
   return EG_OK;
 }
 

@@ -54,7 +54,7 @@ def _declare(lib):
     lib.eg_mesh_num_dof.restype = C.c_int64
     lib.eg_eval_residual.argtypes = [vp, vp, vp, C.c_double, C.c_int32]
     lib.eg_calc_norm.argtypes = [vp, vp, C.c_int32, C.c_int32, dp]
-    lib.eg_mesh_set_stream.argtypes = [vp, vp]
+    lib.eg_mesh_set_stream.argtypes = [vp, vp, C.c_int32]
     lib.eg_eval_residual_async.argtypes = [vp, vp, vp]
     lib.eg_sync.argtypes = [vp]
     lib.eg_set_timing.argtypes = [vp, C.c_int32]
@@ -136,8 +136,12 @@ class GPUMesh:
         return res
 
     def set_stream(self, stream_handle):
-        """run this mesh's work on a caller's CUDA stream (int handle; 0 = own)."""
-        check(self.lib.eg_mesh_set_stream(self.handle, C.c_void_p(stream_handle or None)))
+        """run this mesh's work on a caller's CUDA stream (an int handle, 0 =
+        CUDA's default stream), or on the library's own stream with None."""
+        if stream_handle is None:
+            check(self.lib.eg_mesh_set_stream(self.handle, None, 1))
+        else:
+            check(self.lib.eg_mesh_set_stream(self.handle, C.c_void_p(stream_handle), 0))
 
     def eval_residual_async(self, q_dev, res_dev):
         """enqueue R(q) with device tensors, no host synchronisation."""

@@ -78,7 +78,7 @@ def test_device_pointers_match_host_path(gpu_lib):
     g.eval_residual_async(qd, rd)
     g.sync()
     assert np.array_equal(rd.cpu().numpy(), res_h)
-    g.set_stream(0)
+    g.set_stream(None)
 
 
 def test_negative_density_reports_status(gpu_lib):
