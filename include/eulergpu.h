@@ -149,6 +149,14 @@ int eg_eval_residual(eg_mesh* mesh, const double* q, double* res, double t, int3
  */
 int eg_calc_norm(eg_mesh* mesh, const double* r, int32_t strongres, int32_t mem, double* out);
 
+/*
+ * Boundary functional: integral of the pressure over the faces of one
+ * boundary-condition group, sum_b sum_i wface_i p(q_face) |nrm_bndry|
+ * (the SBP face quadrature of the reference's integratefunctional!,
+ * boundary_functional.jl:82-126).  For the quarter annulus, group 0 is r = 1.
+ */
+int eg_calc_functional(eg_mesh* mesh, const double* q, int32_t bc_group, int32_t mem, double* out);
+
 /* ---- streams, asynchronous launch and phase timers ---------------------- */
 
 /* Run this mesh's work on `stream` (a cudaStream_t; NULL is CUDA's default
@@ -183,6 +191,119 @@ int eg_set_timing(eg_mesh* mesh, int32_t enable);
 /* synchronises the mesh stream, returns the sums since the last reset */
 int eg_get_timings(eg_mesh* mesh, eg_timings* out);
 int eg_reset_timings(eg_mesh* mesh);
+
+/* ---- Jacobian, preconditioner, Krylov solver ----------------------------
+ * Reference: src/linearsolvers/LinearSolvers.jl:68-660 (LinearSolver,
+ * AbstractPC, AbstractLO), ls_standard.jl:28-511, src/jacobian/jacobian.jl,
+ * src/NonlinearSolvers/preconditioning*.jl.
+ *
+ * The explicit Jacobian is stored element-block sparse: one dense
+ * (Np nv) x (Np nv) block per element (volume terms + the element's own face
+ * terms: the reference's element and LL/RR blocks) and two (S nv) x (S nv)
+ * coupling blocks per interface (LR, RL).  Blocks are column-major:
+ *   diag[e][col = m*nv + b][row = j*nv + a] = dR(e,j,a) / dq(e,m,b)
+ *   coupling[n][0][col = s'*nv + b][row = s*nv + a]
+ *       = dR(elementL, perm[faceL][s], a) / dq(elementR, perm[faceR][s'], b)
+ *   coupling[n][1][...] the same with L and R exchanged.
+ */
+typedef enum { EG_F64 = 0, EG_F32 = 1 } eg_precision;
+
+typedef struct eg_lo eg_lo;   /* explicit Jacobian operator (AbstractLO)   */
+typedef struct eg_pc eg_pc;   /* element block-Jacobi (NewtonBDiagPC)      */
+typedef struct eg_ls eg_ls;   /* right-preconditioned GMRES(m)             */
+
+int eg_lo_create(eg_mesh* mesh, int32_t precision, eg_lo** out);
+int eg_lo_destroy(eg_lo* lo);
+/* calcLinearOperator -> evalJacobian (reference evalJacobian.jl:6-72,
+   jacobian.jl:69-176): J = dR/dq at q, overwriting the blocks.
+   Weak-form volume (volume_integral_type 1), Roe or IR faces. */
+int eg_lo_calc(eg_lo* lo, const double* q, int32_t mem);
+/* applyLinearOperator: y = J x; x, y FP64 in host or device memory */
+int eg_lo_apply(eg_lo* lo, const double* x, double* y, int32_t mem);
+/* copy the blocks to host FP64 arrays: diag [E][Np nv][Np nv],
+   coupling [I][2][S nv][S nv] (either may be NULL) */
+int eg_lo_get_blocks(eg_lo* lo, double* diag, double* coupling);
+
+/* calcPC / applyPC of the element block-Jacobi preconditioner (reference
+   preconditioning.jl:7-139: LU with partial pivoting per element block).
+   The factors are turned into explicit block inverses so applyPC is a
+   batched dense matrix-vector product. */
+int eg_pc_create(eg_lo* lo, eg_pc** out);
+int eg_pc_destroy(eg_pc* pc);
+int eg_pc_calc(eg_pc* pc);
+int eg_pc_apply(eg_pc* pc, const double* x, double* y, int32_t mem);
+
+typedef struct {
+  int32_t iters;        /* total Krylov iterations                          */
+  int32_t restarts;
+  int32_t converged;    /* 1 if ||b - A x|| <= max(reltol ||b||, abstol)     */
+  int32_t reserved;
+  double res0;          /* ||b - A x0||                                     */
+  double res_final;     /* final (estimated) residual norm                  */
+} eg_ls_stats;
+
+/* GMRES(restart), right preconditioned, classical Gram-Schmidt with one
+   re-orthogonalisation (the reference uses PETSc GMRES(30) with modified
+   Gram-Schmidt, read_input.jl:559-569).  Vectors are in the operator's
+   precision; b and x are FP64 at the interface. */
+int eg_ls_create(eg_lo* lo, eg_pc* pc, int32_t restart, eg_ls** out);
+int eg_ls_destroy(eg_ls* ls);
+/* setTolerances (ls_standard.jl); negative values leave a field unchanged */
+int eg_ls_set_tolerances(eg_ls* ls, double reltol, double abstol, double dtol, int32_t itermax);
+/* linearSolve: x <- A^-1 b (x is also the initial guess) */
+int eg_ls_solve(eg_ls* ls, const double* b, double* x, int32_t mem, eg_ls_stats* stats);
+
+/* ---- Newton and RK4 drivers ------------------------------------------- */
+typedef struct {
+  double res_abstol;        /* opts["res_abstol"]  (read_input.jl:414)      */
+  double res_reltol;        /* opts["res_reltol"]                           */
+  double step_tol;          /* opts["step_tol"]                             */
+  double krylov_reltol;     /* opts["krylov_reltol"] (1e-2)                 */
+  int32_t itermax;          /* Newton iterations                            */
+  int32_t krylov_itermax;   /* opts["krylov_itermax"]                       */
+  int32_t gmres_restart;    /* 30                                           */
+  int32_t precision;        /* EG_F64: all FP64; EG_F32: FP32 Jacobian,
+                               preconditioner and Krylov, FP64 residual and
+                               update (inexact Newton)                      */
+  int32_t globalize_euler;  /* opts["newton_globalize_euler"]: pseudo-
+                               transient continuation, J - M/tau_vec with
+                               tau_vec = tau/(1 + sqrt(jac)) and tau scaled by
+                               |R|_{i-1}/|R|_i each iteration (reference
+                               globalization.jl:165-320)                    */
+  double euler_tau;         /* opts["euler_tau"], initial tau (1.0)          */
+} eg_newton_opts;
+
+typedef struct {
+  int32_t iters;            /* Newton iterations taken                      */
+  int32_t krylov_iters;     /* total GMRES iterations                       */
+  int32_t converged;
+  int32_t reserved;
+  double res_norm0;         /* calcNorm(R(q0), strongres) (physicsRhs)       */
+  double res_norm;          /* final                                        */
+  double step_norm;         /* last ||dq||_2                                */
+  double t_residual, t_jacobian, t_pc, t_krylov;   /* device ms per phase   */
+} eg_newton_stats;
+
+/* newton / newtonInner (reference src/NonlinearSolvers/newton.jl:54-304):
+   q <- q + dq until calcNorm(R(q), M^-1) < res_abstol, or the relative
+   norm < res_reltol, or ||dq|| <= step_tol.  q is FP64 in host or device
+   memory. */
+int eg_newton_solve(eg_mesh* mesh, double* q, int32_t mem, const eg_newton_opts* opts,
+                    eg_newton_stats* stats);
+
+typedef struct {
+  int32_t steps;            /* time steps taken                             */
+  int32_t reserved;
+  double t;                 /* final time                                   */
+  double res_norm;          /* last stage-1 norm sqrt(sum (M^-1 R)^2 M)     */
+} eg_rk4_stats;
+
+/* rk4 (reference src/NonlinearSolvers/rk4.jl:144-336, 404-456): classical
+   4-stage RK4 on dq/dt = M^-1 R(q) with step h for round(t_max/h) steps
+   (fewer if itermax > 0 is reached, or if res_tol > 0 and the stage-1 norm
+   drops below it). */
+int eg_rk4(eg_mesh* mesh, double* q, double h, double t_max, int32_t itermax, double res_tol,
+           int32_t mem, eg_rk4_stats* stats);
 
 #ifdef __cplusplus
 }

@@ -90,6 +90,7 @@ struct eg_mesh {
   cudaStream_t own_stream;  // the library's stream (stream may be a caller's)
   TimerState* timer;        // phase timers (null until enabled)
   int64_t launches;         // kernel launches since creation
+  int32_t h_bndry_offsets[64];  // host copy of the BC-group offsets
 };
 
 // phase timers: bracket a group of launches on m->stream

@@ -1,0 +1,270 @@
+// eg_jacobian.cu -- explicit Jacobian dR/dq of the weak-form Euler residual.
+//
+// Reference: evalJacobian (src/solver/euler/evalJacobian.jl:6-72) with
+//   calcVolumeIntegrals_nopre_diff  euler_funcs_diff.jl:54-103
+//   calcFaceIntegral_nopre_diff     flux_diff.jl:6-100 (interiorFaceCombined_jac!)
+//   getBCFluxes_diff                bc_diff.jl:16-212 (boundary: the Dirichlet
+//                                   state does not depend on q)
+//   assembleElement/Interface/Boundary  src/jacobian/jacobian.jl:822-1135, 1715-1800
+// The point flux Jacobians (dF/dq of calcEulerFlux, dF/dqL and dF/dqR of the
+// Roe / IR flux) are forward-mode derivatives of the device flux routines of
+// eg_physics.cuh (the reference differentiates the same routines by hand).
+//
+// Storage (element-block sparse, column-major blocks, see eulergpu.h):
+//   diag[E][Np*nv][Np*nv]          element blocks (volume + own face terms)
+//   cpl[I][2][S*nv][S*nv]          interface coupling blocks LR, RL
+// Kernels (templated on the precision T of the Jacobian: double or float):
+//   k_face_jac     one thread per (face slot, face node): dF/dqL, dF/dqR
+//   k_elem_jac     one CTA per element: sum_k Q_k(m,j) A_k(q_m) into a shared
+//                  block, then the element's own face terms, coalesced store
+//   k_couple_jac   one thread per coupling-block entry
+#include <vector>
+
+#include "eg_internal.h"
+#include "eg_kernels.cuh"
+#include "eg_linalg.h"
+#include "eg_physics.cuh"
+
+using eg::Fwd;
+using eg::Gas;
+
+namespace {
+
+// dF/dqL (and dF/dqR for interfaces) at every face node; dF[slot][i][side][a][b]
+template <int DIM, typename T>
+__global__ void k_face_jac(DevMesh md, const double* __restrict__ q, T* __restrict__ dF) {
+  constexpr int NV = DIM + 2;
+  using D2 = Fwd<T, 2 * NV>;
+  const int Nf = md.Nf, S = md.S, Np = md.Np;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (md.I + md.B) * Nf) return;
+  const int slot = t / Nf, i = t - slot * Nf;
+  const Gas g{md.gamma, md.gamma_1};
+  T qLr[NV], qRr[NV];
+#pragma unroll
+  for (int c = 0; c < NV; ++c) { qLr[c] = T(0); qRr[c] = T(0); }
+  T nrm[DIM];
+  const bool interior = slot < md.I;
+  if (interior) {
+    const int* itf = md.ifaces + 5 * slot;
+    const int eL = itf[0], eR = itf[1], fL = itf[2], fR = itf[3], o = itf[4];
+    const int iR = md.nbrperm[o * Nf + i];
+    const double* cL = md.interp + ((size_t)fL * Nf + i) * S;
+    const double* cR = md.interp + ((size_t)fR * Nf + iR) * S;
+    for (int s = 0; s < S; ++s) {
+      const T a = T(cL[s]), b = T(cR[s]);
+      const double* xa = q + ((size_t)eL * Np + md.perm[fL * S + s]) * NV;
+      const double* xb = q + ((size_t)eR * Np + md.perm[fR * S + s]) * NV;
+#pragma unroll
+      for (int c = 0; c < NV; ++c) {
+        qLr[c] += a * T(xa[c]);
+        qRr[c] += b * T(xb[c]);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) nrm[k] = T(md.nrm_face[((size_t)slot * Nf + i) * DIM + k]);
+  } else {
+    const int b = slot - md.I;
+    const int e = md.bfaces[2 * b], f = md.bfaces[2 * b + 1];
+    const double* cL = md.interp + ((size_t)f * Nf + i) * S;
+    for (int s = 0; s < S; ++s) {
+      const T a = T(cL[s]);
+      const double* xa = q + ((size_t)e * Np + md.perm[f * S + s]) * NV;
+#pragma unroll
+      for (int c = 0; c < NV; ++c) qLr[c] += a * T(xa[c]);
+    }
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) nrm[k] = T(md.nrm_bndry[((size_t)b * Nf + i) * DIM + k]);
+#pragma unroll
+    for (int c = 0; c < NV; ++c) qRr[c] = T(md.qg_bndry[((size_t)b * Nf + i) * NV + c]);
+  }
+  D2 qL[NV], qR[NV], fl[NV];
+#pragma unroll
+  for (int c = 0; c < NV; ++c) {
+    qL[c] = D2(qLr[c]);
+    qR[c] = D2(qRr[c]);
+    qL[c].d[c] = T(1);
+    if (interior) qR[c].d[NV + c] = T(1);
+  }
+  if (!interior || md.face_flux == EG_FLUX_ROE) {
+    eg::roe_flux<DIM>(g, qL, qR, nrm, fl);
+  } else {
+    auto av = eg::ir_average<DIM>(g, qL, qR);
+    eg::ir_dir<DIM>(av, nrm, fl);
+  }
+  T* out = dF + (size_t)t * 2 * NV * NV;
+#pragma unroll
+  for (int a = 0; a < NV; ++a)
+#pragma unroll
+    for (int b = 0; b < NV; ++b) {
+      out[a * NV + b] = fl[a].d[b];
+      out[NV * NV + a * NV + b] = fl[a].d[NV + b];
+    }
+}
+
+// Element block: one CTA per element.  Shared: A[k][m][a][b] (flux
+// Jacobians at the nodes), the block blk[col][row] and face tables.
+template <int DIM, typename T>
+__global__ void k_elem_jac(DevMesh md, const double* __restrict__ q, const T* __restrict__ dF,
+                           T* __restrict__ diag) {
+  constexpr int NV = DIM + 2;
+  constexpr int F = DIM + 1;
+  using D1 = Fwd<T, NV>;
+  extern __shared__ unsigned char smraw[];
+  const int Np = md.Np, Nf = md.Nf, S = md.S;
+  const int n = Np * NV;
+  T* sA = reinterpret_cast<T*>(smraw);               // [DIM][Np][NV][NV]
+  T* sB = sA + (size_t)DIM * Np * NV * NV;            // [n][n] col-major
+  const int e = blockIdx.x;
+  const Gas g{md.gamma, md.gamma_1};
+  // flux Jacobians A_k(q_m) = dF_k/dq at node m, direction dxidx[.][k]
+  for (int t = threadIdx.x; t < Np * DIM; t += blockDim.x) {
+    const int m = t / DIM, k = t - m * DIM;
+    const double* src = q + ((size_t)e * Np + m) * NV;
+    D1 qm[NV], Fk[NV];
+#pragma unroll
+    for (int c = 0; c < NV; ++c) {
+      qm[c] = D1(T(src[c]));
+      qm[c].d[c] = T(1);
+    }
+    const double* dx = md.dxidx + ((size_t)e * Np + m) * DIM * DIM;
+    T dir[DIM];
+#pragma unroll
+    for (int pp = 0; pp < DIM; ++pp) dir[pp] = T(dx[pp * DIM + k]);
+    eg::euler_flux<DIM>(g, qm, dir, Fk);
+    T* A = sA + (((size_t)k * Np + m) * NV) * NV;
+#pragma unroll
+    for (int a = 0; a < NV; ++a)
+#pragma unroll
+      for (int b = 0; b < NV; ++b) A[a * NV + b] = Fk[a].d[b];
+  }
+  __syncthreads();
+  // volume: blk[(m,b)][(j,a)] = sum_k Q_k(m, j) A_k(m)[a][b];  Q[k][j][m] = Q_k(m, j)
+  for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+    const int col = t / n, row = t - col * n;
+    const int m = col / NV, b = col - m * NV;
+    const int j = row / NV, a = row - j * NV;
+    T acc = T(0);
+#pragma unroll
+    for (int k = 0; k < DIM; ++k)
+      acc += T(md.Q[((size_t)k * Np + j) * Np + m]) * sA[(((size_t)k * Np + m) * NV + a) * NV + b];
+    sB[t] = acc;
+  }
+  __syncthreads();
+  // the element's own face terms (LL for elementL / boundary, RR for elementR)
+  for (int f = 0; f < F; ++f) {
+    const EFace ef = md.eface[(size_t)e * F + f];
+    const T* dFs = dF + (size_t)ef.slot * Nf * 2 * NV * NV;
+    const int sideoff = ef.side ? NV * NV : 0;  // dF/dq of this element's state
+    const T sgn = ef.side ? T(1) : T(-1);
+    const int* nb = md.nbrperm + ef.orient * Nf;
+    for (int t = threadIdx.x; t < S * S * NV * NV; t += blockDim.x) {
+      const int ab = t % (NV * NV), ss = t / (NV * NV);
+      const int s = ss / S, sp = ss - s * S;        // row stencil s, column stencil s'
+      const int a = ab / NV, b = ab - a * NV;
+      T acc = T(0);
+      for (int i = 0; i < Nf; ++i) {
+        const int ii = ef.side ? nb[i] : i;         // this element's face-node index
+        const T l = T(md.liftS[((size_t)f * Nf + ii) * S + s]);
+        const T r = T(md.interp[((size_t)f * Nf + ii) * S + sp]);
+        acc += l * r * dFs[(size_t)i * 2 * NV * NV + sideoff + a * NV + b];
+      }
+      const int row = md.perm[f * S + s] * NV + a;
+      const int col = md.perm[f * S + sp] * NV + b;
+      sB[(size_t)col * n + row] += sgn * acc;
+    }
+    __syncthreads();
+  }
+  T* dst = diag + (size_t)e * n * n;
+  for (int t = threadIdx.x; t < n * n; t += blockDim.x) dst[t] = sB[t];
+}
+
+// Interface coupling blocks.  cpl[nI][side][col = s'*NV+b][row = s*NV+a]:
+//   side 0: rows elementL stencil, cols elementR stencil, from dF/dqR, sign -
+//   side 1: rows elementR stencil, cols elementL stencil, from dF/dqL, sign +
+template <int DIM, typename T>
+__global__ void k_couple_jac(DevMesh md, const T* __restrict__ dF, T* __restrict__ cpl) {
+  constexpr int NV = DIM + 2;
+  const int Nf = md.Nf, S = md.S;
+  const int nb = S * NV;
+  const int64_t per = 2LL * nb * nb;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= per * md.I) return;
+  const int nI = (int)(t / per);
+  const int rem = (int)(t - (int64_t)nI * per);
+  const int side = rem / (nb * nb);
+  const int cr = rem - side * nb * nb;
+  const int col = cr / nb, row = cr - col * nb;
+  const int sp = col / NV, b = col - sp * NV;
+  const int s = row / NV, a = row - s * NV;
+  const int* itf = md.ifaces + 5 * nI;
+  const int fL = itf[2], fR = itf[3], o = itf[4];
+  const int* nbp = md.nbrperm + o * Nf;
+  const T* dFs = dF + (size_t)nI * Nf * 2 * NV * NV;
+  T acc = T(0);
+  for (int i = 0; i < Nf; ++i) {
+    const int iR = nbp[i];
+    T l, r;
+    int off;
+    if (side == 0) {
+      l = T(md.liftS[((size_t)fL * Nf + i) * S + s]);
+      r = T(md.interp[((size_t)fR * Nf + iR) * S + sp]);
+      off = NV * NV;
+    } else {
+      l = T(md.liftS[((size_t)fR * Nf + iR) * S + s]);
+      r = T(md.interp[((size_t)fL * Nf + i) * S + sp]);
+      off = 0;
+    }
+    acc += l * r * dFs[(size_t)i * 2 * NV * NV + off + a * NV + b];
+  }
+  cpl[t] = side == 0 ? -acc : acc;
+}
+
+template <typename T>
+int launch_jac(eg_lo* lo, const double* q) {
+  eg_mesh* m = lo->mesh;
+  DevMesh md = dev_mesh(m);
+  T* dF = reinterpret_cast<T*>(lo->dF);
+  T* diag = reinterpret_cast<T*>(lo->diag);
+  T* cpl = reinterpret_cast<T*>(lo->cpl);
+  const int nslot = (m->I + m->B) * m->Nf;
+  const int n = m->Np * m->nv;
+  const size_t smem = sizeof(T) * ((size_t)m->dim * m->Np * m->nv * m->nv + (size_t)n * n);
+  eg_phase_begin(m, EG_PHASE_OTHER);
+  if (m->dim == 2) {
+    k_face_jac<2, T><<<(nslot + 127) / 128, 128, 0, m->stream>>>(md, q, dF);
+    cudaFuncSetAttribute(k_elem_jac<2, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    k_elem_jac<2, T><<<m->E, 256, smem, m->stream>>>(md, q, dF, diag);
+  } else {
+    k_face_jac<3, T><<<(nslot + 127) / 128, 128, 0, m->stream>>>(md, q, dF);
+    cudaFuncSetAttribute(k_elem_jac<3, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    k_elem_jac<3, T><<<m->E, 256, smem, m->stream>>>(md, q, dF, diag);
+  }
+  const int64_t ncpl = 2LL * (m->S * m->nv) * (m->S * m->nv) * m->I;
+  if (ncpl > 0) {
+    const int blocks = (int)((ncpl + 255) / 256);
+    if (m->dim == 2)
+      k_couple_jac<2, T><<<blocks, 256, 0, m->stream>>>(md, dF, cpl);
+    else
+      k_couple_jac<3, T><<<blocks, 256, 0, m->stream>>>(md, dF, cpl);
+  }
+  eg_phase_end(m, EG_PHASE_OTHER, ncpl > 0 ? 3 : 2);
+  return EG_OK;
+}
+
+}  // namespace
+
+int eg_jacobian_launch(eg_lo* lo, const double* q) {
+  const size_t smem_needed = (lo->prec == EG_F64 ? 8 : 4) *
+                             ((size_t)lo->mesh->dim * lo->mesh->Np * lo->mesh->nv * lo->mesh->nv +
+                              (size_t)lo->n * lo->n);
+  if (smem_needed > 200 * 1024) {
+    eg_set_error("evalJacobian: element block of %d unknowns exceeds shared memory", lo->n);
+    return EG_ERR_UNSUPPORTED;
+  }
+  if (lo->mesh->params.volume_integral_type != 1) {
+    eg_set_error("evalJacobian: only the weak-form volume integral (type 1) is differentiated");
+    return EG_ERR_UNSUPPORTED;
+  }
+  return lo->prec == EG_F64 ? launch_jac<double>(lo, q) : launch_jac<float>(lo, q);
+}

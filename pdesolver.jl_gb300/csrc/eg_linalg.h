@@ -1,0 +1,58 @@
+// eg_linalg.h -- Jacobian operator, block-Jacobi preconditioner and GMRES
+// objects behind the eg_lo / eg_pc / eg_ls handles of the C ABI.
+#pragma once
+#include "eg_internal.h"
+
+struct eg_lo {
+  eg_mesh* mesh;
+  int prec;        // EG_F64 / EG_F32
+  int n;           // Np * nv: element block size
+  int nb;          // S * nv: coupling block size
+  void* diag;      // [E][n][n] column-major element blocks
+  void* cpl;       // [I][2][nb][nb] column-major coupling blocks
+  void* dF;        // [(I+B)][Nf][2][nv][nv] point flux Jacobians
+  int32_t* spos;   // [F][Np]: stencil position of node j on face f, or -1
+  void* xT;        // [ndof] operand in the operator precision
+  void* yT;        // [ndof]
+  double* xd;      // [ndof] FP64 staging
+  double* yd;      // [ndof]
+  bool valid;      // blocks computed
+};
+
+struct eg_pc {
+  eg_lo* lo;
+  void* inv;       // [E][n][n] column-major inverses of the element blocks
+  bool valid;
+};
+
+struct eg_ls {
+  eg_lo* lo;
+  eg_pc* pc;
+  int m;           // restart length
+  double reltol, abstol, dtol;
+  int itermax;
+  void* V;         // [(m+1)][ndof]
+  void* w;         // [ndof]
+  void* z;         // [ndof]
+  void* xT;        // [ndof]
+  void* bT;        // [ndof]
+  void* part;      // [nblk][m+2] partial sums (operator precision)
+  void* h;         // [m+2] device Hessenberg column (operator precision)
+  double* hh;      // pinned host copy [m+2]
+  void* y;         // [m+1] device least-squares solution
+  double* xd;      // [ndof] FP64 staging
+  double* bd;      // [ndof]
+  int nblk;
+};
+
+// kernels shared across translation units
+int eg_jacobian_launch(eg_lo* lo, const double* q);
+// y = J x in the operator precision (device pointers of that precision)
+int eg_lo_apply_T(eg_lo* lo, const void* x, void* y);
+// y = M^-1 x in the operator precision
+int eg_pc_apply_T(eg_pc* pc, const void* x, void* y);
+// precision conversion helpers (device)
+int eg_convert(eg_mesh* m, const double* src, void* dst, int prec, int64_t n, double scale);
+int eg_convert_back(eg_mesh* m, const void* src, double* dst, int prec, int64_t n);
+// x_T <- GMRES solution of J x = b_T; returns status, fills stats
+int eg_gmres_T(eg_ls* ls, const void* bT, void* xT, eg_ls_stats* st);

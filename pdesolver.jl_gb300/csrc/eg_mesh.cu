@@ -106,6 +106,10 @@ extern "C" int eg_mesh_create(const eg_mesh_desc* d, const eg_params* params, eg
     eg_set_error("eg_mesh_create: dim must be 2 or 3 (got %d)", d->dim);
     return EG_ERR_INVALID;
   }
+  if (d->num_bc > 63) {
+    eg_set_error("eg_mesh_create: at most 63 boundary-condition groups");
+    return EG_ERR_INVALID;
+  }
   if (d->num_el <= 0 || d->nodes_per_el <= 0 || d->nodes_per_el > EG_MAX_NP ||
       d->nodes_per_face <= 0 || d->nodes_per_face > EG_MAX_NF || d->stencil_size <= 0 ||
       d->stencil_size > EG_MAX_S || d->num_interfaces < 0 || d->num_bndry < 0 ||
@@ -200,6 +204,7 @@ extern "C" int eg_mesh_create(const eg_mesh_desc* d, const eg_params* params, eg
       free_mesh(m);
       return EG_ERR_INVALID;
     }
+  for (int g = 0; g <= m->nbc; ++g) m->h_bndry_offsets[g] = d->bndry_offsets[g];
   for (int g = 0; g < m->nbc; ++g) {
     int bct = d->bc_types[g];
     if (bct != EG_BC_VORTEX && bct != EG_BC_FREESTREAM) {

@@ -11,6 +11,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 namespace eg {
 
 // ---------------------------------------------------------------------------
@@ -57,29 +59,38 @@ __host__ __device__ __forceinline__ Fwd<R, N> operator-(const Fwd<R, N>& a) {
   for (int i = 0; i < N; ++i) r.d[i] = -a.d[i];
   return r;
 }
-// mixed with plain scalars
-template <typename R, int N>
-__host__ __device__ __forceinline__ Fwd<R, N> operator*(const Fwd<R, N>& a, R b) {
+// mixed with plain scalars (any arithmetic type, converted to R so an FP32
+// carrier never issues FP64 instructions)
+template <typename S>
+struct IsScalar { static constexpr bool value = false; };
+template <> struct IsScalar<double> { static constexpr bool value = true; };
+template <> struct IsScalar<float> { static constexpr bool value = true; };
+template <> struct IsScalar<int> { static constexpr bool value = true; };
+#define EG_SCALAR_OK(S) typename = typename std::enable_if<IsScalar<S>::value>::type
+
+template <typename R, int N, typename S, EG_SCALAR_OK(S)>
+__host__ __device__ __forceinline__ Fwd<R, N> operator*(const Fwd<R, N>& a, S bs) {
+  const R b = R(bs);
   Fwd<R, N> r;
   r.v = a.v * b;
 #pragma unroll
   for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * b;
   return r;
 }
-template <typename R, int N>
-__host__ __device__ __forceinline__ Fwd<R, N> operator*(R b, const Fwd<R, N>& a) { return a * b; }
-template <typename R, int N>
-__host__ __device__ __forceinline__ Fwd<R, N> operator+(const Fwd<R, N>& a, R b) { Fwd<R, N> r = a; r.v = a.v + b; return r; }
-template <typename R, int N>
-__host__ __device__ __forceinline__ Fwd<R, N> operator+(R b, const Fwd<R, N>& a) { Fwd<R, N> r = a; r.v = b + a.v; return r; }
-template <typename R, int N>
-__host__ __device__ __forceinline__ Fwd<R, N> operator-(const Fwd<R, N>& a, R b) { Fwd<R, N> r = a; r.v = a.v - b; return r; }
-template <typename R, int N>
-__host__ __device__ __forceinline__ Fwd<R, N> operator-(R b, const Fwd<R, N>& a) { return Fwd<R, N>(b) - a; }
-template <typename R, int N>
-__host__ __device__ __forceinline__ Fwd<R, N> operator/(const Fwd<R, N>& a, R b) { return a * (R(1) / b); }
-template <typename R, int N>
-__host__ __device__ __forceinline__ Fwd<R, N> operator/(R a, const Fwd<R, N>& b) { return Fwd<R, N>(a) / b; }
+template <typename R, int N, typename S, EG_SCALAR_OK(S)>
+__host__ __device__ __forceinline__ Fwd<R, N> operator*(S b, const Fwd<R, N>& a) { return a * b; }
+template <typename R, int N, typename S, EG_SCALAR_OK(S)>
+__host__ __device__ __forceinline__ Fwd<R, N> operator+(const Fwd<R, N>& a, S b) { Fwd<R, N> r = a; r.v = a.v + R(b); return r; }
+template <typename R, int N, typename S, EG_SCALAR_OK(S)>
+__host__ __device__ __forceinline__ Fwd<R, N> operator+(S b, const Fwd<R, N>& a) { Fwd<R, N> r = a; r.v = R(b) + a.v; return r; }
+template <typename R, int N, typename S, EG_SCALAR_OK(S)>
+__host__ __device__ __forceinline__ Fwd<R, N> operator-(const Fwd<R, N>& a, S b) { Fwd<R, N> r = a; r.v = a.v - R(b); return r; }
+template <typename R, int N, typename S, EG_SCALAR_OK(S)>
+__host__ __device__ __forceinline__ Fwd<R, N> operator-(S b, const Fwd<R, N>& a) { return Fwd<R, N>(R(b)) - a; }
+template <typename R, int N, typename S, EG_SCALAR_OK(S)>
+__host__ __device__ __forceinline__ Fwd<R, N> operator/(const Fwd<R, N>& a, S b) { return a * (R(1) / R(b)); }
+template <typename R, int N, typename S, EG_SCALAR_OK(S)>
+__host__ __device__ __forceinline__ Fwd<R, N> operator/(S a, const Fwd<R, N>& b) { return Fwd<R, N>(R(a)) / b; }
 
 template <typename R, int N>
 __host__ __device__ __forceinline__ Fwd<R, N> sqrt(const Fwd<R, N>& a) {
@@ -115,31 +126,41 @@ __host__ __device__ __forceinline__ float val(float a) { return a; }
 using ::sqrt;
 using ::log;
 
+// real (non-derivative) type of a scalar
+template <typename T> struct RealOf { using type = T; };
+template <typename R, int N> struct RealOf<Fwd<R, N>> { using type = R; };
+
 // gas constants as seen by the kernels
 struct Gas {
   double gamma, gamma_1;
 };
 
 // ---------------------------------------------------------------------------
+// Every literal below is converted to R = RealOf<T>, so an FP32 instantiation
+// is FP32 throughout and the FP64 one is FP64 throughout.
 template <int DIM, typename T>
 __device__ __forceinline__ T pressure(const Gas& g, const T* q) {
-  if (DIM == 2) return g.gamma_1 * (q[3] - 0.5 * (q[1] * q[1] + q[2] * q[2]) / q[0]);
-  return g.gamma_1 * (q[4] - 0.5 * (q[1] * q[1] + q[2] * q[2] + q[3] * q[3]) / q[0]);
+  using R = typename RealOf<T>::type;
+  const R h = R(0.5), g1 = R(g.gamma_1);
+  if (DIM == 2) return g1 * (q[3] - h * (q[1] * q[1] + q[2] * q[2]) / q[0]);
+  return g1 * (q[4] - h * (q[1] * q[1] + q[2] * q[2] + q[3] * q[3]) / q[0]);
 }
 
 // F . dir for the Euler equations (conservative variables)
 template <int DIM, typename T, typename Tn>
 __device__ __forceinline__ void euler_flux(const Gas& g, const T* q, const Tn* dir, T* F) {
-  const T r = 1.0 / q[0];
+  using R = typename RealOf<T>::type;
+  const R h = R(0.5), g1 = R(g.gamma_1);
+  const T r = R(1) / q[0];
   if (DIM == 2) {
-    T press = g.gamma_1 * (q[3] - 0.5 * (q[1] * q[1] + q[2] * q[2]) * r);
+    T press = g1 * (q[3] - h * (q[1] * q[1] + q[2] * q[2]) * r);
     T U = (q[1] * dir[0] + q[2] * dir[1]) * r;
     F[0] = q[0] * U;
     F[1] = q[1] * U + dir[0] * press;
     F[2] = q[2] * U + dir[1] * press;
     F[3] = (q[3] + press) * U;
   } else {
-    T press = g.gamma_1 * (q[4] - 0.5 * (q[1] * q[1] + q[2] * q[2] + q[3] * q[3]) * r);
+    T press = g1 * (q[4] - h * (q[1] * q[1] + q[2] * q[2] + q[3] * q[3]) * r);
     T U = (q[1] * dir[0] + q[2] * dir[1] + q[3] * dir[2]) * r;
     F[0] = q[0] * U;
     F[1] = q[1] * U + dir[0] * press;
@@ -150,42 +171,43 @@ __device__ __forceinline__ void euler_flux(const Gas& g, const T* q, const Tn* d
 }
 
 // Roe flux: F(qL).n + 0.5 (|A_hat| - A_hat)(qL - qR), eigenvalue floors 0.025.
-// Arranged to spend few FP64 divisions (the scarce resource on GB300): one
+// Arranged to spend few divisions (FP64 is the scarce resource on GB300): one
 // reciprocal per state density, 1/(sqL+sqR), 1/(n.n), 1/(H - phi) (= gami/a^2)
 // and 1/(dA a); the Euler flux of qL reuses 1/rho_L.
 template <int DIM, typename T, typename Tn>
 __device__ __forceinline__ void roe_flux(const Gas& g, const T* q, const T* qg, const Tn* nrm, T* flux) {
+  using R = typename RealOf<T>::type;
   constexpr int NV = DIM + 2;
-  const double gamma = g.gamma, gami = g.gamma_1;
-  const double sat_V = 0.025;
+  const R gamma = R(g.gamma), gami = R(g.gamma_1), h = R(0.5), one = R(1);
+  const R sat_V = R(0.025);
   // Roe averages
-  const T rL = 1.0 / q[0];
+  const T rL = one / q[0];
   T uL = q[1] * rL, vL = q[2] * rL;
-  T wL = (DIM == 3) ? q[3] * rL : T(0.0);
-  T phiL = 0.5 * (uL * uL + vL * vL + wL * wL);
+  T wL = (DIM == 3) ? q[3] * rL : T(R(0));
+  T phiL = h * (uL * uL + vL * vL + wL * wL);
   T HL = gamma * q[NV - 1] * rL - gami * phiL;
-  const T rR = 1.0 / qg[0];
+  const T rR = one / qg[0];
   T uR = qg[1] * rR, vR = qg[2] * rR;
-  T wR = (DIM == 3) ? qg[3] * rR : T(0.0);
-  T phiR = 0.5 * (uR * uR + vR * vR + wR * wR);
+  T wR = (DIM == 3) ? qg[3] * rR : T(R(0));
+  T phiR = h * (uR * uR + vR * vR + wR * wR);
   T HR = gamma * qg[NV - 1] * rR - gami * phiR;
   T sqL = sqrt(q[0]);
   T sqR = sqrt(qg[0]);
-  T fac = 1.0 / (sqL + sqR);
+  T fac = one / (sqL + sqR);
   T u = (sqL * uL + sqR * uR) * fac;
   T v = (sqL * vL + sqR * vR) * fac;
-  T w = (DIM == 3) ? (sqL * wL + sqR * wR) * fac : T(0.0);
+  T w = (DIM == 3) ? (sqL * wL + sqR * wR) * fac : T(R(0));
   T H = (sqL * HL + sqR * HR) * fac;
   T dq[NV];
 #pragma unroll
   for (int i = 0; i < NV; ++i) dq[i] = q[i] - qg[i];
   // SAT
   Tn nx = nrm[0], ny = nrm[1];
-  Tn nz = (DIM == 3) ? nrm[2] : Tn(0.0);
+  Tn nz = (DIM == 3) ? nrm[2] : Tn(0);
   Tn n2 = nx * nx + ny * ny + nz * nz;
   Tn dA = sqrt(n2);
   T Un = u * nx + v * ny + w * nz;
-  T phi = 0.5 * (u * u + v * v + w * w);
+  T phi = h * (u * u + v * v + w * w);
   T Hp = H - phi;
   T a = sqrt(gami * Hp);
   T dAa = dA * a;
@@ -193,9 +215,9 @@ __device__ __forceinline__ void roe_flux(const Gas& g, const T* q, const T* qg, 
   T lambda2 = Un - dAa;
   T lambda3 = Un;
   T rhoA = absval(Un) + dAa;
-  lambda1 = 0.5 * (maxval(absval(lambda1), sat_V * rhoA) - lambda1);
-  lambda2 = 0.5 * (maxval(absval(lambda2), sat_V * rhoA) - lambda2);
-  lambda3 = 0.5 * (maxval(absval(lambda3), sat_V * rhoA) - lambda3);
+  lambda1 = h * (maxval(absval(lambda1), sat_V * rhoA) - lambda1);
+  lambda2 = h * (maxval(absval(lambda2), sat_V * rhoA) - lambda2);
+  lambda3 = h * (maxval(absval(lambda3), sat_V * rhoA) - lambda3);
   T dqE, dqN;
   if (DIM == 2) {
     dqE = phi * dq[0] - u * dq[1] - v * dq[2] + dq[3];
@@ -204,16 +226,20 @@ __device__ __forceinline__ void roe_flux(const Gas& g, const T* q, const T* qg, 
     dqE = phi * dq[0] - u * dq[1] - v * dq[2] - w * dq[3] + dq[4];
     dqN = -Un * dq[0] + nx * dq[1] + ny * dq[2] + nz * dq[3];
   }
-  T t1 = 0.5 * (lambda1 + lambda2) - lambda3;
-  T t2 = 1.0 / Hp;                 // gami / a^2
-  Tn t3 = 1.0 / n2;                // 1 / dA^2
-  T t4 = 0.5 * (lambda1 - lambda2) / dAa;
+  T t1 = h * (lambda1 + lambda2) - lambda3;
+  T t2 = one / Hp;                 // gami / a^2
+  Tn t3 = Tn(1) / n2;              // 1 / dA^2
+  T t4 = h * (lambda1 - lambda2) / dAa;
   // sat = l3 dq + t1 (t2 E1dq + t3 E2dq) + t4 (E3dq + gami E4dq)
   T c1 = t1 * t2 * dqE + t4 * dqN;        // coefficient of (1, u, v, w, H)
   T c2 = t1 * t3 * dqN + t4 * gami * dqE; // coefficient of (0, nx, ny, nz, Un)
   // Euler flux of qL in direction n, reusing 1/rho_L
-  T pL = gami * (q[NV - 1] - 0.5 * (q[1] * q[1] + q[2] * q[2] + ((DIM == 3) ? q[3] * q[3] : T(0.0))) * rL);
-  T UL = (q[1] * nx + q[2] * ny + ((DIM == 3) ? q[3] * nz : T(0.0))) * rL;
+  T ke = q[1] * q[1] + q[2] * q[2];
+  if (DIM == 3) ke = ke + q[3] * q[3];
+  T pL = gami * (q[NV - 1] - h * ke * rL);
+  T UL = q[1] * nx + q[2] * ny;
+  if (DIM == 3) UL = UL + q[3] * nz;
+  UL = UL * rL;
   flux[0] = q[0] * UL + lambda3 * dq[0] + c1;
   flux[1] = q[1] * UL + nx * pL + lambda3 * dq[1] + c1 * u + c2 * nx;
   flux[2] = q[2] * UL + ny * pL + lambda3 * dq[2] + c1 * v + c2 * ny;
@@ -224,16 +250,18 @@ __device__ __forceinline__ void roe_flux(const Gas& g, const T* q, const T* qg, 
 // logarithmic mean with the 5-term series below u = 1e-3
 template <typename T>
 __device__ __forceinline__ T logavg(const T& aL, const T& aR) {
+  using R = typename RealOf<T>::type;
+  const R one = R(1);
   T xi = aL / aR;
-  T f = (xi - 1.0) / (xi + 1.0);
+  T f = (xi - one) / (xi + one);
   T u = f * f;
   T F;
-  if (val(u) < 1e-3) {
-    F = 1.0 + u * (1.0 / 3.0 + u * (1.0 / 5.0 + u * (1.0 / 7.0 + u * (1.0 / 9.0))));
+  if (val(u) < R(1e-3)) {
+    F = one + u * (R(1.0 / 3.0) + u * (R(1.0 / 5.0) + u * (R(1.0 / 7.0) + u * R(1.0 / 9.0))));
   } else {
-    F = (log(xi) * 0.5) / f;
+    F = (log(xi) * R(0.5)) / f;
   }
-  return (aL + aR) / (2.0 * F);
+  return (aL + aR) / (R(2) * F);
 }
 
 // Ismail-Roe flux: shared averages, then NDIR directions dir[d*DIM + k]
@@ -244,28 +272,30 @@ struct IRAvg {
 
 template <int DIM, typename T>
 __device__ __forceinline__ IRAvg<DIM, T> ir_average(const Gas& g, const T* qL, const T* qR) {
-  const double gamma = g.gamma, gamma_1 = g.gamma_1;
+  using R = typename RealOf<T>::type;
+  const R gamma = R(g.gamma), gamma_1 = R(g.gamma_1), h = R(0.5), one = R(1);
   T pL = pressure<DIM>(g, qL), pR = pressure<DIM>(g, qR);
   T z1L = sqrt(qL[0] / pL), z1R = sqrt(qR[0] / pR);
   T zpL = sqrt(qL[0] * pL), zpR = sqrt(qR[0] * pR);
-  T iz = 1.0 / (z1L + z1R);
+  T iz = one / (z1L + z1R);
   IRAvg<DIM, T> r;
   T lp = logavg(zpL, zpR);
-  r.rho_hat = 0.5 * (z1L + z1R) * lp;
+  r.rho_hat = h * (z1L + z1R) * lp;
   r.u_hat = (z1L * qL[1] / qL[0] + z1R * qR[1] / qR[0]) * iz;
   r.v_hat = (z1L * qL[2] / qL[0] + z1R * qR[2] / qR[0]) * iz;
-  r.w_hat = (DIM == 3) ? (z1L * qL[3] / qL[0] + z1R * qR[3] / qR[0]) * iz : T(0.0);
+  r.w_hat = (DIM == 3) ? (z1L * qL[3] / qL[0] + z1R * qR[3] / qR[0]) * iz : T(R(0));
   r.p1_hat = (zpL + zpR) * iz;
-  T p2_hat = ((gamma + 1) / (2 * gamma)) * lp / logavg(z1L, z1R) + (gamma_1 / (2 * gamma)) * (zpL + zpR) * iz;
+  T p2_hat = R((g.gamma + 1) / (2 * g.gamma)) * lp / logavg(z1L, z1R) +
+             R(g.gamma_1 / (2 * g.gamma)) * (zpL + zpR) * iz;
   r.h_hat = gamma * p2_hat / (r.rho_hat * gamma_1) +
-            0.5 * (r.u_hat * r.u_hat + r.v_hat * r.v_hat + r.w_hat * r.w_hat);
+            h * (r.u_hat * r.u_hat + r.v_hat * r.v_hat + r.w_hat * r.w_hat);
   return r;
 }
 
 template <int DIM, typename T, typename Tn>
 __device__ __forceinline__ void ir_dir(const IRAvg<DIM, T>& a, const Tn* n, T* F) {
   constexpr int NV = DIM + 2;
-  Tn nz = (DIM == 3) ? n[2] : Tn(0.0);
+  Tn nz = (DIM == 3) ? n[2] : Tn(0);
   T mv_n = a.rho_hat * (n[0] * a.u_hat + n[1] * a.v_hat + nz * a.w_hat);
   F[0] = mv_n;
   F[1] = mv_n * a.u_hat + n[0] * a.p1_hat;

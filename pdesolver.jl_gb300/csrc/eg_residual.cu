@@ -168,7 +168,7 @@ __global__ void k_norm_partial(const double* __restrict__ r, const double* __res
   double s = 0.0;
   for (int64_t n = blockIdx.x * (int64_t)NT + threadIdx.x; n < nnode; n += (int64_t)gridDim.x * NT) {
     const double mi = Minv[n];
-    const double fac = strongres ? mi : 1.0 / mi;
+    const double fac = strongres == 2 ? 1.0 : (strongres ? mi : 1.0 / mi);
     double t = 0.0;
     for (int c = 0; c < nv; ++c) {
       const double x = r[n * nv + c];
@@ -197,6 +197,57 @@ __global__ void k_norm_final(const double* __restrict__ part, int n, double* __r
     __syncthreads();
   }
   if (threadIdx.x == 0) out[0] = sqrt(sh[0]);
+}
+
+// boundary functional: partial sums of w_i p(q_face,i) |nrm_i| over the
+// faces b0 <= b < b1 (one thread per face node), then k_norm_final-style sum.
+template <int DIM, int NT>
+__global__ void k_functional_pressure(DevMesh md, const double* __restrict__ q, int b0, int b1,
+                                      double* __restrict__ part) {
+  constexpr int NV = DIM + 2;
+  __shared__ double sh[NT];
+  const int Nf = md.Nf, S = md.S, Np = md.Np;
+  const Gas g{md.gamma, md.gamma_1};
+  double acc = 0.0;
+  for (int t = blockIdx.x * NT + threadIdx.x; t < (b1 - b0) * Nf; t += gridDim.x * NT) {
+    const int b = b0 + t / Nf, i = t % Nf;
+    const int e = md.bfaces[2 * b], f = md.bfaces[2 * b + 1];
+    double qf[NV];
+#pragma unroll
+    for (int c = 0; c < NV; ++c) qf[c] = 0.0;
+    for (int s = 0; s < S; ++s) {
+      const double a = md.interp[((size_t)f * Nf + i) * S + s];
+      const double* x = q + ((size_t)e * Np + md.perm[f * S + s]) * NV;
+#pragma unroll
+      for (int c = 0; c < NV; ++c) qf[c] = fma(a, x[c], qf[c]);
+    }
+    const double* nr = md.nrm_bndry + ((size_t)b * Nf + i) * DIM;
+    double a2 = 0.0;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) a2 = fma(nr[k], nr[k], a2);
+    acc += md.wface[i] * eg::pressure<DIM>(g, qf) * sqrt(a2);
+  }
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = NT / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+template <int NT>
+__global__ void k_sum_final(const double* __restrict__ part, int n, double* __restrict__ out) {
+  __shared__ double sh[NT];
+  double s = 0.0;
+  for (int k = threadIdx.x; k < n; k += NT) s += part[k];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = NT / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[0] = sh[0];
 }
 
 }  // namespace
@@ -330,6 +381,36 @@ extern "C" int eg_calc_norm(eg_mesh* m, const double* r, int32_t strongres, int3
     rd = m->res_dev;
   }
   eg_launch_norm(m, rd, strongres, m->red + 2048);
+  EG_CUDA(cudaGetLastError());
+  EG_CUDA(cudaMemcpyAsync(m->h_red, m->red + 2048, sizeof(double), cudaMemcpyDeviceToHost, m->stream));
+  EG_CUDA(cudaStreamSynchronize(m->stream));
+  *out = m->h_red[0];
+  return EG_OK;
+}
+
+extern "C" int eg_calc_functional(eg_mesh* m, const double* q, int32_t bc_group, int32_t mem,
+                                  double* out) {
+  if (!m || !q || !out || bc_group < 0 || bc_group >= m->nbc) {
+    eg_set_error("eg_calc_functional: invalid argument (bc_group %d of %d)", bc_group, m ? m->nbc : 0);
+    return EG_ERR_INVALID;
+  }
+  const double* qd = q;
+  if (mem == EG_MEM_HOST) {
+    EG_CUDA(cudaMemcpyAsync(m->q_dev, q, sizeof(double) * (size_t)m->ndof, cudaMemcpyHostToDevice, m->stream));
+    qd = m->q_dev;
+  }
+  const int b0 = m->h_bndry_offsets[bc_group], b1 = m->h_bndry_offsets[bc_group + 1];
+  DevMesh md = dev_mesh(m);
+  int blocks = ((b1 - b0) * m->Nf + 255) / 256;
+  if (blocks < 1) blocks = 1;
+  if (blocks > 1024) blocks = 1024;
+  eg_phase_begin(m, EG_PHASE_OTHER);
+  if (m->dim == 2)
+    k_functional_pressure<2, 256><<<blocks, 256, 0, m->stream>>>(md, qd, b0, b1, m->red);
+  else
+    k_functional_pressure<3, 256><<<blocks, 256, 0, m->stream>>>(md, qd, b0, b1, m->red);
+  k_sum_final<256><<<1, 256, 0, m->stream>>>(m->red, blocks, m->red + 2048);
+  eg_phase_end(m, EG_PHASE_OTHER, 2);
   EG_CUDA(cudaGetLastError());
   EG_CUDA(cudaMemcpyAsync(m->h_red, m->red + 2048, sizeof(double), cudaMemcpyDeviceToHost, m->stream));
   EG_CUDA(cudaStreamSynchronize(m->stream));

@@ -1,0 +1,332 @@
+// eg_solvers.cu -- Newton steady solve and RK4 time stepping on the device.
+//
+// newton / newtonInner: reference src/NonlinearSolvers/newton.jl:54-304 with
+//   physicsRhs (src/jacobian/residual_evaluation.jl:64-84: residual + calcNorm
+//   with M^-1), doRecalculation every iteration (jac_recalc.jl:60-97),
+//   linearSolve to krylov_reltol (ls_standard.jl:321-371), q += dq,
+//   checkConvergence (newton.jl:402-455).
+// rk4: reference src/NonlinearSolvers/rk4.jl:144-336 with pde_pre_func /
+//   pde_post_func (rk4.jl:425-456): k_s = M^-1 R(q_s), classical stages.
+// The state, residual, norms and update stay FP64; with EG_F32 the Jacobian,
+// preconditioner and Krylov vectors are FP32 (inexact Newton against the FP64
+// residual).
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+
+#include "eg_internal.h"
+#include "eg_kernels.cuh"
+#include "eg_linalg.h"
+
+namespace {
+
+// y = a*x + b*y (FP64)
+__global__ void k_axpby64(double a, const double* __restrict__ x, double b, double* __restrict__ y,
+                          int64_t N) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = a * x[i] + b * y[i];
+}
+
+// RK4 stage: k_s = M^-1 res (in place into ks), q = x_old + c * k_s
+__global__ void k_rk4_stage(const double* __restrict__ res, const double* __restrict__ Minv,
+                            const double* __restrict__ xold, double c, double* __restrict__ ks,
+                            double* __restrict__ q, int64_t nnode, int nv) {
+  const int64_t N = nnode * nv;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+    const double k = Minv[i / nv] * res[i];
+    ks[i] = k;
+    q[i] = xold[i] + c * k;
+  }
+}
+
+// final RK4 update: x_old += h/6 (k1 + 2 k2 + 2 k3 + k4), q = x_old (k4 = M^-1 res)
+__global__ void k_rk4_final(const double* __restrict__ k1, const double* __restrict__ k2,
+                            const double* __restrict__ k3, const double* __restrict__ res,
+                            const double* __restrict__ Minv, double h, double* __restrict__ xold,
+                            double* __restrict__ q, int64_t nnode, int nv) {
+  const int64_t N = nnode * nv;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+    const double k4 = Minv[i / nv] * res[i];
+    const double x = xold[i] + (h / 6) * (k1[i] + 2 * k2[i] + 2 * k3[i] + k4);
+    xold[i] = x;
+    q[i] = x;
+  }
+}
+
+// pseudo-transient continuation: J(e,(j,a),(j,a)) -= M_j / tau_vec_j with
+// tau_vec = tau_l / (1 + sqrt(jac))  (reference globalization.jl:165-320)
+template <typename T>
+__global__ void k_ptc_shift(T* __restrict__ diag, const double* __restrict__ jac,
+                            const double* __restrict__ w, double tau_l, int E, int Np, int nv) {
+  const int n = Np * nv;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < (int64_t)E * n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int e = (int)(t / n), r = (int)(t - (int64_t)e * n);
+    const int j = r / nv;
+    const double jj = jac[(size_t)e * Np + j];
+    const double M = w[j] / jj;
+    const double tv = tau_l / (1.0 + sqrt(jj));
+    diag[(size_t)e * n * n + (size_t)r * n + r] -= T(M / tv);
+  }
+}
+
+int grid64(int64_t n) {
+  int64_t b = (n + 255) / 256;
+  return (int)(b > 152 * 16 ? 152 * 16 : (b < 1 ? 1 : b));
+}
+
+// residual + strong norm; synchronises and reports device status
+int residual_and_norm(eg_mesh* m, const double* q, double* res, double* norm) {
+  EG_CUDA(cudaMemsetAsync(m->status, 0, sizeof(unsigned int), m->stream));
+  int st = eg_launch_residual(m, q, res);
+  if (st != EG_OK) return st;
+  eg_launch_norm(m, res, 1, m->red + 2048);
+  EG_CUDA(cudaGetLastError());
+  EG_CUDA(cudaMemcpyAsync(m->h_red, m->red + 2048, sizeof(double), cudaMemcpyDeviceToHost, m->stream));
+  EG_CUDA(cudaMemcpyAsync(m->h_status, m->status, sizeof(unsigned int), cudaMemcpyDeviceToHost, m->stream));
+  EG_CUDA(cudaStreamSynchronize(m->stream));
+  st = eg_check_status(m);
+  if (st != EG_OK) return st;
+  *norm = m->h_red[0];
+  if (!std::isfinite(*norm)) {
+    eg_set_error("non-finite residual norm");
+    return EG_ERR_NONFINITE;
+  }
+  return EG_OK;
+}
+
+double ms_since(std::chrono::steady_clock::time_point t0) {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+}  // namespace
+
+// largest factor by which the pseudo-time step may grow in one iteration, and
+// the residual growth that makes a pseudo-time step be rejected (recovery
+// added here; the reference has neither)
+constexpr double PTC_MAX_GROWTH = 1.5;
+constexpr double PTC_MAX_INCREASE = 10.0;
+
+extern "C" int eg_newton_solve(eg_mesh* m, double* q, int32_t mem, const eg_newton_opts* o,
+                               eg_newton_stats* stats) {
+  if (!m || !q || !o) {
+    eg_set_error("eg_newton_solve: NULL argument");
+    return EG_ERR_INVALID;
+  }
+  const int64_t N = m->ndof;
+  double* qd = q;
+  double* res = nullptr;
+  double* dq = nullptr;
+  eg_lo* lo = nullptr;
+  eg_pc* pc = nullptr;
+  eg_ls* ls = nullptr;
+  eg_newton_stats s;
+  std::memset(&s, 0, sizeof(s));
+  int st = EG_OK;
+  auto cleanup = [&]() {
+    if (ls) eg_ls_destroy(ls);
+    if (pc) eg_pc_destroy(pc);
+    if (lo) eg_lo_destroy(lo);
+    if (res) cudaFree(res);
+    if (dq) cudaFree(dq);
+    if (qd != q && qd) cudaFree(qd);
+  };
+  cudaError_t ce = cudaMalloc((void**)&res, 8 * N);
+  if (ce == cudaSuccess) ce = cudaMalloc((void**)&dq, 8 * N);
+  if (ce == cudaSuccess && mem == EG_MEM_HOST) {
+    ce = cudaMalloc((void**)&qd, 8 * N);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(qd, q, 8 * N, cudaMemcpyHostToDevice, m->stream);
+  }
+  if (ce != cudaSuccess) {
+    if (mem == EG_MEM_HOST && ce != cudaSuccess) qd = (qd == q) ? q : qd;
+    cleanup();
+    return eg_cuda_fail(ce, "eg_newton_solve");
+  }
+  st = eg_lo_create(m, o->precision, &lo);
+  if (st == EG_OK) st = eg_pc_create(lo, &pc);
+  if (st == EG_OK) st = eg_ls_create(lo, pc, o->gmres_restart > 0 ? o->gmres_restart : 30, &ls);
+  if (st == EG_OK) st = eg_ls_set_tolerances(ls, o->krylov_reltol, 1e-30, -1, o->krylov_itermax > 0 ? o->krylov_itermax : 1000);
+  if (st != EG_OK) {
+    cleanup();
+    return st;
+  }
+  auto t0 = std::chrono::steady_clock::now();
+  double norm = 0;
+  st = residual_and_norm(m, qd, res, &norm);
+  s.t_residual += ms_since(t0);
+  if (st != EG_OK) {
+    cleanup();
+    return st;
+  }
+  s.res_norm0 = norm;
+  s.res_norm = norm;
+  const double norm_rel = norm;
+  bool conv = norm < o->res_abstol || (norm_rel > 0 && norm / norm_rel < o->res_reltol && false);
+  const int g = grid64(N);
+  double* qsave = nullptr;
+  if (o->globalize_euler) {
+    ce = cudaMalloc((void**)&qsave, 8 * N);
+    if (ce != cudaSuccess) {
+      cleanup();
+      return eg_cuda_fail(ce, "eg_newton_solve");
+    }
+  }
+  double tau_l = o->euler_tau, norm_prev = 0.0;
+  // per-iteration trace on stderr (the reference's newton_verbosity output)
+  const bool verbose = std::getenv("EG_NEWTON_VERBOSE") != nullptr;
+  for (int it = 1; !conv && it <= o->itermax; ++it) {
+    // Jacobian (+ pseudo-time diagonal) and preconditioner at the current state
+    t0 = std::chrono::steady_clock::now();
+    st = eg_lo_calc(lo, qd, EG_MEM_DEVICE);
+    if (st == EG_OK && o->globalize_euler) {
+      if (norm_prev != 0.0) tau_l *= fmin(norm_prev / norm, PTC_MAX_GROWTH);
+      norm_prev = norm;
+      const int blocks = grid64((int64_t)m->E * lo->n);
+      if (lo->prec == EG_F64)
+        k_ptc_shift<double><<<blocks, 256, 0, m->stream>>>((double*)lo->diag, m->jac, m->w, tau_l, m->E, m->Np, m->nv);
+      else
+        k_ptc_shift<float><<<blocks, 256, 0, m->stream>>>((float*)lo->diag, m->jac, m->w, tau_l, m->E, m->Np, m->nv);
+      m->launches += 1;
+    }
+    if (st == EG_OK) EG_CUDA(cudaStreamSynchronize(m->stream));
+    s.t_jacobian += ms_since(t0);
+    if (st != EG_OK) break;
+    t0 = std::chrono::steady_clock::now();
+    st = eg_pc_calc(pc);
+    if (st == EG_OK) {
+      EG_CUDA(cudaMemcpyAsync(m->h_status, m->status, sizeof(unsigned int), cudaMemcpyDeviceToHost, m->stream));
+      EG_CUDA(cudaStreamSynchronize(m->stream));
+      st = eg_check_status(m);
+    }
+    s.t_pc += ms_since(t0);
+    if (st != EG_OK) break;
+    // J dq = -R, dq0 = 0
+    t0 = std::chrono::steady_clock::now();
+    EG_CUDA(cudaMemsetAsync(dq, 0, 8 * N, m->stream));
+    eg_convert(m, res, ls->bT, lo->prec, N, -1.0);
+    eg_convert(m, dq, ls->xT, lo->prec, N, 1.0);
+    eg_ls_stats ks;
+    st = eg_gmres_T(ls, ls->bT, ls->xT, &ks);
+    if (st != EG_OK) break;
+    eg_convert_back(m, ls->xT, dq, lo->prec, N);
+    s.krylov_iters += ks.iters;
+    // step norm ||dq||_2 (reference newton.jl:238: norm(delta_q_vec))
+    eg_launch_norm(m, dq, 2, m->red + 2049);
+    if (qsave) EG_CUDA(cudaMemcpyAsync(qsave, qd, 8 * N, cudaMemcpyDeviceToDevice, m->stream));
+    k_axpby64<<<g, 256, 0, m->stream>>>(1.0, dq, 1.0, qd, N);
+    m->launches += 1;
+    EG_CUDA(cudaMemcpyAsync(m->h_red + 1, m->red + 2049, sizeof(double), cudaMemcpyDeviceToHost, m->stream));
+    EG_CUDA(cudaStreamSynchronize(m->stream));
+    s.step_norm = m->h_red[1];
+    s.t_krylov += ms_since(t0);
+    // residual at the new state
+    t0 = std::chrono::steady_clock::now();
+    double nn = 0.0;
+    st = residual_and_norm(m, qd, res, &nn);
+    s.t_residual += ms_since(t0);
+    s.iters = it;
+    if (verbose)
+      std::fprintf(stderr, "eg_newton %3d |R| %.3e -> %.3e tau %.3e krylov %d st %d\n", it, norm, nn,
+                   tau_l, ks.iters, st);
+    const bool bad = st == EG_ERR_NEG_DENSITY || st == EG_ERR_NEG_PRESSURE || st == EG_ERR_NONFINITE ||
+                     (st == EG_OK && nn > PTC_MAX_INCREASE * norm);
+    if (bad && o->globalize_euler) {
+      // reject the pseudo-time step: restore q, shrink tau
+      EG_CUDA(cudaMemcpyAsync(qd, qsave, 8 * N, cudaMemcpyDeviceToDevice, m->stream));
+      st = residual_and_norm(m, qd, res, &nn);
+      if (st != EG_OK) break;
+      tau_l *= 0.25;
+      norm_prev = 0.0;
+      continue;
+    }
+    if (st != EG_OK) break;
+    norm = nn;
+    s.res_norm = norm;
+    conv = norm < o->res_abstol || (norm / norm_rel < o->res_reltol) ||
+           (s.step_norm <= o->step_tol);
+  }
+  if (qsave) cudaFree(qsave);
+  s.converged = conv ? 1 : 0;
+  if (st == EG_OK && mem == EG_MEM_HOST) {
+    ce = cudaMemcpyAsync(q, qd, 8 * N, cudaMemcpyDeviceToHost, m->stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(m->stream);
+    if (ce != cudaSuccess) st = eg_cuda_fail(ce, "eg_newton_solve copy-out");
+  }
+  if (stats) *stats = s;
+  cleanup();
+  if (st == EG_OK && !conv) {
+    eg_set_error("Newton did not converge in %d iterations (|R| = %g)", o->itermax, s.res_norm);
+    return EG_ERR_NOT_CONVERGED;
+  }
+  return st;
+}
+
+extern "C" int eg_rk4(eg_mesh* m, double* q, double h, double t_max, int32_t itermax, double res_tol,
+                      int32_t mem, eg_rk4_stats* stats) {
+  if (!m || !q || !(h > 0)) {
+    eg_set_error("eg_rk4: invalid argument");
+    return EG_ERR_INVALID;
+  }
+  const int64_t N = m->ndof, nnode = (int64_t)m->E * m->Np;
+  double* buf = nullptr;
+  cudaError_t ce = cudaMalloc((void**)&buf, 8 * N * (mem == EG_MEM_HOST ? 6 : 5));
+  if (ce != cudaSuccess) return eg_cuda_fail(ce, "eg_rk4");
+  double* xold = buf;
+  double* k1 = buf + N;
+  double* k2 = buf + 2 * N;
+  double* k3 = buf + 3 * N;
+  double* res = buf + 4 * N;
+  double* qd = mem == EG_MEM_HOST ? buf + 5 * N : q;
+  if (mem == EG_MEM_HOST) cudaMemcpyAsync(qd, q, 8 * N, cudaMemcpyHostToDevice, m->stream);
+  cudaMemcpyAsync(xold, qd, 8 * N, cudaMemcpyDeviceToDevice, m->stream);
+  const int g = grid64(N);
+  const long t_steps = lround(t_max / h);
+  double t = 0.0, last_norm = 0.0;
+  int steps = 0, st = EG_OK;
+  cudaMemsetAsync(m->status, 0, sizeof(unsigned int), m->stream);
+  // loop i = 2 .. t_steps+1 of the reference (rk4.jl:201)
+  for (long i = 2; i <= t_steps + 1; ++i) {
+    t = (i - 2) * h;
+    // stage 1 (with the norm, as pde_post_func with calc_norm=true)
+    st = eg_launch_residual(m, qd, res);
+    if (st != EG_OK) break;
+    k_rk4_stage<<<g, 256, 0, m->stream>>>(res, m->Minv, xold, h / 2, k1, qd, nnode, m->nv);
+    m->launches += 1;
+    if (res_tol > 0) {
+      // norm of k1 = M^-1 R weighted by M: sqrt(sum k1^2 M)
+      eg_launch_norm(m, k1, 0, m->red + 2048);
+      cudaMemcpyAsync(m->h_red, m->red + 2048, sizeof(double), cudaMemcpyDeviceToHost, m->stream);
+      cudaStreamSynchronize(m->stream);
+      last_norm = m->h_red[0];
+      // the reference breaks after the stage-1 update of q (rk4.jl:258-280)
+      if (last_norm < res_tol) break;
+    }
+    if (itermax > 0 && i > itermax) break;
+    // stages 2, 3, 4
+    eg_launch_residual(m, qd, res);
+    k_rk4_stage<<<g, 256, 0, m->stream>>>(res, m->Minv, xold, h / 2, k2, qd, nnode, m->nv);
+    eg_launch_residual(m, qd, res);
+    k_rk4_stage<<<g, 256, 0, m->stream>>>(res, m->Minv, xold, h, k3, qd, nnode, m->nv);
+    eg_launch_residual(m, qd, res);
+    k_rk4_final<<<g, 256, 0, m->stream>>>(k1, k2, k3, res, m->Minv, h, xold, qd, nnode, m->nv);
+    m->launches += 3;
+    ++steps;
+  }
+  t += h;
+  if (st == EG_OK) {
+    cudaMemcpyAsync(m->h_status, m->status, sizeof(unsigned int), cudaMemcpyDeviceToHost, m->stream);
+    if (mem == EG_MEM_HOST) cudaMemcpyAsync(q, qd, 8 * N, cudaMemcpyDeviceToHost, m->stream);
+    ce = cudaStreamSynchronize(m->stream);
+    if (ce != cudaSuccess) st = eg_cuda_fail(ce, "eg_rk4");
+    else st = eg_check_status(m);
+  }
+  cudaFree(buf);
+  if (stats) {
+    stats->steps = steps;
+    stats->t = t;
+    stats->res_norm = last_norm;
+  }
+  return st;
+}

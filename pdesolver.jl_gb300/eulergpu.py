@@ -60,6 +60,59 @@ def _declare(lib):
     lib.eg_set_timing.argtypes = [vp, C.c_int32]
     lib.eg_get_timings.argtypes = [vp, C.POINTER(Timings)]
     lib.eg_reset_timings.argtypes = [vp]
+    lib.eg_calc_functional.argtypes = [vp, vp, C.c_int32, C.c_int32, dp]
+    lib.eg_lo_create.argtypes = [vp, C.c_int32, C.POINTER(vp)]
+    lib.eg_lo_destroy.argtypes = [vp]
+    lib.eg_lo_calc.argtypes = [vp, vp, C.c_int32]
+    lib.eg_lo_apply.argtypes = [vp, vp, vp, C.c_int32]
+    lib.eg_lo_get_blocks.argtypes = [vp, vp, vp]
+    lib.eg_pc_create.argtypes = [vp, C.POINTER(vp)]
+    lib.eg_pc_destroy.argtypes = [vp]
+    lib.eg_pc_calc.argtypes = [vp]
+    lib.eg_pc_apply.argtypes = [vp, vp, vp, C.c_int32]
+    lib.eg_ls_create.argtypes = [vp, vp, C.c_int32, C.POINTER(vp)]
+    lib.eg_ls_destroy.argtypes = [vp]
+    lib.eg_ls_set_tolerances.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_int32]
+    lib.eg_ls_solve.argtypes = [vp, vp, vp, C.c_int32, C.POINTER(LsStats)]
+    lib.eg_newton_solve.argtypes = [vp, vp, C.c_int32, C.POINTER(NewtonOpts), C.POINTER(NewtonStats)]
+    lib.eg_rk4.argtypes = [vp, vp, C.c_double, C.c_double, C.c_int32, C.c_double, C.c_int32,
+                           C.POINTER(Rk4Stats)]
+
+
+class LsStats(C.Structure):
+    _fields_ = [("iters", C.c_int32), ("restarts", C.c_int32), ("converged", C.c_int32),
+                ("reserved", C.c_int32), ("res0", C.c_double), ("res_final", C.c_double)]
+
+
+class NewtonOpts(C.Structure):
+    _fields_ = [("res_abstol", C.c_double), ("res_reltol", C.c_double), ("step_tol", C.c_double),
+                ("krylov_reltol", C.c_double), ("itermax", C.c_int32),
+                ("krylov_itermax", C.c_int32), ("gmres_restart", C.c_int32), ("precision", C.c_int32),
+                ("globalize_euler", C.c_int32), ("euler_tau", C.c_double)]
+
+    @classmethod
+    def from_opts(cls, opts=None, precision=0):
+        """Reference option keys (read_input.jl:414-496) with their defaults."""
+        o = dict(opts or {})
+        return cls(o.get("res_abstol", 1e-6), o.get("res_reltol", 1e-6), o.get("step_tol", 0.0),
+                   o.get("krylov_reltol", 1e-2), o.get("itermax", 50),
+                   o.get("krylov_itermax", 1000), o.get("gmres_restart", 30), precision,
+                   int(o.get("newton_globalize_euler", False)), o.get("euler_tau", 1.0))
+
+
+class NewtonStats(C.Structure):
+    _fields_ = [("iters", C.c_int32), ("krylov_iters", C.c_int32), ("converged", C.c_int32),
+                ("reserved", C.c_int32), ("res_norm0", C.c_double), ("res_norm", C.c_double),
+                ("step_norm", C.c_double), ("t_residual", C.c_double), ("t_jacobian", C.c_double),
+                ("t_pc", C.c_double), ("t_krylov", C.c_double)]
+
+    def asdict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
+class Rk4Stats(C.Structure):
+    _fields_ = [("steps", C.c_int32), ("reserved", C.c_int32), ("t", C.c_double),
+                ("res_norm", C.c_double)]
 
 
 class Timings(C.Structure):
@@ -162,6 +215,31 @@ class GPUMesh:
     def reset_timings(self):
         check(self.lib.eg_reset_timings(self.handle))
 
+    def functional_pressure(self, q, bc_group=0):
+        """integral of p over the faces of a boundary-condition group."""
+        pq, mq = self._ptr(q)
+        out = C.c_double()
+        check(self.lib.eg_calc_functional(self.handle, pq, bc_group, mq, C.byref(out)))
+        return out.value
+
+    def newton(self, q, opts=None, precision=0):
+        """steady Newton solve in place (reference newton.jl:54); returns stats.
+        Raises EulerGPUError(EG_ERR_NOT_CONVERGED) if the tolerances are not met."""
+        pq, mq = self._ptr(q)
+        o = NewtonOpts.from_opts(opts, precision)
+        st = NewtonStats()
+        rc = self.lib.eg_newton_solve(self.handle, pq, mq, C.byref(o), C.byref(st))
+        self.last_newton = st
+        check(rc)
+        return st
+
+    def rk4(self, q, h, t_max, itermax=0, res_tol=-1.0):
+        """classical RK4 in place (reference rk4.jl:404); returns stats."""
+        pq, mq = self._ptr(q)
+        st = Rk4Stats()
+        check(self.lib.eg_rk4(self.handle, pq, h, t_max, itermax, res_tol, mq, C.byref(st)))
+        return st
+
     def calc_norm(self, r, strongres=True):
         pr, mr = self._ptr(r)
         out = C.c_double()
@@ -202,3 +280,111 @@ def calcNorm(eqn, res_vec, strongres=False):
     """SBP norm of a residual vector (reference Utils.jl:427)."""
     r = np.ascontiguousarray(np.asarray(res_vec, dtype=np.float64).reshape(eqn.q.shape))
     return eqn.gpu.calc_norm(r, strongres)
+
+
+class LinearOperator:
+    """Explicit Jacobian (reference AbstractLO: calcLinearOperator /
+    applyLinearOperator), element-block sparse on the device."""
+
+    def __init__(self, gmesh: GPUMesh, precision=0):
+        self.g = gmesh
+        self.lib = gmesh.lib
+        self.precision = precision
+        h = C.c_void_p()
+        check(self.lib.eg_lo_create(gmesh.handle, precision, C.byref(h)))
+        self.handle = h
+        op = gmesh.mesh.sbp
+        self.n = op.numnodes * gmesh.mesh.numDofPerNode
+        self.nb = op.stencilsize * gmesh.mesh.numDofPerNode
+
+    def calc(self, q):
+        pq, mq = GPUMesh._ptr(q)
+        check(self.lib.eg_lo_calc(self.handle, pq, mq))
+
+    def apply(self, x, y):
+        px, mx = GPUMesh._ptr(x)
+        py, _ = GPUMesh._ptr(y)
+        check(self.lib.eg_lo_apply(self.handle, px, py, mx))
+        return y
+
+    def blocks(self):
+        ms = self.g.mesh
+        diag = np.zeros((ms.numEl, self.n, self.n))
+        cpl = np.zeros((max(ms.numInterfaces, 1), 2, self.nb, self.nb))
+        check(self.lib.eg_lo_get_blocks(self.handle, C.c_void_p(diag.ctypes.data),
+                                        C.c_void_p(cpl.ctypes.data)))
+        return diag, cpl[:ms.numInterfaces]
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.eg_lo_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class BlockJacobiPC:
+    """Element block-Jacobi preconditioner (reference NewtonBDiagPC)."""
+
+    def __init__(self, lo: LinearOperator):
+        self.lo = lo
+        self.lib = lo.lib
+        h = C.c_void_p()
+        check(self.lib.eg_pc_create(lo.handle, C.byref(h)))
+        self.handle = h
+
+    def calc(self):
+        check(self.lib.eg_pc_calc(self.handle))
+
+    def apply(self, x, y):
+        px, mx = GPUMesh._ptr(x)
+        py, _ = GPUMesh._ptr(y)
+        check(self.lib.eg_pc_apply(self.handle, px, py, mx))
+        return y
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.eg_pc_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class LinearSolver:
+    """GMRES(restart) with right block-Jacobi preconditioning (reference
+    StandardLinearSolver: linearSolve / setTolerances)."""
+
+    def __init__(self, pc: BlockJacobiPC, lo: LinearOperator, restart=30):
+        self.pc, self.lo, self.lib = pc, lo, lo.lib
+        h = C.c_void_p()
+        check(self.lib.eg_ls_create(lo.handle, pc.handle, restart, C.byref(h)))
+        self.handle = h
+
+    def set_tolerances(self, reltol=-1.0, abstol=-1.0, dtol=-1.0, itermax=-1):
+        check(self.lib.eg_ls_set_tolerances(self.handle, reltol, abstol, dtol, itermax))
+
+    def solve(self, b, x):
+        pb, mb = GPUMesh._ptr(b)
+        px, _ = GPUMesh._ptr(x)
+        st = LsStats()
+        check(self.lib.eg_ls_solve(self.handle, pb, px, mb, C.byref(st)))
+        return st
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.eg_ls_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

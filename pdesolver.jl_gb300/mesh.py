@@ -156,12 +156,14 @@ def _connect(elverts, faces_local, sbp, face_pts_all, tags_of_faces, bc_of_tag):
     nbrperm = uperm.astype(np.int32) if len(uperm) else np.arange(Nf, dtype=np.int32)[None]
     be, bf = bids // F, bids % F
     tags = np.asarray(tags_of_faces(be, bf), dtype=np.int32)
-    bc = np.array([bc_of_tag(t) for t in tags], dtype=np.int32)
-    o = np.lexsort((np.arange(len(bids)), tags, bc))
+    # one boundary-condition group per geometric boundary (reference BC1..BCn
+    # with bndry_offsets), ordered by tag, faces in element order within it
+    o = np.lexsort((np.arange(len(bids)), tags))
     bfaces = np.stack([be, bf], axis=1).astype(np.int32)[o]
-    tags, bc = tags[o], bc[o]
-    bc_types = np.unique(bc).astype(np.int32)
-    offsets = np.searchsorted(bc, bc_types).tolist() + [len(bc)]
+    tags = tags[o]
+    gtags = np.unique(tags)
+    bc_types = np.array([bc_of_tag(int(t)) for t in gtags], dtype=np.int32)
+    offsets = np.searchsorted(tags, gtags).tolist() + [len(tags)]
     return iface, nbrperm, bfaces, np.array(offsets, dtype=np.int32), bc_types, tags
 
 

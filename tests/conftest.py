@@ -32,6 +32,7 @@ def oracle():
     lib.oracle_calc_norm.restype = C.c_double
     lib.oracle_logavg.restype = C.c_double
     lib.oracle_logavg.argtypes = [C.c_double, C.c_double]
+    lib.oracle_functional_pressure.restype = C.c_double
     return lib
 
 
@@ -50,3 +51,43 @@ def oracle_residual(oracle, desc, params, q):
     st = oracle.oracle_eval_residual(C.byref(desc.desc), C.byref(params), abi.dptr(q), abi.dptr(res))
     assert st == 0, st
     return res
+
+
+def oracle_jacobian(oracle, desc, params, ms, q):
+    """element blocks [E][n][n] and coupling blocks [I][2][nb][nb] (FP64)."""
+    from pdesolver_gb300 import abi
+    nv = ms.numDofPerNode
+    n = ms.sbp.numnodes * nv
+    nb = ms.sbp.stencilsize * nv
+    diag = np.zeros((ms.numEl, n, n))
+    cpl = np.zeros((max(ms.numInterfaces, 1), 2, nb, nb))
+    st = oracle.oracle_eval_jacobian(C.byref(desc.desc), C.byref(params), abi.dptr(q),
+                                     abi.dptr(diag), abi.dptr(cpl))
+    assert st == 0, st
+    return diag, cpl[:ms.numInterfaces]
+
+
+def oracle_jvp(oracle, desc, params, q, v):
+    from pdesolver_gb300 import abi
+    res = np.zeros_like(q)
+    jv = np.zeros_like(q)
+    st = oracle.oracle_residual_jvp(C.byref(desc.desc), C.byref(params), abi.dptr(q),
+                                    abi.dptr(np.ascontiguousarray(v)), abi.dptr(res), abi.dptr(jv))
+    assert st == 0, st
+    return jv
+
+
+def block_apply(ms, diag, cpl, x):
+    """y = J x for the element-block storage (host, numpy)."""
+    E, n = diag.shape[0], diag.shape[1]
+    op = ms.sbp
+    nv = ms.numDofPerNode
+    xe = x.reshape(E, n)
+    # diag[e][c][r]: column-major -> y_r = sum_c D[c][r] x_c
+    y = np.einsum("ecr,ec->er", diag, xe)
+    for k, (eL, eR, fL, fR, o) in enumerate(ms.interfaces):
+        iL = (op.perm[fL][:, None] * nv + np.arange(nv)[None]).ravel()
+        iR = (op.perm[fR][:, None] * nv + np.arange(nv)[None]).ravel()
+        y[eL, iL] += cpl[k, 0].T @ xe[eR, iR]
+        y[eR, iR] += cpl[k, 1].T @ xe[eL, iL]
+    return y.reshape(x.shape)

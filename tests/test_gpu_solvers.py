@@ -1,0 +1,149 @@
+"""GPU Jacobian, block-Jacobi preconditioner, GMRES, Newton, RK4 and the
+boundary functional against the CPU oracle (through the C ABI).
+
+Tolerances: Jacobian (FP64) 1e-10 relative to the largest entry; block
+inverse 1e-12; Newton (FP64) converged state and functional 1e-10, mixed
+(FP32 Jacobian/PC/Krylov) functional 1e-8; RK4 1e-11.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import block_apply, oracle_jacobian, oracle_jvp
+from pdesolver_gb300 import abi, eulergpu, problems
+
+pytestmark = pytest.mark.gpu
+
+
+def setup(fam="gamma", p=3, n=4, flux="RoeFlux", seed=51):
+    ms, opts, q = problems.config1(n=n, p=p, family=fam, seed=seed)
+    opts = dict(opts, Flux_name=flux)
+    g = eulergpu.GPUMesh(ms, opts)
+    return ms, opts, q, g
+
+
+@pytest.mark.parametrize("fam,p,flux", [("omega", 2, "RoeFlux"), ("gamma", 3, "RoeFlux"),
+                                        ("gamma", 2, "IRFlux"), ("gamma", 4, "RoeFlux")])
+def test_jacobian_blocks_fp64(gpu_lib, oracle, fam, p, flux):
+    ms, opts, q, g = setup(fam, p, flux=flux)
+    lo = eulergpu.LinearOperator(g, precision=0)
+    lo.calc(q)
+    d, c = lo.blocks()
+    rd, rc = oracle_jacobian(oracle, g.desc, g.params, ms, q)
+    scale = max(np.abs(rd).max(), np.abs(rc).max())
+    assert np.abs(d - rd).max() <= 1e-10 * scale
+    assert np.abs(c - rc).max() <= 1e-10 * scale
+
+
+def test_jacobian_fp32_and_apply(gpu_lib, oracle):
+    ms, opts, q, g = setup()
+    rd, rc = oracle_jacobian(oracle, g.desc, g.params, ms, q)
+    scale = max(np.abs(rd).max(), np.abs(rc).max())
+    lo32 = eulergpu.LinearOperator(g, precision=1)
+    lo32.calc(q)
+    d, c = lo32.blocks()
+    assert np.abs(d - rd).max() <= 1e-5 * scale
+    # FP64 operator apply == dual-number directional derivative of the residual
+    lo = eulergpu.LinearOperator(g, precision=0)
+    lo.calc(q)
+    rng = np.random.default_rng(9)
+    for _ in range(3):
+        v = rng.normal(size=q.shape)
+        y = lo.apply(np.ascontiguousarray(v), np.zeros_like(v))
+        jv = oracle_jvp(oracle, g.desc, g.params, q, v)
+        assert np.abs(y - jv).max() <= 1e-10 * np.abs(jv).max()
+        y32 = lo32.apply(np.ascontiguousarray(v), np.zeros_like(v))
+        assert np.abs(y32 - jv).max() <= 1e-5 * np.abs(jv).max()
+
+
+def test_block_jacobi_inverse(gpu_lib, oracle):
+    """test/euler/test_jac.jl:3073-3140: the element block-Jacobi
+    preconditioner inverts the element blocks (1e-12)."""
+    ms, opts, q, g = setup()
+    lo = eulergpu.LinearOperator(g, precision=0)
+    lo.calc(q)
+    pc = eulergpu.BlockJacobiPC(lo)
+    pc.calc()
+    d, _ = lo.blocks()
+    x = np.random.default_rng(3).normal(size=q.shape)
+    b = np.einsum("ecr,ec->er", d, x.reshape(d.shape[0], -1)).reshape(q.shape)
+    y = pc.apply(np.ascontiguousarray(b), np.zeros_like(b))
+    assert np.abs(y - x).max() <= 1e-12 * np.abs(x).max() * 10
+
+
+@pytest.mark.parametrize("precision,tol", [(0, 1e-8), (1, 1e-4)])
+def test_gmres_solves(gpu_lib, precision, tol):
+    ms, opts, q, g = setup(n=6)
+    lo = eulergpu.LinearOperator(g, precision=precision)
+    lo.calc(q)
+    pc = eulergpu.BlockJacobiPC(lo)
+    pc.calc()
+    ls = eulergpu.LinearSolver(pc, lo, restart=30)
+    ls.set_tolerances(reltol=tol, abstol=0.0, itermax=3000)
+    b = np.random.default_rng(7).normal(size=q.shape)
+    x = np.zeros_like(b)
+    st = ls.solve(b, x)
+    assert st.converged == 1
+    lo64 = eulergpu.LinearOperator(g, precision=0)
+    lo64.calc(q)
+    r = b - lo64.apply(x, np.zeros_like(x))
+    assert np.linalg.norm(r) <= 3 * tol * np.linalg.norm(b)
+
+
+NEWTON_OPTS = {"res_abstol": 1e-10, "res_reltol": 1e-14, "itermax": 150,
+               "newton_globalize_euler": True, "euler_tau": 0.5, "krylov_reltol": 1e-2}
+
+
+def _oracle_newton(oracle, g, q):
+    o = eulergpu.NewtonOpts.from_opts(NEWTON_OPTS, 0)
+    st = eulergpu.NewtonStats()
+    rc = oracle.oracle_newton(C.byref(g.desc.desc), C.byref(g.params), abi.dptr(q), C.byref(o),
+                              C.byref(st))
+    assert rc == 0, (rc, st.asdict())
+    return st
+
+
+def test_newton_fp64_and_mixed_match_oracle(gpu_lib, oracle):
+    """Newton-GMRES with pseudo-transient continuation from the perturbed free
+    stream to |R| < 1e-10 (8x8 annulus, SBP-Gamma p=3).  FP64: state and
+    integral of p along r = 1 agree with the oracle's Newton to 1e-10;
+    mixed (FP32 Jacobian, PC, Krylov): functional within 1e-8."""
+    ms, opts, q0 = problems.config2(n=8)
+    g = eulergpu.GPUMesh(ms, opts)
+    qo = q0.copy()
+    _oracle_newton(oracle, g, qo)
+    fo = oracle.oracle_functional_pressure(C.byref(g.desc.desc), C.byref(g.params), abi.dptr(qo), 0)
+    q64 = q0.copy()
+    st = g.newton(q64, NEWTON_OPTS, precision=0)
+    assert st.converged == 1 and st.res_norm < 1e-10
+    assert np.abs(q64 - qo).max() <= 1e-9 * np.abs(qo).max()
+    f64 = g.functional_pressure(q64, 0)
+    assert abs(f64 - fo) <= 1e-10 * abs(fo)
+    q32 = q0.copy()
+    st = g.newton(q32, NEWTON_OPTS, precision=1)
+    assert st.converged == 1 and st.res_norm < 1e-10
+    f32 = g.functional_pressure(q32, 0)
+    assert abs(f32 - fo) <= 1e-8 * abs(fo)
+
+
+def test_rk4_matches_oracle(gpu_lib, oracle):
+    ms, opts, q0 = problems.config1()
+    g = eulergpu.GPUMesh(ms, opts)
+    h = 1e-3
+    qg = q0.copy()
+    g.rk4(qg, h, 10 * h)
+    qo = q0.copy()
+    st = eulergpu.Rk4Stats()
+    assert oracle.oracle_rk4(C.byref(g.desc.desc), C.byref(g.params), abi.dptr(qo), C.c_double(h),
+                             C.c_double(10 * h), 0, C.c_double(-1.0), C.byref(st)) == 0
+    assert st.steps == 10
+    assert np.abs(qg - qo).max() <= 1e-11 * np.abs(qo).max()
+
+
+def test_functional_matches_oracle(gpu_lib, oracle):
+    ms, opts, q = problems.config1()
+    g = eulergpu.GPUMesh(ms, opts)
+    for grp in range(len(ms.bc_types)):
+        fo = oracle.oracle_functional_pressure(C.byref(g.desc.desc), C.byref(g.params), abi.dptr(q), grp)
+        assert abs(g.functional_pressure(q, grp) - fo) <= 1e-13 * abs(fo)

@@ -234,3 +234,65 @@ def test_calc_norm(oracle):
                         math.sqrt(np.sum(r * r * M)), rel_tol=1e-13)
     assert math.isclose(oracle.oracle_calc_norm(C.byref(desc.desc), abi.dptr(r), 1),
                         math.sqrt(np.sum(r * r / M)), rel_tol=1e-13)
+
+
+@pytest.mark.parametrize("fam,p,flux", [("omega", 2, "RoeFlux"), ("gamma", 3, "RoeFlux"),
+                                        ("gamma", 2, "IRFlux")])
+def test_explicit_jacobian_vs_dual_jvp(oracle, fam, p, flux):
+    """test/euler/test_jac.jl:2370-2465: the explicitly assembled Jacobian
+    times random vectors equals the directional derivative of the residual
+    (here by forward-mode dual numbers instead of complex step) at 1e-11."""
+    from conftest import block_apply, oracle_jacobian, oracle_jvp
+    ms, opts, q = problems.config1(n=3, p=p, family=fam, seed=31)
+    opts = dict(opts, Flux_name=flux)
+    desc = abi.MeshDesc(ms)
+    P = eulergpu_params(opts)
+    diag, cpl = oracle_jacobian(oracle, desc, P, ms, q)
+    rng = np.random.default_rng(4)
+    for _ in range(3):
+        v = rng.normal(size=q.shape)
+        b1 = block_apply(ms, diag, cpl, v)
+        b2 = oracle_jvp(oracle, desc, P, q, v)
+        assert np.abs(b1 - b2).max() < 1e-11 * max(1.0, np.abs(b2).max())
+
+
+def eulergpu_params(opts):
+    from pdesolver_gb300 import eulergpu
+    return eulergpu.params_from_opts(opts)
+
+
+def test_oracle_rk4_fourth_order(oracle):
+    """rk4.jl: classical RK4 (the reference's test_rk4.jl integrates a quartic
+    exactly); here: the error of the Euler vortex RK4 solution at a fixed time
+    falls by ~2^4 when the step is halved."""
+    from pdesolver_gb300 import eulergpu
+    ms, opts, q0 = problems.config1(n=3, p=1, seed=41)
+    desc = abi.MeshDesc(ms)
+    P = eulergpu.params_from_opts(opts)
+    T = 0.02
+
+    def run(h):
+        q = q0.copy()
+        st = eulergpu.Rk4Stats()
+        assert oracle.oracle_rk4(C.byref(desc.desc), C.byref(P), abi.dptr(q), C.c_double(h),
+                                 C.c_double(T), 0, C.c_double(-1.0), C.byref(st)) == 0
+        return q
+
+    ref = run(T / 64)
+    e1 = np.abs(run(T / 4) - ref).max()
+    e2 = np.abs(run(T / 8) - ref).max()
+    assert 12.0 < e1 / e2 < 20.0, (e1, e2)
+
+
+def test_oracle_newton_converges_small(oracle):
+    """newton.jl with pseudo-transient continuation reaches |R| < 1e-10 from the
+    perturbed free stream on a small annulus (Gamma p=2)."""
+    from pdesolver_gb300 import eulergpu
+    ms, opts, q = problems.config2(n=4, p=2)
+    desc = abi.MeshDesc(ms)
+    P = eulergpu.params_from_opts(opts)
+    o = eulergpu.NewtonOpts.from_opts({"res_abstol": 1e-10, "res_reltol": 1e-14, "itermax": 100,
+                                       "newton_globalize_euler": True, "euler_tau": 0.5})
+    st = eulergpu.NewtonStats()
+    rc = oracle.oracle_newton(C.byref(desc.desc), C.byref(P), abi.dptr(q), C.byref(o), C.byref(st))
+    assert rc == 0 and st.converged == 1 and st.res_norm < 1e-10
