@@ -291,6 +291,15 @@ typedef struct {
 int eg_newton_solve(eg_mesh* mesh, double* q, int32_t mem, const eg_newton_opts* opts,
                     eg_newton_stats* stats);
 
+/*
+ * Degree prolongation between two eg_mesh objects on the same elements
+ * (p-continuation, the reference's p_homotopy idea): q_hi[e] = T q_lo[e] for
+ * every element, T[Np_hi*nv][Np_lo*nv] row-major (host pointer, copied);
+ * q_lo, q_hi in host or device memory per `mem`.
+ */
+int eg_prolong(eg_mesh* lo, const double* q_lo, eg_mesh* hi, double* q_hi, const double* T,
+               int32_t mem);
+
 typedef struct {
   int32_t steps;            /* time steps taken                             */
   int32_t reserved;

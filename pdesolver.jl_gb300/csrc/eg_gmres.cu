@@ -1,0 +1,388 @@
+// eg_gmres.cu -- right-preconditioned restarted GMRES driven from the device.
+//
+// Reference: linearSolve -> PETSc KSPSolve with GMRES(30), right
+// preconditioning (src/linearsolvers/ls_standard.jl:321-371,
+// src/input/read_input.jl:559-569).  The algorithm is Saad's GMRES(m) with
+// classical Gram-Schmidt applied twice (CGS2; as stable as the reference's
+// modified Gram-Schmidt, but each pass is one batched multi-dot kernel).
+//
+// GB300 design: the Hessenberg column, Givens rotations, convergence test and
+// the small triangular solve all run on the device (FP64, one thread), so a
+// restart cycle needs no host round trip.  A device flag `done` makes every
+// remaining kernel of the cycle return immediately once the residual estimate
+// meets the tolerance.  One cycle (m iterations, the update x += M^-1 V y,
+// the true residual b - A x and the re-initialisation) is captured once as a
+// CUDA graph and replayed; the host reads 2 ints and 2 doubles per cycle.
+#include <cmath>
+#include <cstring>
+
+#include "eg_internal.h"
+#include "eg_kernels.cuh"
+#include "eg_linalg.h"
+
+namespace {
+
+enum { F_DONE = 0, F_JDONE = 1, F_ITS = 2, F_CONV = 3, F_ITERMAX = 4 };
+enum { S_TOL = 0, S_RESID = 1, S_BETA = 2, S_BNORM = 3, S_RELTOL = 4, S_ABSTOL = 5 };
+
+// per-block partial sums of V[k] . w for k < cnt (skips when *done)
+template <typename T, int NT>
+__global__ void k_gm_multidot(const T* __restrict__ V, const T* __restrict__ w, int cnt, int64_t N,
+                              T* __restrict__ part, int stride, const int* __restrict__ flags) {
+  if (flags && flags[F_DONE]) return;
+  __shared__ T sh[NT];
+  const int64_t chunk = (N + gridDim.x - 1) / gridDim.x;
+  const int64_t lo = blockIdx.x * chunk;
+  const int64_t hi = min(N, lo + chunk);
+  for (int k = 0; k < cnt; ++k) {
+    const T* v = V + (size_t)k * N;
+    T s = T(0);
+    for (int64_t i = lo + threadIdx.x; i < hi; i += NT) s += v[i] * w[i];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = NT / 2; o > 0; o >>= 1) {
+      if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) part[(size_t)blockIdx.x * stride + k] = sh[0];
+    __syncthreads();
+  }
+}
+
+// out[k] = sum_b part[b][k] (sqrt when take_sqrt)
+template <typename T, int NT>
+__global__ void k_gm_reduce(const T* __restrict__ part, int nblk, int cnt, int stride,
+                            T* __restrict__ out, int take_sqrt, const int* __restrict__ flags) {
+  if (flags && flags[F_DONE]) return;
+  __shared__ T sh[NT];
+  for (int k = 0; k < cnt; ++k) {
+    T s = T(0);
+    for (int b = threadIdx.x; b < nblk; b += NT) s += part[(size_t)b * stride + k];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = NT / 2; o > 0; o >>= 1) {
+      if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) out[k] = take_sqrt ? sqrt(sh[0]) : sh[0];
+    __syncthreads();
+  }
+}
+
+// w -= sum_{k<cnt} V[k] h[k]
+template <typename T>
+__global__ void k_gm_sub(const T* __restrict__ V, const T* __restrict__ h, int cnt, int64_t N,
+                         T* __restrict__ w, const int* __restrict__ flags) {
+  if (flags[F_DONE]) return;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+    T acc = w[i];
+    for (int k = 0; k < cnt; ++k) acc -= V[(size_t)k * N + i] * h[k];
+    w[i] = acc;
+  }
+}
+
+// dst = src / nrm[0] (zero when nrm[0] == 0); skipped when *done unless force
+template <typename T>
+__global__ void k_gm_scale(const T* __restrict__ src, const T* __restrict__ nrm, int64_t N,
+                           T* __restrict__ dst, const int* __restrict__ flags, int force) {
+  if (!force && flags[F_DONE]) return;
+  const T s = nrm[0];
+  const T inv = (s > T(0)) ? T(1) / s : T(0);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = src[i] * inv;
+}
+
+// w = b - w
+template <typename T>
+__global__ void k_gm_bminus(const T* __restrict__ b, T* __restrict__ w, int64_t N) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x)
+    w[i] = b[i] - w[i];
+}
+
+// x += z
+template <typename T>
+__global__ void k_gm_add(const T* __restrict__ z, T* __restrict__ x, int64_t N) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x)
+    x[i] += z[i];
+}
+
+// w = sum_{k < jdone} V[k] y[k]
+template <typename T>
+__global__ void k_gm_Vy(const T* __restrict__ V, const double* __restrict__ y, int64_t N,
+                        T* __restrict__ w, const int* __restrict__ flags) {
+  const int cnt = flags[F_JDONE];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+    T acc = T(0);
+    for (int k = 0; k < cnt; ++k) acc += V[(size_t)k * N + i] * T(y[k]);
+    w[i] = acc;
+  }
+}
+
+// start of a cycle: beta = |b - A x|, g = (beta, 0, ...), decide done
+template <typename T>
+__global__ void k_gm_init(const T* __restrict__ beta, const T* __restrict__ bnorm, int first, int m,
+                          double* __restrict__ dH, int* __restrict__ flags, double* __restrict__ scal) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double* g = dH + (size_t)(m + 1) * m + 2 * m;
+  if (first) {
+    scal[S_BNORM] = double(bnorm[0]);
+    scal[S_TOL] = fmax(scal[S_RELTOL] * scal[S_BNORM], scal[S_ABSTOL]);
+    flags[F_ITS] = 0;
+  }
+  const double b = double(beta[0]);
+  scal[S_BETA] = b;
+  scal[S_RESID] = b;
+  for (int k = 0; k <= m; ++k) g[k] = 0.0;
+  g[0] = b;
+  const bool conv = !(b > scal[S_TOL]);
+  flags[F_CONV] = conv ? 1 : 0;
+  flags[F_DONE] = (conv || flags[F_ITS] >= flags[F_ITERMAX] || !isfinite(b)) ? 1 : 0;
+  flags[F_JDONE] = 0;
+}
+
+// Hessenberg column j from the two CGS passes and |w|; Givens update
+template <typename T>
+__global__ void k_gm_givens(int j, int m, const T* __restrict__ h1, const T* __restrict__ h2,
+                            const T* __restrict__ hn, double* __restrict__ dH,
+                            int* __restrict__ flags, double* __restrict__ scal) {
+  if (threadIdx.x != 0 || blockIdx.x != 0 || flags[F_DONE]) return;
+  double* H = dH;
+  double* cs = dH + (size_t)(m + 1) * m;
+  double* sn = cs + m;
+  double* g = sn + m;
+  double* Hc = H + (size_t)j * (m + 1);
+  for (int k = 0; k <= j; ++k) Hc[k] = double(h1[k]) + double(h2[k]);
+  Hc[j + 1] = double(hn[0]);
+  for (int k = 0; k < j; ++k) {
+    const double t0 = cs[k] * Hc[k] + sn[k] * Hc[k + 1];
+    Hc[k + 1] = -sn[k] * Hc[k] + cs[k] * Hc[k + 1];
+    Hc[k] = t0;
+  }
+  const double den = hypot(Hc[j], Hc[j + 1]);
+  flags[F_ITS] += 1;
+  if (!(den > 0.0) || !isfinite(den)) {  // breakdown: stop with the current basis
+    flags[F_DONE] = 1;
+    flags[F_JDONE] = j;
+    return;
+  }
+  cs[j] = Hc[j] / den;
+  sn[j] = Hc[j + 1] / den;
+  Hc[j] = den;
+  Hc[j + 1] = 0.0;
+  g[j + 1] = -sn[j] * g[j];
+  g[j] = cs[j] * g[j];
+  const double resid = fabs(g[j + 1]);
+  scal[S_RESID] = resid;
+  flags[F_JDONE] = j + 1;
+  if (resid <= scal[S_TOL] || double(hn[0]) == 0.0 || flags[F_ITS] >= flags[F_ITERMAX])
+    flags[F_DONE] = 1;
+}
+
+// y = H^-1 g on the leading jdone x jdone block
+__global__ void k_gm_lsq(int m, double* __restrict__ dH, const int* __restrict__ flags) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int n = flags[F_JDONE];
+  const double* H = dH;
+  const double* g = dH + (size_t)(m + 1) * m + 2 * m;
+  double* y = dH + (size_t)(m + 1) * m + 3 * m + 1;
+  for (int k = n - 1; k >= 0; --k) {
+    double s = g[k];
+    for (int c = k + 1; c < n; ++c) s -= H[(size_t)c * (m + 1) + k] * y[c];
+    y[k] = s / H[(size_t)k * (m + 1) + k];
+  }
+}
+
+int gridN(int64_t n) {
+  int64_t b = (n + 255) / 256;
+  return (int)(b > 152 * 8 ? 152 * 8 : (b < 1 ? 1 : b));
+}
+
+// |v| into out[0] (two launches)
+template <typename T>
+void norm_T(eg_ls* ls, const T* v, T* out, const int* flags) {
+  eg_mesh* m = ls->lo->mesh;
+  const int stride = ls->m + 2;
+  k_gm_multidot<T, 256><<<ls->nblk, 256, 0, m->stream>>>(v, v, 1, m->ndof, (T*)ls->part, stride, flags);
+  k_gm_reduce<T, 256><<<1, 256, 0, m->stream>>>((const T*)ls->part, ls->nblk, 1, stride, out, 1, flags);
+}
+
+// the launches of the initial residual + cycle set-up
+template <typename T>
+void enqueue_init(eg_ls* ls, int first) {
+  eg_mesh* m = ls->lo->mesh;
+  const int64_t N = m->ndof;
+  T* V = (T*)ls->V;
+  T* w = (T*)ls->w;
+  T* h = (T*)ls->h;  // h: [0..m+1] pass 1 | [m+2 ..] pass 2 | [2(m+2)] |w| | [2(m+2)+1] beta | +2 bnorm
+  T* beta = h + 2 * (ls->m + 2) + 1;
+  T* bnorm = h + 2 * (ls->m + 2) + 2;
+  const T* b = (const T*)ls->bT;
+  const T* x = (const T*)ls->xT;
+  if (first) norm_T<T>(ls, b, bnorm, nullptr);
+  eg_lo_apply_T(ls->lo, x, w);
+  k_gm_bminus<T><<<gridN(N), 256, 0, m->stream>>>(b, w, N);
+  norm_T<T>(ls, w, beta, nullptr);
+  k_gm_init<T><<<1, 32, 0, m->stream>>>(beta, bnorm, first, ls->m, ls->dH, ls->dflags, ls->dscal);
+  k_gm_scale<T><<<gridN(N), 256, 0, m->stream>>>(w, beta, N, V, ls->dflags, 0);
+}
+
+// one restart cycle, the update, and the set-up of the next cycle
+template <typename T>
+void enqueue_cycle(eg_ls* ls) {
+  eg_mesh* m = ls->lo->mesh;
+  const int64_t N = m->ndof;
+  const int mm = ls->m, stride = mm + 2;
+  T* V = (T*)ls->V;
+  T* w = (T*)ls->w;
+  T* z = (T*)ls->z;
+  T* h = (T*)ls->h;
+  T* h1 = h;
+  T* h2 = h + (mm + 2);
+  T* hn = h + 2 * (mm + 2);
+  T* part = (T*)ls->part;
+  const int* fl = ls->dflags;
+  for (int j = 0; j < mm; ++j) {
+    T* vj = V + (size_t)j * N;
+    eg_pc_apply_T(ls->pc, vj, z, fl);
+    eg_lo_apply_T(ls->lo, z, w, fl);
+    for (int pass = 0; pass < 2; ++pass) {
+      T* hp = pass ? h2 : h1;
+      k_gm_multidot<T, 256><<<ls->nblk, 256, 0, m->stream>>>(V, w, j + 1, N, part, stride, fl);
+      k_gm_reduce<T, 256><<<1, 256, 0, m->stream>>>(part, ls->nblk, j + 1, stride, hp, 0, fl);
+      k_gm_sub<T><<<gridN(N), 256, 0, m->stream>>>(V, hp, j + 1, N, w, fl);
+    }
+    norm_T<T>(ls, w, hn, fl);
+    k_gm_scale<T><<<gridN(N), 256, 0, m->stream>>>(w, hn, N, V + (size_t)(j + 1) * N, ls->dflags, 0);
+    k_gm_givens<T><<<1, 32, 0, m->stream>>>(j, mm, h1, h2, hn, ls->dH, ls->dflags, ls->dscal);
+  }
+  k_gm_lsq<<<1, 32, 0, m->stream>>>(mm, ls->dH, ls->dflags);
+  k_gm_Vy<T><<<gridN(N), 256, 0, m->stream>>>(V, ls->dH + (size_t)(mm + 1) * mm + 3 * mm + 1, N, w,
+                                              ls->dflags);
+  eg_pc_apply_T(ls->pc, w, z);
+  k_gm_add<T><<<gridN(N), 256, 0, m->stream>>>(z, (T*)ls->xT, N);
+  enqueue_init<T>(ls, 0);
+}
+
+// capture fn into a graph; on failure fall back to eager launches
+template <typename F>
+bool capture(eg_mesh* m, F fn, cudaGraphExec_t* exec, int64_t* nodes) {
+  if (m->stream == 0 || m->stream == cudaStreamLegacy || m->stream == cudaStreamPerThread) return false;
+  cudaGraph_t graph = nullptr;
+  m->capturing = true;
+  cudaError_t e = cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) {
+    m->capturing = false;
+    cudaGetLastError();
+    return false;
+  }
+  fn();
+  e = cudaStreamEndCapture(m->stream, &graph);
+  m->capturing = false;
+  if (e != cudaSuccess || !graph) {
+    cudaGetLastError();
+    return false;
+  }
+  size_t n = 0;
+  cudaGraphGetNodes(graph, nullptr, &n);
+  e = cudaGraphInstantiate(exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  *nodes = (int64_t)n;
+  return true;
+}
+
+template <typename T>
+int gmres_T(eg_ls* ls, eg_ls_stats* st) {
+  eg_mesh* m = ls->lo->mesh;
+  // tolerances into device memory (graphs read them there)
+  double sc[8] = {0, 0, 0, 0, ls->reltol, ls->abstol, 0, 0};
+  int fl[8] = {0, 0, 0, 0, ls->itermax, 0, 0, 0};
+  EG_CUDA(cudaMemcpyAsync(ls->dscal, sc, sizeof(sc), cudaMemcpyHostToDevice, m->stream));
+  EG_CUDA(cudaMemcpyAsync(ls->dflags, fl, sizeof(fl), cudaMemcpyHostToDevice, m->stream));
+  if (!ls->g_init && !ls->g_cycle && !ls->graphs_ok) {
+    cudaGraphExec_t gi = nullptr, gc = nullptr;
+    bool ok = capture(m, [&]() { enqueue_init<T>(ls, 1); }, &gi, &ls->g_init_nodes);
+    ok = ok && capture(m, [&]() { enqueue_cycle<T>(ls); }, &gc, &ls->g_cycle_nodes);
+    if (ok) {
+      ls->g_init = (void*)gi;
+      ls->g_cycle = (void*)gc;
+      ls->graphs_ok = true;
+    } else {
+      if (gi) cudaGraphExecDestroy(gi);
+      if (gc) cudaGraphExecDestroy(gc);
+    }
+  }
+  auto run_init = [&]() -> int {
+    if (ls->graphs_ok) {
+      EG_CUDA(cudaGraphLaunch((cudaGraphExec_t)ls->g_init, m->stream));
+      m->launches += ls->g_init_nodes;
+    } else {
+      enqueue_init<T>(ls, 1);
+      m->launches += 8;
+    }
+    return EG_OK;
+  };
+  auto run_cycle = [&]() -> int {
+    if (ls->graphs_ok) {
+      EG_CUDA(cudaGraphLaunch((cudaGraphExec_t)ls->g_cycle, m->stream));
+      m->launches += ls->g_cycle_nodes;
+    } else {
+      enqueue_cycle<T>(ls);
+      m->launches += 12 * ls->m + 12;
+    }
+    return EG_OK;
+  };
+  int rc = run_init();
+  if (rc != EG_OK) return rc;
+  int flags[8];
+  double scal[8];
+  int restarts = 0;
+  double res0 = -1.0;
+  for (;;) {
+    EG_CUDA(cudaMemcpyAsync(ls->hh, ls->dscal, sizeof(scal), cudaMemcpyDeviceToHost, m->stream));
+    EG_CUDA(cudaMemcpyAsync(ls->hh + 8, ls->dflags, sizeof(flags), cudaMemcpyDeviceToHost, m->stream));
+    EG_CUDA(cudaStreamSynchronize(m->stream));
+    std::memcpy(scal, ls->hh, sizeof(scal));
+    std::memcpy(flags, ls->hh + 8, sizeof(flags));
+    if (res0 < 0) res0 = scal[S_BETA];
+    if (!std::isfinite(scal[S_BETA])) {
+      eg_set_error("GMRES: non-finite residual");
+      return EG_ERR_NONFINITE;
+    }
+    if (flags[F_DONE]) break;
+    rc = run_cycle();
+    if (rc != EG_OK) return rc;
+    ++restarts;
+  }
+  EG_CUDA(cudaGetLastError());
+  if (st) {
+    st->iters = flags[F_ITS];
+    st->restarts = restarts;
+    st->converged = flags[F_CONV];
+    st->res0 = res0;
+    st->res_final = scal[S_BETA];
+  }
+  return EG_OK;
+}
+
+}  // namespace
+
+void eg_gmres_release(eg_ls* ls) {
+  if (ls->g_init) cudaGraphExecDestroy((cudaGraphExec_t)ls->g_init);
+  if (ls->g_cycle) cudaGraphExecDestroy((cudaGraphExec_t)ls->g_cycle);
+  ls->g_init = ls->g_cycle = nullptr;
+  ls->graphs_ok = false;
+}
+
+// x_T <- GMRES(J, b_T) from the initial guess in x_T; the graphs are bound to
+// ls->bT / ls->xT, so callers stage their vectors there.
+int eg_gmres_T(eg_ls* ls, const void* bT, void* xT, eg_ls_stats* st) {
+  if (bT != ls->bT || xT != ls->xT) {
+    eg_set_error("GMRES: right-hand side and solution must be the solver's staging vectors");
+    return EG_ERR_INVALID;
+  }
+  return ls->lo->prec == EG_F64 ? gmres_T<double>(ls, st) : gmres_T<float>(ls, st);
+}

@@ -91,6 +91,7 @@ struct eg_mesh {
   TimerState* timer;        // phase timers (null until enabled)
   int64_t launches;         // kernel launches since creation
   int32_t h_bndry_offsets[64];  // host copy of the BC-group offsets
+  bool capturing;           // a CUDA graph is being captured on `stream`
 };
 
 // phase timers: bracket a group of launches on m->stream

@@ -43,14 +43,24 @@ struct eg_ls {
   double* xd;      // [ndof] FP64 staging
   double* bd;      // [ndof]
   int nblk;
+  // device-side GMRES state (eg_gmres.cu)
+  double* dH;      // H | cs | sn | g | y  (FP64)
+  int* dflags;     // done, jdone, its, converged, itermax
+  double* dscal;   // tol, resid, beta, bnorm, reltol, abstol
+  void* g_init;    // cudaGraphExec_t: residual + cycle initialisation
+  void* g_cycle;   // cudaGraphExec_t: one restart cycle + update + re-initialisation
+  int64_t g_init_nodes, g_cycle_nodes;
+  bool graphs_ok;  // capture succeeded (else the same launches run eagerly)
 };
+void eg_gmres_release(eg_ls* ls);
 
 // kernels shared across translation units
 int eg_jacobian_launch(eg_lo* lo, const double* q);
-// y = J x in the operator precision (device pointers of that precision)
-int eg_lo_apply_T(eg_lo* lo, const void* x, void* y);
+// y = J x in the operator precision (device pointers of that precision);
+// with `done` non-null the launch does nothing while *done != 0
+int eg_lo_apply_T(eg_lo* lo, const void* x, void* y, const int* done = nullptr);
 // y = M^-1 x in the operator precision
-int eg_pc_apply_T(eg_pc* pc, const void* x, void* y);
+int eg_pc_apply_T(eg_pc* pc, const void* x, void* y, const int* done = nullptr);
 // precision conversion helpers (device)
 int eg_convert(eg_mesh* m, const double* src, void* dst, int prec, int64_t n, double scale);
 int eg_convert_back(eg_mesh* m, const void* src, double* dst, int prec, int64_t n);

@@ -26,9 +26,10 @@ namespace {
 template <int DIM, typename T>
 __global__ void k_spmv(DevMesh md, const T* __restrict__ diag, const T* __restrict__ cpl,
                        const int* __restrict__ spos, const T* __restrict__ x, T* __restrict__ y,
-                       int epb) {
+                       int epb, const int* __restrict__ done) {
   constexpr int NV = DIM + 2;
   constexpr int F = DIM + 1;
+  if (done && *done) return;
   extern __shared__ unsigned char smraw[];
   T* sx = reinterpret_cast<T*>(smraw);
   const int Np = md.Np, S = md.S, Nf = md.Nf;
@@ -145,7 +146,8 @@ __global__ void k_block_inverse(const T* __restrict__ blocks, T* __restrict__ in
 // y_e = inv_e x_e (batched dense matrix-vector product, thread per row)
 template <typename T>
 __global__ void k_block_apply(const T* __restrict__ inv, const T* __restrict__ x, T* __restrict__ y,
-                              int E, int n, int epb) {
+                              int E, int n, int epb, const int* __restrict__ done) {
+  if (done && *done) return;
   extern __shared__ unsigned char smraw[];
   T* sx = reinterpret_cast<T*>(smraw);
   const int e0 = blockIdx.x * epb;
@@ -264,7 +266,7 @@ int grid_for(int64_t n) {
 }
 
 template <typename T>
-int spmv_T(eg_lo* lo, const T* x, T* y) {
+int spmv_T(eg_lo* lo, const T* x, T* y, const int* done = nullptr) {
   eg_mesh* m = lo->mesh;
   DevMesh md = dev_mesh(m);
   const int n = lo->n;
@@ -275,16 +277,16 @@ int spmv_T(eg_lo* lo, const T* x, T* y) {
   eg_phase_begin(m, EG_PHASE_OTHER);
   if (m->dim == 2)
     k_spmv<2, T><<<blocks, epb * n, smem, m->stream>>>(md, (const T*)lo->diag, (const T*)lo->cpl,
-                                                      lo->spos, x, y, epb);
+                                                      lo->spos, x, y, epb, done);
   else
     k_spmv<3, T><<<blocks, epb * n, smem, m->stream>>>(md, (const T*)lo->diag, (const T*)lo->cpl,
-                                                      lo->spos, x, y, epb);
+                                                      lo->spos, x, y, epb, done);
   eg_phase_end(m, EG_PHASE_OTHER, 1);
   return EG_OK;
 }
 
 template <typename T>
-int pcapply_T(eg_pc* pc, const T* x, T* y) {
+int pcapply_T(eg_pc* pc, const T* x, T* y, const int* done = nullptr) {
   eg_lo* lo = pc->lo;
   eg_mesh* m = lo->mesh;
   const int n = lo->n;
@@ -293,7 +295,7 @@ int pcapply_T(eg_pc* pc, const T* x, T* y) {
   const int blocks = (m->E + epb - 1) / epb;
   eg_phase_begin(m, EG_PHASE_OTHER);
   k_block_apply<T><<<blocks, epb * n, sizeof(T) * (size_t)epb * n, m->stream>>>(
-      (const T*)pc->inv, x, y, m->E, n, epb);
+      (const T*)pc->inv, x, y, m->E, n, epb, done);
   eg_phase_end(m, EG_PHASE_OTHER, 1);
   return EG_OK;
 }
@@ -308,148 +310,6 @@ int pccalc_T(eg_pc* pc) {
   eg_phase_begin(m, EG_PHASE_OTHER);
   k_block_inverse<T><<<m->E, 256, smem, m->stream>>>((const T*)lo->diag, (T*)pc->inv, n, m->status);
   eg_phase_end(m, EG_PHASE_OTHER, 1);
-  return EG_OK;
-}
-
-// ---------------------------------------------------------------- GMRES
-template <typename T>
-int gmres_T(eg_ls* ls, const T* b, T* x, eg_ls_stats* st) {
-  eg_lo* lo = ls->lo;
-  eg_mesh* m = lo->mesh;
-  const int64_t N = m->ndof;
-  const int mm = ls->m;
-  const int nblk = ls->nblk;
-  const int stride = mm + 2;
-  T* V = (T*)ls->V;
-  T* w = (T*)ls->w;
-  T* z = (T*)ls->z;
-  T* part = (T*)ls->part;
-  T* h = (T*)ls->h;
-  T* yv = (T*)ls->y;
-  const int g = grid_for(N);
-  std::vector<double> H((size_t)(mm + 1) * mm, 0.0), cs(mm), sn(mm), gvec(mm + 1), yh(mm);
-  auto norm_into = [&](const T* v, T* out) {
-    k_multidot<T, 256><<<nblk, 256, 0, m->stream>>>(v, v, 1, N, part, stride);
-    k_reduce_parts<T, 256><<<1, 256, 0, m->stream>>>(part, nblk, 1, stride, out, 2);
-    m->launches += 2;
-  };
-  auto fetch = [&](int cnt) -> int {
-    T tmp[64];
-    EG_CUDA(cudaMemcpyAsync(tmp, h, sizeof(T) * cnt, cudaMemcpyDeviceToHost, m->stream));
-    EG_CUDA(cudaStreamSynchronize(m->stream));
-    for (int k = 0; k < cnt; ++k) ls->hh[k] = double(tmp[k]);
-    return EG_OK;
-  };
-  // r = b - A x  (into V[0])
-  int its = 0, restarts = 0;
-  double beta = 0.0, res0 = -1.0, bnorm = 0.0;
-  norm_into(b, h);
-  if (fetch(1) != EG_OK) return EG_ERR_CUDA;
-  bnorm = ls->hh[0];
-  bool converged = false;
-  double resid = 0.0;
-  while (true) {
-    spmv_T<T>(lo, x, w);
-    k_axpby<T><<<g, 256, 0, m->stream>>>(T(1), b, T(-1), w, N);  // w = b - A x
-    m->launches += 1;
-    norm_into(w, h);
-    if (fetch(1) != EG_OK) return EG_ERR_CUDA;
-    beta = ls->hh[0];
-    if (res0 < 0) res0 = beta;
-    resid = beta;
-    const double tol = fmax(ls->reltol * bnorm, ls->abstol);
-    if (!(beta > tol) || its >= ls->itermax) {
-      converged = !(beta > tol);
-      break;
-    }
-    if (!std::isfinite(beta)) {
-      eg_set_error("GMRES: non-finite residual");
-      return EG_ERR_NONFINITE;
-    }
-    k_scale_by_inv<T><<<g, 256, 0, m->stream>>>(w, h, N, V);  // v0 = r / beta
-    m->launches += 1;
-    std::fill(gvec.begin(), gvec.end(), 0.0);
-    gvec[0] = beta;
-    int j = 0;
-    for (; j < mm && its < ls->itermax; ++j) {
-      ++its;
-      T* vj = V + (size_t)j * N;
-      pcapply_T<T>(ls->pc, vj, z);
-      spmv_T<T>(lo, z, w);
-      // classical Gram-Schmidt, twice: pass-1 coefficients in h[0..j],
-      // pass-2 coefficients in h2[0..j] (h2 = h + mm + 2), ||w|| in h[j+1]
-      T* h2 = h + (mm + 2);
-      for (int pass = 0; pass < 2; ++pass) {
-        T* hp = pass ? h2 : h;
-        k_multidot<T, 256><<<nblk, 256, 0, m->stream>>>(V, w, j + 1, N, part, stride);
-        k_reduce_parts<T, 256><<<1, 256, 0, m->stream>>>(part, nblk, j + 1, stride, hp, 0);
-        k_sub_Vh<T><<<g, 256, 0, m->stream>>>(V, hp, j + 1, N, w);
-        m->launches += 3;
-      }
-      norm_into(w, h + j + 1);
-      k_scale_by_inv<T><<<g, 256, 0, m->stream>>>(w, h + j + 1, N, V + (size_t)(j + 1) * N);
-      m->launches += 1;
-      // host: H[0..j, j] = pass1 + pass2, H[j+1, j] = ||w||
-      T tmp[2 * 64];
-      EG_CUDA(cudaMemcpyAsync(tmp, h, sizeof(T) * 2 * (mm + 2), cudaMemcpyDeviceToHost, m->stream));
-      EG_CUDA(cudaStreamSynchronize(m->stream));
-      double* Hc = &H[(size_t)j * (mm + 1)];
-      for (int k = 0; k <= j; ++k) Hc[k] = double(tmp[k]) + double(tmp[mm + 2 + k]);
-      Hc[j + 1] = double(tmp[j + 1]);
-      // Givens rotations
-      for (int k = 0; k < j; ++k) {
-        const double t0 = cs[k] * Hc[k] + sn[k] * Hc[k + 1];
-        Hc[k + 1] = -sn[k] * Hc[k] + cs[k] * Hc[k + 1];
-        Hc[k] = t0;
-      }
-      const double den = std::hypot(Hc[j], Hc[j + 1]);
-      if (den == 0.0) {
-        eg_set_error("GMRES: breakdown (zero Hessenberg column)");
-        return EG_ERR_KRYLOV;
-      }
-      cs[j] = Hc[j] / den;
-      sn[j] = Hc[j + 1] / den;
-      Hc[j] = den;
-      Hc[j + 1] = 0.0;
-      gvec[j + 1] = -sn[j] * gvec[j];
-      gvec[j] = cs[j] * gvec[j];
-      resid = std::fabs(gvec[j + 1]);
-      if (!std::isfinite(resid)) {
-        eg_set_error("GMRES: non-finite residual estimate");
-        return EG_ERR_NONFINITE;
-      }
-      if (resid <= tol || tmp[j + 1] == T(0)) {
-        ++j;
-        break;
-      }
-    }
-    // y = H^-1 g (upper triangular j x j), x += M^-1 V y
-    for (int k = j - 1; k >= 0; --k) {
-      double s = gvec[k];
-      for (int c = k + 1; c < j; ++c) s -= H[(size_t)c * (mm + 1) + k] * yh[c];
-      yh[k] = s / H[(size_t)k * (mm + 1) + k];
-    }
-    T ytmp[128];
-    for (int k = 0; k < j; ++k) ytmp[k] = T(yh[k]);
-    EG_CUDA(cudaMemcpyAsync(yv, ytmp, sizeof(T) * j, cudaMemcpyHostToDevice, m->stream));
-    k_Vy<T><<<g, 256, 0, m->stream>>>(V, yv, j, N, w);
-    m->launches += 1;
-    pcapply_T<T>(ls->pc, w, z);
-    k_axpby<T><<<g, 256, 0, m->stream>>>(T(1), z, T(1), x, N);
-    m->launches += 1;
-    EG_CUDA(cudaStreamSynchronize(m->stream));
-    ++restarts;
-    if (resid <= tol) {
-      // recompute the true residual on the next pass of the loop
-    }
-  }
-  if (st) {
-    st->iters = its;
-    st->restarts = restarts;
-    st->converged = converged ? 1 : 0;
-    st->res0 = res0;
-    st->res_final = resid;
-  }
   return EG_OK;
 }
 
@@ -476,19 +336,14 @@ int eg_convert_back(eg_mesh* m, const void* src, double* dst, int prec, int64_t 
   return EG_OK;
 }
 
-int eg_lo_apply_T(eg_lo* lo, const void* x, void* y) {
-  return lo->prec == EG_F64 ? spmv_T<double>(lo, (const double*)x, (double*)y)
-                            : spmv_T<float>(lo, (const float*)x, (float*)y);
+int eg_lo_apply_T(eg_lo* lo, const void* x, void* y, const int* done) {
+  return lo->prec == EG_F64 ? spmv_T<double>(lo, (const double*)x, (double*)y, done)
+                            : spmv_T<float>(lo, (const float*)x, (float*)y, done);
 }
 
-int eg_pc_apply_T(eg_pc* pc, const void* x, void* y) {
-  return pc->lo->prec == EG_F64 ? pcapply_T<double>(pc, (const double*)x, (double*)y)
-                                : pcapply_T<float>(pc, (const float*)x, (float*)y);
-}
-
-int eg_gmres_T(eg_ls* ls, const void* bT, void* xT, eg_ls_stats* st) {
-  return ls->lo->prec == EG_F64 ? gmres_T<double>(ls, (const double*)bT, (double*)xT, st)
-                                : gmres_T<float>(ls, (const float*)bT, (float*)xT, st);
+int eg_pc_apply_T(eg_pc* pc, const void* x, void* y, const int* done) {
+  return pc->lo->prec == EG_F64 ? pcapply_T<double>(pc, (const double*)x, (double*)y, done)
+                                : pcapply_T<float>(pc, (const float*)x, (float*)y, done);
 }
 
 static void lo_free(eg_lo* lo) {
@@ -682,7 +537,9 @@ extern "C" int eg_pc_apply(eg_pc* pc, const double* x, double* y, int32_t mem) {
 
 static void ls_free(eg_ls* ls) {
   if (!ls) return;
-  void* bufs[] = {ls->V, ls->w, ls->z, ls->xT, ls->bT, ls->part, ls->h, ls->y, ls->xd, ls->bd};
+  eg_gmres_release(ls);
+  void* bufs[] = {ls->V, ls->w, ls->z, ls->xT, ls->bT, ls->part, ls->h, ls->y, ls->xd, ls->bd,
+                  ls->dH, ls->dflags, ls->dscal};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (ls->hh) cudaFreeHost(ls->hh);
@@ -712,11 +569,17 @@ extern "C" int eg_ls_create(eg_lo* lo, eg_pc* pc, int32_t restart, eg_ls** out) 
   if (e == cudaSuccess) e = cudaMalloc(&ls->xT, es * N);
   if (e == cudaSuccess) e = cudaMalloc(&ls->bT, es * N);
   if (e == cudaSuccess) e = cudaMalloc(&ls->part, es * (size_t)ls->nblk * (restart + 2));
-  if (e == cudaSuccess) e = cudaMalloc(&ls->h, es * 2 * (restart + 2));
+  if (e == cudaSuccess) e = cudaMalloc(&ls->h, es * 4 * (restart + 2));
   if (e == cudaSuccess) e = cudaMalloc(&ls->y, es * (restart + 1));
+  // Hessenberg, Givens and least-squares state in FP64: H[(m+1) m] | cs[m] |
+  // sn[m] | g[m+1] | y[m]
+  if (e == cudaSuccess)
+    e = cudaMalloc((void**)&ls->dH, sizeof(double) * ((size_t)(restart + 1) * restart + 4 * (restart + 1)));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&ls->dflags, sizeof(int) * 8);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&ls->dscal, sizeof(double) * 8);
   if (e == cudaSuccess) e = cudaMalloc((void**)&ls->xd, 8 * N);
   if (e == cudaSuccess) e = cudaMalloc((void**)&ls->bd, 8 * N);
-  if (e == cudaSuccess) e = cudaMallocHost((void**)&ls->hh, 8 * (restart + 2));
+  if (e == cudaSuccess) e = cudaMallocHost((void**)&ls->hh, 8 * (restart + 16));
   if (e != cudaSuccess) {
     ls_free(ls);
     return eg_cuda_fail(e, "eg_ls_create");

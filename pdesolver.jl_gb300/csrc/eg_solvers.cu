@@ -330,3 +330,46 @@ extern "C" int eg_rk4(eg_mesh* m, double* q, double h, double t_max, int32_t ite
   }
   return st;
 }
+
+namespace {
+// q_hi[e][r] = sum_c T[r][c] q_lo[e][c]
+__global__ void k_prolong(const double* __restrict__ T, const double* __restrict__ qlo,
+                          double* __restrict__ qhi, int E, int nlo, int nhi) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < (int64_t)E * nhi;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int e = (int)(t / nhi), r = (int)(t - (int64_t)e * nhi);
+    const double* x = qlo + (size_t)e * nlo;
+    const double* Tr = T + (size_t)r * nlo;
+    double acc = 0.0;
+    for (int c = 0; c < nlo; ++c) acc = fma(Tr[c], x[c], acc);
+    qhi[t] = acc;
+  }
+}
+}  // namespace
+
+extern "C" int eg_prolong(eg_mesh* lo, const double* q_lo, eg_mesh* hi, double* q_hi, const double* T,
+                          int32_t mem) {
+  if (!lo || !hi || !q_lo || !q_hi || !T || lo->E != hi->E || lo->nv != hi->nv) {
+    eg_set_error("eg_prolong: invalid argument (meshes must share their elements)");
+    return EG_ERR_INVALID;
+  }
+  const int nlo = lo->Np * lo->nv, nhi = hi->Np * hi->nv;
+  double* dT = nullptr;
+  EG_CUDA(cudaMalloc((void**)&dT, sizeof(double) * (size_t)nlo * nhi));
+  EG_CUDA(cudaMemcpyAsync(dT, T, sizeof(double) * (size_t)nlo * nhi, cudaMemcpyHostToDevice, hi->stream));
+  const double* src = q_lo;
+  double* dst = q_hi;
+  if (mem == EG_MEM_HOST) {
+    EG_CUDA(cudaMemcpyAsync(lo->q_dev, q_lo, 8 * (size_t)lo->ndof, cudaMemcpyHostToDevice, hi->stream));
+    src = lo->q_dev;
+    dst = hi->q_dev;
+  }
+  k_prolong<<<grid64((int64_t)hi->E * nhi), 256, 0, hi->stream>>>(dT, src, dst, hi->E, nlo, nhi);
+  hi->launches += 1;
+  EG_CUDA(cudaGetLastError());
+  if (mem == EG_MEM_HOST)
+    EG_CUDA(cudaMemcpyAsync(q_hi, dst, 8 * (size_t)hi->ndof, cudaMemcpyDeviceToHost, hi->stream));
+  EG_CUDA(cudaStreamSynchronize(hi->stream));
+  cudaFree(dT);
+  return EG_OK;
+}

@@ -30,12 +30,13 @@ static cudaEvent_t take_event(TimerState* t) {
 void eg_phase_begin(eg_mesh* m, int phase) {
   (void)phase;
   TimerState* t = m->timer;
-  if (!t || !t->enabled) return;
+  if (!t || !t->enabled || m->capturing) return;
   t->open_ev = take_event(t);
   cudaEventRecord(t->open_ev, m->stream);
 }
 
 void eg_phase_end(eg_mesh* m, int phase, int nlaunch) {
+  if (m->capturing) return;  // graph nodes are counted per replay
   m->launches += nlaunch;
   TimerState* t = m->timer;
   if (!t || !t->enabled || !t->open_ev) return;

@@ -61,6 +61,7 @@ def _declare(lib):
     lib.eg_get_timings.argtypes = [vp, C.POINTER(Timings)]
     lib.eg_reset_timings.argtypes = [vp]
     lib.eg_calc_functional.argtypes = [vp, vp, C.c_int32, C.c_int32, dp]
+    lib.eg_prolong.argtypes = [vp, vp, vp, vp, vp, C.c_int32]
     lib.eg_lo_create.argtypes = [vp, C.c_int32, C.POINTER(vp)]
     lib.eg_lo_destroy.argtypes = [vp]
     lib.eg_lo_calc.argtypes = [vp, vp, C.c_int32]
@@ -388,3 +389,47 @@ class LinearSolver:
             self.close()
         except Exception:
             pass
+
+
+def prolongation_matrix(op_lo, op_hi, nv):
+    """T[(j,a)][(m,b)] = delta_ab P[j][m] with P the degree-p_lo interpolation
+    from op_lo's nodes to op_hi's nodes (least squares where op_lo has more
+    nodes than degree-p_lo polynomials, as SBP-Gamma does)."""
+    from . import sbp as _sbp
+    V_lo, _ = _sbp.vandermonde(op_lo.nodes, op_lo.p)
+    V_hi, _ = _sbp.vandermonde(op_hi.nodes, op_lo.p)
+    P = V_hi @ np.linalg.pinv(V_lo)
+    return np.ascontiguousarray(np.kron(P, np.eye(nv)))
+
+
+def prolong(g_lo: GPUMesh, q_lo, g_hi: GPUMesh, q_hi):
+    """q_hi <- degree prolongation of q_lo (same elements, on the device)."""
+    T = prolongation_matrix(g_lo.mesh.sbp, g_hi.mesh.sbp, g_lo.mesh.numDofPerNode)
+    pl, ml = GPUMesh._ptr(q_lo)
+    ph, mh = GPUMesh._ptr(q_hi)
+    if ml != mh:
+        raise ValueError("q_lo and q_hi must both be host or both be device arrays")
+    check(g_lo.lib.eg_prolong(g_lo.handle, pl, g_hi.handle, ph, C.c_void_p(T.ctypes.data), ml))
+    return q_hi
+
+
+def solve_steady(levels, q_lo, opts=None, precision=0, level_tol=None):
+    """Steady solve with p-continuation: Newton on levels[0] (a GPUMesh of the
+    lowest degree) from q_lo, prolong the result to the next level, Newton
+    again, up to levels[-1].  Intermediate levels stop at level_tol (default:
+    the final tolerance).  Returns (q of the last level, list of stats)."""
+    opts = dict(opts or {})
+    stats = []
+    q = q_lo
+    for k, g in enumerate(levels):
+        if k > 0:
+            qn = np.zeros((g.mesh.numEl, g.mesh.numNodesPerElement, g.mesh.numDofPerNode)) \
+                if isinstance(q, np.ndarray) else q.new_zeros(
+                    (g.mesh.numEl, g.mesh.numNodesPerElement, g.mesh.numDofPerNode))
+            prolong(levels[k - 1], q, g, qn)
+            q = qn
+        o = dict(opts)
+        if k < len(levels) - 1 and level_tol is not None:
+            o["res_abstol"] = level_tol
+        stats.append(g.newton(q, o, precision=precision))
+    return q, stats
