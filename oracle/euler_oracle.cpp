@@ -14,6 +14,7 @@
 // interiorfaceintegrate!, boundaryinterpolate!, boundaryintegrate!) belong to
 // SummationByParts.jl, which is not vendored; they are restated from their
 // call sites with the operator fields interp / perm / nbrperm / wface.
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -767,4 +768,37 @@ double oracle_functional_pressure(const eg_mesh_desc* d, const eg_params* ep, co
   return val;
 }
 
+}  // extern "C"
+
+extern "C" {
+// Per-phase host times of one Newton iteration of the oracle (test
+// infrastructure, used for a bounded CPU baseline sample): out[0] residual,
+// out[1] Jacobian, out[2] block LU factorisation, out[3] one GMRES iteration
+// (averaged over n_gmres iterations), all in seconds.
+int oracle_newton_phase_times(const eg_mesh_desc* d, const eg_params* p, const double* q,
+                              int n_gmres, double* out) {
+  using clk = std::chrono::steady_clock;
+  const int NV = d->dim + 2, n = d->nodes_per_el * NV, nb = d->stencil_size * NV;
+  const size_t N = (size_t)d->num_el * n;
+  std::vector<double> res(N), diag((size_t)d->num_el * n * n),
+      cpl((size_t)d->num_interfaces * 2 * nb * nb), b(N), x(N, 0.0);
+  auto t0 = clk::now();
+  int st = oracle_eval_residual(d, p, q, res.data());
+  if (st != EG_OK) return st;
+  auto t1 = clk::now();
+  oracle_eval_jacobian(d, p, q, diag.data(), cpl.data());
+  auto t2 = clk::now();
+  BlockLU lu;
+  if (!lu.factor(d, diag.data(), n)) return EG_ERR_LU_PIVOT;
+  auto t3 = clk::now();
+  for (size_t i = 0; i < N; ++i) b[i] = -res[i];
+  int its = 0;
+  gmres(d, n, nb, diag.data(), cpl.data(), lu, b, x, n_gmres, 1e-30, 0.0, n_gmres, &its);
+  auto t4 = clk::now();
+  out[0] = std::chrono::duration<double>(t1 - t0).count();
+  out[1] = std::chrono::duration<double>(t2 - t1).count();
+  out[2] = std::chrono::duration<double>(t3 - t2).count();
+  out[3] = std::chrono::duration<double>(t4 - t3).count() / std::max(its, 1);
+  return EG_OK;
+}
 }  // extern "C"

@@ -629,3 +629,25 @@ extern "C" int eg_ls_solve(eg_ls* ls, const double* b, double* x, int32_t mem, e
   EG_CUDA(cudaStreamSynchronize(m->stream));
   return EG_OK;
 }
+
+extern "C" int eg_lo_apply_native(eg_lo* lo, const void* x, void* y) {
+  if (!lo || !x || !y || !lo->valid) {
+    eg_set_error("eg_lo_apply_native: invalid argument or operator not computed");
+    return EG_ERR_INVALID;
+  }
+  int st = eg_lo_apply_T(lo, x, y);
+  if (st != EG_OK) return st;
+  EG_CUDA(cudaGetLastError());
+  return EG_OK;
+}
+
+extern "C" int eg_pc_apply_native(eg_pc* pc, const void* x, void* y) {
+  if (!pc || !x || !y || !pc->valid) {
+    eg_set_error("eg_pc_apply_native: invalid argument or preconditioner not computed");
+    return EG_ERR_INVALID;
+  }
+  int st = eg_pc_apply_T(pc, x, y);
+  if (st != EG_OK) return st;
+  EG_CUDA(cudaGetLastError());
+  return EG_OK;
+}

@@ -67,6 +67,8 @@ def _declare(lib):
     lib.eg_lo_calc.argtypes = [vp, vp, C.c_int32]
     lib.eg_lo_apply.argtypes = [vp, vp, vp, C.c_int32]
     lib.eg_lo_get_blocks.argtypes = [vp, vp, vp]
+    lib.eg_lo_apply_native.argtypes = [vp, vp, vp]
+    lib.eg_pc_apply_native.argtypes = [vp, vp, vp]
     lib.eg_pc_create.argtypes = [vp, C.POINTER(vp)]
     lib.eg_pc_destroy.argtypes = [vp]
     lib.eg_pc_calc.argtypes = [vp]
@@ -308,6 +310,11 @@ class LinearOperator:
         check(self.lib.eg_lo_apply(self.handle, px, py, mx))
         return y
 
+    def apply_native(self, x_dev, y_dev):
+        """y = J x on device tensors of the operator's precision (enqueued)."""
+        check(self.lib.eg_lo_apply_native(self.handle, C.c_void_p(x_dev.data_ptr()),
+                                          C.c_void_p(y_dev.data_ptr())))
+
     def blocks(self):
         ms = self.g.mesh
         diag = np.zeros((ms.numEl, self.n, self.n))
@@ -346,6 +353,11 @@ class BlockJacobiPC:
         py, _ = GPUMesh._ptr(y)
         check(self.lib.eg_pc_apply(self.handle, px, py, mx))
         return y
+
+    def apply_native(self, x_dev, y_dev):
+        """y = M^-1 x on device tensors of the operator's precision (enqueued)."""
+        check(self.lib.eg_pc_apply_native(self.handle, C.c_void_p(x_dev.data_ptr()),
+                                          C.c_void_p(y_dev.data_ptr())))
 
     def close(self):
         if getattr(self, "handle", None):
