@@ -447,7 +447,25 @@ def run_kernels_only(args, which):
     g = eulergpu.GPUMesh(ms, opts)
     g.set_stream(stream.cuda_stream)
     out = {}
-    if which == "krylov":
+    if which == "gmres":
+        # one Newton linear system: FP32 Jacobian + block-Jacobi at the initial
+        # state, GMRES(30) for `steps` iterations (one restart cycle per 30)
+        lo = eulergpu.LinearOperator(g, precision=1)
+        lo.calc(q)
+        pc = eulergpu.BlockJacobiPC(lo)
+        pc.calc()
+        ls = eulergpu.LinearSolver(pc, lo, restart=30)
+        ls.set_tolerances(reltol=1e-12, abstol=0.0, itermax=args.steps)
+        b = np.random.default_rng(0).normal(size=q.shape)
+        x = np.zeros_like(b)
+        ls.solve(b, x)                       # capture + warm
+        x[...] = 0
+        t0 = time.perf_counter()
+        st = ls.solve(b, x)
+        out["gmres_its"] = st.iters
+        out["ms_per_iteration_wall"] = 1e3 * (time.perf_counter() - t0) / max(st.iters, 1)
+        out["kernels"] = ["GMRES cycle"]
+    elif which == "krylov":
         lo = eulergpu.LinearOperator(g, precision=1)
         lo.calc(q)
         pc = eulergpu.BlockJacobiPC(lo)
@@ -475,7 +493,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--only", default=None, choices=["krylov", "residual"],
+    ap.add_argument("--only", default=None, choices=["krylov", "residual", "gmres"],
                     help="run only the isolated kernels (for profiler captures)")
     args = ap.parse_args()
     if args.only:

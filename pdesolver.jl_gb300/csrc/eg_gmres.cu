@@ -3,8 +3,9 @@
 // Reference: linearSolve -> PETSc KSPSolve with GMRES(30), right
 // preconditioning (src/linearsolvers/ls_standard.jl:321-371,
 // src/input/read_input.jl:559-569).  The algorithm is Saad's GMRES(m) with
-// classical Gram-Schmidt applied twice (CGS2; as stable as the reference's
-// modified Gram-Schmidt, but each pass is one batched multi-dot kernel).
+// classical Gram-Schmidt and a second pass when the Daniel-Gragg-Kaufman-
+// Stewart test asks for it (as stable as the reference's modified
+// Gram-Schmidt, but each pass is one batched multi-dot kernel).
 //
 // GB300 design: the Hessenberg column, Givens rotations, convergence test and
 // the small triangular solve all run on the device (FP64, one thread), so a
@@ -22,14 +23,21 @@
 
 namespace {
 
-enum { F_DONE = 0, F_JDONE = 1, F_ITS = 2, F_CONV = 3, F_ITERMAX = 4 };
+enum { F_DONE = 0, F_JDONE = 1, F_ITS = 2, F_CONV = 3, F_ITERMAX = 4, F_REORTH = 5 };
+
+// a cycle kernel runs unless the cycle is done, or its optional condition
+// flag (need >= 0) is zero
+__device__ __forceinline__ bool gm_skip(const int* flags, int need) {
+  return flags && (flags[F_DONE] || (need >= 0 && !flags[need]));
+}
 enum { S_TOL = 0, S_RESID = 1, S_BETA = 2, S_BNORM = 3, S_RELTOL = 4, S_ABSTOL = 5 };
 
 // per-block partial sums of V[k] . w for k < cnt (skips when *done)
 template <typename T, int NT>
 __global__ void k_gm_multidot(const T* __restrict__ V, const T* __restrict__ w, int cnt, int64_t N,
-                              T* __restrict__ part, int stride, const int* __restrict__ flags) {
-  if (flags && flags[F_DONE]) return;
+                              T* __restrict__ part, int stride, const int* __restrict__ flags,
+                              int need) {
+  if (gm_skip(flags, need)) return;
   __shared__ T sh[NT];
   const int64_t chunk = (N + gridDim.x - 1) / gridDim.x;
   const int64_t lo = blockIdx.x * chunk;
@@ -52,8 +60,9 @@ __global__ void k_gm_multidot(const T* __restrict__ V, const T* __restrict__ w, 
 // out[k] = sum_b part[b][k] (sqrt when take_sqrt)
 template <typename T, int NT>
 __global__ void k_gm_reduce(const T* __restrict__ part, int nblk, int cnt, int stride,
-                            T* __restrict__ out, int take_sqrt, const int* __restrict__ flags) {
-  if (flags && flags[F_DONE]) return;
+                            T* __restrict__ out, int take_sqrt, const int* __restrict__ flags,
+                            int need) {
+  if (gm_skip(flags, need)) return;
   __shared__ T sh[NT];
   for (int k = 0; k < cnt; ++k) {
     T s = T(0);
@@ -72,8 +81,8 @@ __global__ void k_gm_reduce(const T* __restrict__ part, int nblk, int cnt, int s
 // w -= sum_{k<cnt} V[k] h[k]
 template <typename T>
 __global__ void k_gm_sub(const T* __restrict__ V, const T* __restrict__ h, int cnt, int64_t N,
-                         T* __restrict__ w, const int* __restrict__ flags) {
-  if (flags[F_DONE]) return;
+                         T* __restrict__ w, const int* __restrict__ flags, int need) {
+  if (gm_skip(flags, need)) return;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
     T acc = w[i];
     for (int k = 0; k < cnt; ++k) acc -= V[(size_t)k * N + i] * h[k];
@@ -178,17 +187,258 @@ __global__ void k_gm_givens(int j, int m, const T* __restrict__ h1, const T* __r
     flags[F_DONE] = 1;
 }
 
-// y = H^-1 g on the leading jdone x jdone block
+// selective re-orthogonalisation (Daniel-Gragg-Kaufman-Stewart test): after
+// one classical Gram-Schmidt pass, |w|^2 before the pass is sum h1^2 + |w|^2
+// after it; a second pass is needed only when |w| dropped below 1/sqrt(2) of
+// that.  Without one, the second-pass coefficients h2 are zero.
+template <typename T>
+__global__ void k_gm_reorth_check(int j, const T* __restrict__ h1, const T* __restrict__ hn,
+                                  T* __restrict__ h2, int* __restrict__ flags) {
+  if (threadIdx.x != 0 || blockIdx.x != 0 || flags[F_DONE]) return;
+  double before = double(hn[0]) * double(hn[0]);
+  for (int k = 0; k <= j; ++k) before += double(h1[k]) * double(h1[k]);
+  const int need = double(hn[0]) * double(hn[0]) < 0.5 * before;
+  flags[F_REORTH] = need;
+  if (!need)
+    for (int k = 0; k <= j; ++k) h2[k] = T(0);
+}
+
+// y = H^-1 g on the leading jdone x jdone block (H staged in shared memory)
 __global__ void k_gm_lsq(int m, double* __restrict__ dH, const int* __restrict__ flags) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  __shared__ double sH[32 * 33];
+  __shared__ double sg[33];
   const int n = flags[F_JDONE];
   const double* H = dH;
   const double* g = dH + (size_t)(m + 1) * m + 2 * m;
   double* y = dH + (size_t)(m + 1) * m + 3 * m + 1;
+  for (int t = threadIdx.x; t < n * (m + 1); t += blockDim.x) sH[t] = H[t];
+  for (int t = threadIdx.x; t < n; t += blockDim.x) sg[t] = g[t];
+  __syncthreads();
+  if (threadIdx.x != 0) return;
   for (int k = n - 1; k >= 0; --k) {
-    double s = g[k];
-    for (int c = k + 1; c < n; ++c) s -= H[(size_t)c * (m + 1) + k] * y[c];
-    y[k] = s / H[(size_t)k * (m + 1) + k];
+    double s = sg[k];
+    for (int c = k + 1; c < n; ++c) s -= sH[(size_t)c * (m + 1) + k] * sg[c];
+    sg[k] = s / sH[(size_t)k * (m + 1) + k];
+  }
+  for (int k = 0; k < n; ++k) y[k] = sg[k];
+}
+
+// ---- fused Arnoldi kernels --------------------------------------------------
+// The basis has at most 32 vectors (restart <= 31).  Partial sums go to
+// part[block][k]; the last block to finish (threadfence + counter) reduces
+// them in block order, so the results are deterministic and no separate
+// reduction launch is needed.
+
+// Givens update of Hessenberg column j (h1 + h2 when a second pass ran)
+template <typename T>
+__device__ void gm_givens_core(int j, int m, const T* h1, const T* h2, double hn, double* dH,
+                               int* flags, double* scal) {
+  double* H = dH;
+  double* cs = dH + (size_t)(m + 1) * m;
+  double* sn = cs + m;
+  double* g = sn + m;
+  double* Hc = H + (size_t)j * (m + 1);
+  for (int k = 0; k <= j; ++k) Hc[k] = double(h1[k]) + (h2 ? double(h2[k]) : 0.0);
+  Hc[j + 1] = hn;
+  for (int k = 0; k < j; ++k) {
+    const double t0 = cs[k] * Hc[k] + sn[k] * Hc[k + 1];
+    Hc[k + 1] = -sn[k] * Hc[k] + cs[k] * Hc[k + 1];
+    Hc[k] = t0;
+  }
+  const double den = hypot(Hc[j], Hc[j + 1]);
+  flags[F_ITS] += 1;
+  if (!(den > 0.0) || !isfinite(den)) {  // breakdown: stop with the current basis
+    flags[F_DONE] = 1;
+    flags[F_JDONE] = j;
+    return;
+  }
+  cs[j] = Hc[j] / den;
+  sn[j] = Hc[j + 1] / den;
+  Hc[j] = den;
+  Hc[j + 1] = 0.0;
+  g[j + 1] = -sn[j] * g[j];
+  g[j] = cs[j] * g[j];
+  const double resid = fabs(g[j + 1]);
+  scal[S_RESID] = resid;
+  flags[F_JDONE] = j + 1;
+  if (resid <= scal[S_TOL] || hn == 0.0 || flags[F_ITS] >= flags[F_ITERMAX]) flags[F_DONE] = 1;
+}
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// true in every thread of the last block to arrive
+__device__ __forceinline__ bool last_block(unsigned int* counter) {
+  __shared__ bool s_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  __syncthreads();
+  return s_last;
+}
+
+// vector load of W consecutive values (16-byte aligned when W > 1)
+template <typename T, int W> struct VecOf;
+template <> struct VecOf<float, 4> { using type = float4; };
+template <> struct VecOf<double, 2> { using type = double2; };
+template <typename T, int W>
+__device__ __forceinline__ void vload(const T* p, T (&v)[W]) {
+  if constexpr (W == 1) {
+    v[0] = p[0];
+  } else {
+    const auto t = *reinterpret_cast<const typename VecOf<T, W>::type*>(p);
+    if constexpr (W == 4) { v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w; }
+    else { v[0] = t.x; v[1] = t.y; }
+  }
+}
+template <typename T, int W>
+__device__ __forceinline__ void vstore(T* p, const T (&v)[W]) {
+  if constexpr (W == 1) {
+    p[0] = v[0];
+  } else if constexpr (W == 4) {
+    *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+  } else {
+    *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]);
+  }
+}
+
+// h[k] = V[k] . w for k < cnt (and ww = w . w when with_ww).  Each thread
+// owns groups of W consecutive rows and accumulates every coefficient in
+// registers (W-wide vector loads of all basis vectors in flight at once);
+// warp shuffles and shared memory combine the block's partials.
+template <typename T, int W>
+__global__ void __launch_bounds__(256) k_gm_dots2(const T* __restrict__ V, const T* __restrict__ w,
+                                                  int cnt, int with_ww, int64_t N, T* __restrict__ part,
+                                                  int stride, const int* __restrict__ flags, int need,
+                                                  unsigned int* __restrict__ counter, T* __restrict__ h,
+                                                  T* __restrict__ ww) {
+  if (gm_skip(flags, need)) return;
+  __shared__ T sred[8][33];
+  const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
+  const int64_t ng = N / W;                         // row groups (N % W == 0)
+  const int64_t chunk = (ng + gridDim.x - 1) / gridDim.x;
+  const int64_t lo = blockIdx.x * chunk;
+  const int64_t hi = min(ng, lo + chunk);
+  T acc[33];
+#pragma unroll
+  for (int k = 0; k < 33; ++k) acc[k] = T(0);
+  for (int64_t g = lo + threadIdx.x; g < hi; g += 256) {
+    T wv[W];
+    vload<T, W>(w + g * W, wv);
+#pragma unroll
+    for (int k = 0; k < 32; ++k) {
+      if (k < cnt) {
+        T vv[W];
+        vload<T, W>(V + (size_t)k * N + g * W, vv);
+#pragma unroll
+        for (int q = 0; q < W; ++q) acc[k] += vv[q] * wv[q];
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < W; ++q) acc[32] += wv[q] * wv[q];
+  }
+#pragma unroll
+  for (int k = 0; k < 33; ++k) {
+    if (k < cnt || (k == 32 && with_ww)) {
+      const T v = warp_sum(acc[k]);
+      if (lane == 0) sred[wq][k] = v;
+    }
+  }
+  __syncthreads();
+  T* pb = part + (size_t)blockIdx.x * stride;
+  for (int k = threadIdx.x; k < 33; k += 256) {
+    if (k < cnt || (k == 32 && with_ww)) {
+      T v = T(0);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) v += sred[q][k];
+      pb[k == 32 ? cnt : k] = v;
+    }
+  }
+  if (!last_block(counter)) return;
+  const int tot = cnt + (with_ww ? 1 : 0);
+  for (int k = wq; k < tot; k += 8) {
+    T v = T(0);
+    for (int b = lane; b < (int)gridDim.x; b += 32) v += part[(size_t)b * stride + k];
+    v = warp_sum(v);
+    if (lane == 0) {
+      if (k < cnt) h[k] = v;
+      else ww[0] = v;
+    }
+  }
+  if (threadIdx.x == 0) *counter = 0u;
+}
+
+// w -= sum_k V[k] h[k]; then |w| and, in the last block, the DGKS test
+// (pass 1) and/or the Givens update of column j
+template <typename T, int W>
+__global__ void __launch_bounds__(256) k_gm_sub2(const T* __restrict__ V, const T* __restrict__ h,
+                                                 int cnt, int64_t N, T* __restrict__ w,
+                                                 T* __restrict__ part, int stride, const int* __restrict__ flagsc,
+                                                 int need, unsigned int* __restrict__ counter, int pass, int j,
+                                                 int m, const T* __restrict__ h1, const T* __restrict__ h2,
+                                                 const T* __restrict__ ww, T* __restrict__ hn,
+                                                 double* __restrict__ dH, int* __restrict__ flags,
+                                                 double* __restrict__ scal) {
+  if (gm_skip(flagsc, need)) return;
+  __shared__ T sh[32];
+  __shared__ T sw[8];
+  if (threadIdx.x < cnt) sh[threadIdx.x] = h[threadIdx.x];
+  __syncthreads();
+  const int64_t ng = N / W;
+  const int64_t chunk = (ng + gridDim.x - 1) / gridDim.x;
+  const int64_t lo = blockIdx.x * chunk;
+  const int64_t hi = min(ng, lo + chunk);
+  T acc = T(0);
+  for (int64_t g = lo + threadIdx.x; g < hi; g += 256) {
+    T a[W];
+    vload<T, W>(w + g * W, a);
+#pragma unroll
+    for (int k = 0; k < 32; ++k) {
+      if (k < cnt) {
+        T vv[W];
+        vload<T, W>(V + (size_t)k * N + g * W, vv);
+        const T hk = sh[k];
+#pragma unroll
+        for (int q = 0; q < W; ++q) a[q] -= vv[q] * hk;
+      }
+    }
+    vstore<T, W>(w + g * W, a);
+#pragma unroll
+    for (int q = 0; q < W; ++q) acc += a[q] * a[q];
+  }
+  acc = warp_sum(acc);
+  if ((threadIdx.x & 31) == 0) sw[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    T t = T(0);
+    for (int q = 0; q < 8; ++q) t += sw[q];
+    part[(size_t)blockIdx.x * stride] = t;
+  }
+  if (!last_block(counter)) return;
+  if (threadIdx.x < 32) {
+    T v = T(0);
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += 32) v += part[(size_t)b * stride];
+    v = warp_sum(v);
+    if (threadIdx.x == 0) {
+      *counter = 0u;
+      const double n2 = double(v);
+      hn[0] = T(sqrt(n2));
+      if (pass == 1) {
+        const int need2 = n2 < 0.5 * double(ww[0]);
+        flags[F_REORTH] = need2;
+        if (!need2) gm_givens_core<T>(j, m, h1, nullptr, sqrt(n2), dH, flags, scal);
+      } else {
+        gm_givens_core<T>(j, m, h1, h2, sqrt(n2), dH, flags, scal);
+      }
+    }
   }
 }
 
@@ -198,15 +448,17 @@ int gridN(int64_t n) {
 }
 
 // |v| into out[0] (two launches)
+// |v| into out[0] (two launches)
 template <typename T>
-void norm_T(eg_ls* ls, const T* v, T* out, const int* flags) {
+void norm_T(eg_ls* ls, const T* v, T* out, const int* flags, int need = -1) {
   eg_mesh* m = ls->lo->mesh;
   const int stride = ls->m + 2;
-  k_gm_multidot<T, 256><<<ls->nblk, 256, 0, m->stream>>>(v, v, 1, m->ndof, (T*)ls->part, stride, flags);
-  k_gm_reduce<T, 256><<<1, 256, 0, m->stream>>>((const T*)ls->part, ls->nblk, 1, stride, out, 1, flags);
+  k_gm_multidot<T, 256><<<ls->nblk, 256, 0, m->stream>>>(v, v, 1, m->ndof, (T*)ls->part, stride, flags, need);
+  k_gm_reduce<T, 256><<<1, 256, 0, m->stream>>>((const T*)ls->part, ls->nblk, 1, stride, out, 1, flags, need);
 }
 
-// the launches of the initial residual + cycle set-up
+// the launches of the initial residual + cycle set-up (the k_gm_* kernels
+// take flags == nullptr to run unconditionally)
 template <typename T>
 void enqueue_init(eg_ls* ls, int first) {
   eg_mesh* m = ls->lo->mesh;
@@ -226,6 +478,46 @@ void enqueue_init(eg_ls* ls, int first) {
   k_gm_scale<T><<<gridN(N), 256, 0, m->stream>>>(w, beta, N, V, ls->dflags, 0);
 }
 
+// vector width of the Arnoldi kernels: 16-byte loads when the vector length
+// allows (every 2-D problem: nv = 4)
+template <typename T>
+int vec_width(int64_t N) {
+  const int W = sizeof(T) == 4 ? 4 : 2;
+  return (N % W == 0) ? W : 1;
+}
+
+template <typename T>
+void launch_dots(eg_ls* ls, const T* V, const T* w, int cnt, int with_ww, const int* fl, int need,
+                 unsigned int* counter, T* h, T* ww) {
+  eg_mesh* m = ls->lo->mesh;
+  const int stride = ls->m + 2;
+  const int64_t N = m->ndof;
+  T* part = (T*)ls->part;
+  if (vec_width<T>(N) > 1)
+    k_gm_dots2<T, (sizeof(T) == 4 ? 4 : 2)><<<ls->nblk, 256, 0, m->stream>>>(
+        V, w, cnt, with_ww, N, part, stride, fl, need, counter, h, ww);
+  else
+    k_gm_dots2<T, 1><<<ls->nblk, 256, 0, m->stream>>>(V, w, cnt, with_ww, N, part, stride, fl, need,
+                                                      counter, h, ww);
+}
+
+template <typename T>
+void launch_sub(eg_ls* ls, const T* V, const T* h, int cnt, T* w, const int* fl, int need,
+                unsigned int* counter, int pass, int j, const T* h1, const T* h2, const T* ww, T* hn) {
+  eg_mesh* m = ls->lo->mesh;
+  const int stride = ls->m + 2;
+  const int64_t N = m->ndof;
+  T* part = (T*)ls->part;
+  if (vec_width<T>(N) > 1)
+    k_gm_sub2<T, (sizeof(T) == 4 ? 4 : 2)><<<ls->nblk, 256, 0, m->stream>>>(
+        V, h, cnt, N, w, part, stride, fl, need, counter, pass, j, ls->m, h1, h2, ww, hn, ls->dH,
+        ls->dflags, ls->dscal);
+  else
+    k_gm_sub2<T, 1><<<ls->nblk, 256, 0, m->stream>>>(V, h, cnt, N, w, part, stride, fl, need, counter,
+                                                     pass, j, ls->m, h1, h2, ww, hn, ls->dH, ls->dflags,
+                                                     ls->dscal);
+}
+
 // one restart cycle, the update, and the set-up of the next cycle
 template <typename T>
 void enqueue_cycle(eg_ls* ls) {
@@ -243,19 +535,21 @@ void enqueue_cycle(eg_ls* ls) {
   const int* fl = ls->dflags;
   for (int j = 0; j < mm; ++j) {
     T* vj = V + (size_t)j * N;
+    // w = J M^-1 v_j = v_j + C (D^-1 v_j): the element blocks cancel with
+    // their inverses, so only the coupling blocks are read here
     eg_pc_apply_T(ls->pc, vj, z, fl);
-    eg_lo_apply_T(ls->lo, z, w, fl);
-    for (int pass = 0; pass < 2; ++pass) {
-      T* hp = pass ? h2 : h1;
-      k_gm_multidot<T, 256><<<ls->nblk, 256, 0, m->stream>>>(V, w, j + 1, N, part, stride, fl);
-      k_gm_reduce<T, 256><<<1, 256, 0, m->stream>>>(part, ls->nblk, j + 1, stride, hp, 0, fl);
-      k_gm_sub<T><<<gridN(N), 256, 0, m->stream>>>(V, hp, j + 1, N, w, fl);
-    }
-    norm_T<T>(ls, w, hn, fl);
+    eg_cpl_apply_T(ls->lo, vj, z, w, fl);
+    // classical Gram-Schmidt (with |w|^2 before, for the DGKS test), a second
+    // pass only when the test asks, Givens on the device
+    T* ww = hn + 3;  // slots hn+1, hn+2 hold beta and |b| (enqueue_init)
+    unsigned int* cnt = (unsigned int*)(ls->dflags + 8);
+    launch_dots<T>(ls, V, w, j + 1, 1, fl, -1, cnt, h1, ww);
+    launch_sub<T>(ls, V, h1, j + 1, w, fl, -1, cnt + 1, 1, j, h1, h2, ww, hn);
+    launch_dots<T>(ls, V, w, j + 1, 0, fl, F_REORTH, cnt, h2, ww);
+    launch_sub<T>(ls, V, h2, j + 1, w, fl, F_REORTH, cnt + 1, 2, j, h1, h2, ww, hn);
     k_gm_scale<T><<<gridN(N), 256, 0, m->stream>>>(w, hn, N, V + (size_t)(j + 1) * N, ls->dflags, 0);
-    k_gm_givens<T><<<1, 32, 0, m->stream>>>(j, mm, h1, h2, hn, ls->dH, ls->dflags, ls->dscal);
   }
-  k_gm_lsq<<<1, 32, 0, m->stream>>>(mm, ls->dH, ls->dflags);
+  k_gm_lsq<<<1, 256, 0, m->stream>>>(mm, ls->dH, ls->dflags);
   k_gm_Vy<T><<<gridN(N), 256, 0, m->stream>>>(V, ls->dH + (size_t)(mm + 1) * mm + 3 * mm + 1, N, w,
                                               ls->dflags);
   eg_pc_apply_T(ls->pc, w, z);

@@ -12,7 +12,7 @@
 //
 // Storage (element-block sparse, column-major blocks, see eulergpu.h):
 //   diag[E][Np*nv][Np*nv]          element blocks (volume + own face terms)
-//   cpl[I][2][S*nv][S*nv]          interface coupling blocks LR, RL
+//   cpl[I][2][S*nv][S*nv]          interface coupling blocks LR, RL (row-major)
 // Kernels (templated on the precision T of the Jacobian: double or float):
 //   k_face_jac     one thread per (face slot, face node): dF/dqL, dF/dqR
 //   k_elem_jac     one CTA per element: sum_k Q_k(m,j) A_k(q_m) into a shared
@@ -179,7 +179,8 @@ __global__ void k_elem_jac(DevMesh md, const double* __restrict__ q, const T* __
   for (int t = threadIdx.x; t < n * n; t += blockDim.x) dst[t] = sB[t];
 }
 
-// Interface coupling blocks.  cpl[nI][side][col = s'*NV+b][row = s*NV+a]:
+// Interface coupling blocks, stored row-major so an operator row is one
+// contiguous read: cpl[nI][side][row = s*NV+a][col = s'*NV+b]:
 //   side 0: rows elementL stencil, cols elementR stencil, from dF/dqR, sign -
 //   side 1: rows elementR stencil, cols elementL stencil, from dF/dqL, sign +
 template <int DIM, typename T>
@@ -194,7 +195,7 @@ __global__ void k_couple_jac(DevMesh md, const T* __restrict__ dF, T* __restrict
   const int rem = (int)(t - (int64_t)nI * per);
   const int side = rem / (nb * nb);
   const int cr = rem - side * nb * nb;
-  const int col = cr / nb, row = cr - col * nb;
+  const int row = cr / nb, col = cr - row * nb;
   const int sp = col / NV, b = col - sp * NV;
   const int s = row / NV, a = row - s * NV;
   const int* itf = md.ifaces + 5 * nI;

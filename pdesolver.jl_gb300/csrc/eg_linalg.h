@@ -59,6 +59,9 @@ int eg_jacobian_launch(eg_lo* lo, const double* q);
 // y = J x in the operator precision (device pointers of that precision);
 // with `done` non-null the launch does nothing while *done != 0
 int eg_lo_apply_T(eg_lo* lo, const void* x, void* y, const int* done = nullptr);
+// w = v + C z: the preconditioned operator J M^-1 v with z = M^-1 v, using the
+// coupling blocks only (the element blocks times their inverses are I)
+int eg_cpl_apply_T(eg_lo* lo, const void* v, const void* z, void* w, const int* done = nullptr);
 // y = M^-1 x in the operator precision
 int eg_pc_apply_T(eg_pc* pc, const void* x, void* y, const int* done = nullptr);
 // precision conversion helpers (device)

@@ -20,33 +20,18 @@
 namespace {
 
 // ---------------------------------------------------------------- SpMV
-// y[e][r] = sum_c diag[e][c][r] x[e][c] + face couplings of row r.
-// One CTA per `epb` elements, one thread per row; x of the CTA's elements in
-// shared memory; coupling operands read from the neighbours (L2).
+// Face-coupling part of row r of element e: sum over the element's interface
+// faces whose stencil holds row r's node of C (coupling block) x (neighbour's
+// stencil values).
 template <int DIM, typename T>
-__global__ void k_spmv(DevMesh md, const T* __restrict__ diag, const T* __restrict__ cpl,
-                       const int* __restrict__ spos, const T* __restrict__ x, T* __restrict__ y,
-                       int epb, const int* __restrict__ done) {
+__device__ __forceinline__ T coupling_row(const DevMesh& md, const T* __restrict__ cpl,
+                                          const int* __restrict__ spos, const T* __restrict__ x,
+                                          int e, int r, int n) {
   constexpr int NV = DIM + 2;
   constexpr int F = DIM + 1;
-  if (done && *done) return;
-  extern __shared__ unsigned char smraw[];
-  T* sx = reinterpret_cast<T*>(smraw);
-  const int Np = md.Np, S = md.S, Nf = md.Nf;
-  (void)Nf;
-  const int n = Np * NV, nb = S * NV;
-  const int e0 = blockIdx.x * epb;
-  const int nloc = min(epb, md.E - e0);
-  for (int t = threadIdx.x; t < nloc * n; t += blockDim.x) sx[t] = x[(size_t)e0 * n + t];
-  __syncthreads();
-  const int le = threadIdx.x / n, r = threadIdx.x - le * n;
-  if (le >= nloc) return;
-  const int e = e0 + le;
-  const T* D = diag + (size_t)e * n * n;
-  const T* xe = sx + (size_t)le * n;
-  T acc = T(0);
-  for (int c = 0; c < n; ++c) acc += D[(size_t)c * n + r] * xe[c];
+  const int Np = md.Np, S = md.S, nb = S * NV;
   const int j = r / NV, a = r - j * NV;
+  T acc = T(0);
 #pragma unroll
   for (int f = 0; f < F; ++f) {
     const int s = spos[f * Np + j];
@@ -56,16 +41,78 @@ __global__ void k_spmv(DevMesh md, const T* __restrict__ diag, const T* __restri
     const int* itf = md.ifaces + 5 * ef.slot;
     const int en = ef.side ? itf[0] : itf[1];
     const int fn = ef.side ? itf[2] : itf[3];
-    const T* C = cpl + ((size_t)ef.slot * 2 + ef.side) * nb * nb;
+    // row (s, a) of the row-major coupling block: nb contiguous values
+    const T* C = cpl + (((size_t)ef.slot * 2 + ef.side) * nb + s * NV + a) * nb;
     const T* xn = x + (size_t)en * n;
     for (int sp = 0; sp < S; ++sp) {
-      const int mnode = md.perm[fn * S + sp];
+      const T* xs = xn + md.perm[fn * S + sp] * NV;
 #pragma unroll
-      for (int b = 0; b < NV; ++b)
-        acc += C[(size_t)(sp * NV + b) * nb + s * NV + a] * xn[mnode * NV + b];
+      for (int b = 0; b < NV; ++b) acc += C[sp * NV + b] * xs[b];
     }
   }
+  return acc;
+}
+
+// dense element-block row: sum_c A[c*n + r] xe[c]; NB > 0 fixes n at compile
+// time so the loads of a row are all in flight at once
+template <int NB, typename T>
+__device__ __forceinline__ T block_row(const T* __restrict__ A, const T* __restrict__ xe, int r, int n) {
+  T acc0 = T(0), acc1 = T(0), acc2 = T(0), acc3 = T(0);
+  if (NB > 0) {
+#pragma unroll
+    for (int c = 0; c < NB; c += 4) {
+      acc0 += A[(size_t)c * NB + r] * xe[c];
+      if (c + 1 < NB) acc1 += A[(size_t)(c + 1) * NB + r] * xe[c + 1];
+      if (c + 2 < NB) acc2 += A[(size_t)(c + 2) * NB + r] * xe[c + 2];
+      if (c + 3 < NB) acc3 += A[(size_t)(c + 3) * NB + r] * xe[c + 3];
+    }
+  } else {
+#pragma unroll 4
+    for (int c = 0; c < n; ++c) acc0 += A[(size_t)c * n + r] * xe[c];
+  }
+  return (acc0 + acc1) + (acc2 + acc3);
+}
+
+// y[e][r] = sum_c diag[e][c][r] x[e][c] + face couplings of row r.
+// One CTA per `epb` elements, one thread per row; x of the CTA's elements in
+// shared memory; coupling operands read from the neighbours (L2).
+template <int DIM, int NB, typename T>
+__global__ void k_spmv(DevMesh md, const T* __restrict__ diag, const T* __restrict__ cpl,
+                       const int* __restrict__ spos, const T* __restrict__ x, T* __restrict__ y,
+                       int epb, const int* __restrict__ done) {
+  constexpr int NV = DIM + 2;
+  if (done && *done) return;
+  extern __shared__ unsigned char smraw[];
+  T* sx = reinterpret_cast<T*>(smraw);
+  const int n = NB > 0 ? NB : md.Np * NV;
+  const int e0 = blockIdx.x * epb;
+  const int nloc = min(epb, md.E - e0);
+  for (int t = threadIdx.x; t < nloc * n; t += blockDim.x) sx[t] = x[(size_t)e0 * n + t];
+  __syncthreads();
+  const int le = threadIdx.x / n, r = threadIdx.x - le * n;
+  if (le >= nloc) return;
+  const int e = e0 + le;
+  T acc = block_row<NB, T>(diag + (size_t)e * n * n, sx + (size_t)le * n, r, n);
+  acc += coupling_row<DIM, T>(md, cpl, spos, x, e, r, n);
   y[(size_t)e * n + r] = acc;
+}
+
+// Right-preconditioned operator without the element blocks:
+// (D + C) D^-1 v = v + C z with z = D^-1 v (z computed by k_block_apply).
+// Inside the Arnoldi loop this replaces k_spmv + the diagonal-block read.
+template <int DIM, typename T>
+__global__ void k_cpl_apply(DevMesh md, const T* __restrict__ cpl, const int* __restrict__ spos,
+                            const T* __restrict__ v, const T* __restrict__ z, T* __restrict__ w,
+                            const int* __restrict__ done) {
+  constexpr int NV = DIM + 2;
+  if (done && *done) return;
+  const int n = md.Np * NV;
+  const int64_t N = (int64_t)md.E * n;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int e = (int)(t / n), r = (int)(t - (int64_t)e * n);
+    w[t] = v[t] + coupling_row<DIM, T>(md, cpl, spos, z, e, r, n);
+  }
 }
 
 // ---------------------------------------------------------------- block-Jacobi
@@ -144,23 +191,21 @@ __global__ void k_block_inverse(const T* __restrict__ blocks, T* __restrict__ in
 }
 
 // y_e = inv_e x_e (batched dense matrix-vector product, thread per row)
-template <typename T>
+template <int NB, typename T>
 __global__ void k_block_apply(const T* __restrict__ inv, const T* __restrict__ x, T* __restrict__ y,
-                              int E, int n, int epb, const int* __restrict__ done) {
+                              int E, int nrt, int epb, const int* __restrict__ done) {
   if (done && *done) return;
   extern __shared__ unsigned char smraw[];
   T* sx = reinterpret_cast<T*>(smraw);
+  const int n = NB > 0 ? NB : nrt;
   const int e0 = blockIdx.x * epb;
   const int nloc = min(epb, E - e0);
   for (int t = threadIdx.x; t < nloc * n; t += blockDim.x) sx[t] = x[(size_t)e0 * n + t];
   __syncthreads();
   const int le = threadIdx.x / n, r = threadIdx.x - le * n;
   if (le >= nloc) return;
-  const T* A = inv + (size_t)(e0 + le) * n * n;
-  const T* xe = sx + (size_t)le * n;
-  T acc = T(0);
-  for (int c = 0; c < n; ++c) acc += A[(size_t)c * n + r] * xe[c];
-  y[(size_t)(e0 + le) * n + r] = acc;
+  y[(size_t)(e0 + le) * n + r] =
+      block_row<NB, T>(inv + (size_t)(e0 + le) * n * n, sx + (size_t)le * n, r, n);
 }
 
 // ---------------------------------------------------------------- vectors
@@ -265,6 +310,25 @@ int grid_for(int64_t n) {
   return (int)(b > 152 * 16 ? 152 * 16 : (b < 1 ? 1 : b));
 }
 
+// element-block sizes with a compiled specialisation (Np * nv of the tri
+// Omega/Gamma operators p = 1..4 and the tet diagonal-E p = 1)
+#define EG_NB_CASES(X) X(12) X(24) X(28) X(40) X(48) X(60) X(72) X(30)
+
+template <int DIM, typename T>
+void launch_spmv(eg_mesh* m, const DevMesh& md, const eg_lo* lo, const T* x, T* y, int blocks,
+                 int threads, size_t smem, int epb, const int* done) {
+  const T* D = (const T*)lo->diag;
+  const T* Cp = (const T*)lo->cpl;
+  switch (lo->n) {
+#define EG_CASE(NBV) \
+  case NBV: k_spmv<DIM, NBV, T><<<blocks, threads, smem, m->stream>>>(md, D, Cp, lo->spos, x, y, epb, done); return;
+    EG_NB_CASES(EG_CASE)
+#undef EG_CASE
+    default:
+      k_spmv<DIM, 0, T><<<blocks, threads, smem, m->stream>>>(md, D, Cp, lo->spos, x, y, epb, done);
+  }
+}
+
 template <typename T>
 int spmv_T(eg_lo* lo, const T* x, T* y, const int* done = nullptr) {
   eg_mesh* m = lo->mesh;
@@ -276,11 +340,25 @@ int spmv_T(eg_lo* lo, const T* x, T* y, const int* done = nullptr) {
   const size_t smem = sizeof(T) * (size_t)epb * n;
   eg_phase_begin(m, EG_PHASE_OTHER);
   if (m->dim == 2)
-    k_spmv<2, T><<<blocks, epb * n, smem, m->stream>>>(md, (const T*)lo->diag, (const T*)lo->cpl,
-                                                      lo->spos, x, y, epb, done);
+    launch_spmv<2, T>(m, md, lo, x, y, blocks, epb * n, smem, epb, done);
   else
-    k_spmv<3, T><<<blocks, epb * n, smem, m->stream>>>(md, (const T*)lo->diag, (const T*)lo->cpl,
-                                                      lo->spos, x, y, epb, done);
+    launch_spmv<3, T>(m, md, lo, x, y, blocks, epb * n, smem, epb, done);
+  eg_phase_end(m, EG_PHASE_OTHER, 1);
+  return EG_OK;
+}
+
+template <typename T>
+int cplapply_T(eg_lo* lo, const T* v, const T* z, T* w, const int* done) {
+  eg_mesh* m = lo->mesh;
+  DevMesh md = dev_mesh(m);
+  const int64_t N = m->ndof;
+  int blocks = (int)((N + 255) / 256);
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  eg_phase_begin(m, EG_PHASE_OTHER);
+  if (m->dim == 2)
+    k_cpl_apply<2, T><<<blocks, 256, 0, m->stream>>>(md, (const T*)lo->cpl, lo->spos, v, z, w, done);
+  else
+    k_cpl_apply<3, T><<<blocks, 256, 0, m->stream>>>(md, (const T*)lo->cpl, lo->spos, v, z, w, done);
   eg_phase_end(m, EG_PHASE_OTHER, 1);
   return EG_OK;
 }
@@ -293,9 +371,17 @@ int pcapply_T(eg_pc* pc, const T* x, T* y, const int* done = nullptr) {
   int epb = 256 / n;
   if (epb < 1) epb = 1;
   const int blocks = (m->E + epb - 1) / epb;
+  const size_t smem = sizeof(T) * (size_t)epb * n;
+  const T* A = (const T*)pc->inv;
   eg_phase_begin(m, EG_PHASE_OTHER);
-  k_block_apply<T><<<blocks, epb * n, sizeof(T) * (size_t)epb * n, m->stream>>>(
-      (const T*)pc->inv, x, y, m->E, n, epb, done);
+  switch (n) {
+#define EG_CASE(NBV) \
+  case NBV: k_block_apply<NBV, T><<<blocks, epb * n, smem, m->stream>>>(A, x, y, m->E, n, epb, done); break;
+    EG_NB_CASES(EG_CASE)
+#undef EG_CASE
+    default:
+      k_block_apply<0, T><<<blocks, epb * n, smem, m->stream>>>(A, x, y, m->E, n, epb, done);
+  }
   eg_phase_end(m, EG_PHASE_OTHER, 1);
   return EG_OK;
 }
@@ -339,6 +425,11 @@ int eg_convert_back(eg_mesh* m, const void* src, double* dst, int prec, int64_t 
 int eg_lo_apply_T(eg_lo* lo, const void* x, void* y, const int* done) {
   return lo->prec == EG_F64 ? spmv_T<double>(lo, (const double*)x, (double*)y, done)
                             : spmv_T<float>(lo, (const float*)x, (float*)y, done);
+}
+
+int eg_cpl_apply_T(eg_lo* lo, const void* v, const void* z, void* w, const int* done) {
+  return lo->prec == EG_F64 ? cplapply_T<double>(lo, (const double*)v, (const double*)z, (double*)w, done)
+                            : cplapply_T<float>(lo, (const float*)v, (const float*)z, (float*)w, done);
 }
 
 int eg_pc_apply_T(eg_pc* pc, const void* x, void* y, const int* done) {
@@ -463,7 +554,16 @@ extern "C" int eg_lo_get_blocks(eg_lo* lo, double* diag, double* coupling) {
     return EG_OK;
   };
   int st = copy(lo->diag, diag, nd);
-  if (st == EG_OK) st = copy(lo->cpl, coupling, nc);
+  if (st == EG_OK && coupling && nc) {
+    // device coupling blocks are row-major; the ABI exports them column-major
+    std::vector<double> tmp(nc);
+    st = copy(lo->cpl, tmp.data(), nc);
+    const int nb = lo->nb;
+    for (size_t blk = 0; blk < (size_t)m->I * 2; ++blk)
+      for (int r = 0; r < nb; ++r)
+        for (int c = 0; c < nb; ++c)
+          coupling[blk * nb * nb + (size_t)c * nb + r] = tmp[blk * nb * nb + (size_t)r * nb + c];
+  }
   return st;
 }
 
@@ -547,8 +647,8 @@ static void ls_free(eg_ls* ls) {
 }
 
 extern "C" int eg_ls_create(eg_lo* lo, eg_pc* pc, int32_t restart, eg_ls** out) {
-  if (!lo || !pc || !out || restart < 1 || restart > 60 || pc->lo != lo) {
-    eg_set_error("eg_ls_create: invalid argument (restart must be 1..60, pc built on lo)");
+  if (!lo || !pc || !out || restart < 1 || restart > 31 || pc->lo != lo) {
+    eg_set_error("eg_ls_create: invalid argument (restart must be 1..31, pc built on lo)");
     return EG_ERR_INVALID;
   }
   eg_ls* ls = new eg_ls();
@@ -560,7 +660,7 @@ extern "C" int eg_ls_create(eg_lo* lo, eg_pc* pc, int32_t restart, eg_ls** out) 
   ls->abstol = 1e-12;
   ls->dtol = 1e5;
   ls->itermax = 1000;    // read_input.jl:496 krylov_itermax
-  ls->nblk = 304;
+  ls->nblk = 608;
   const int64_t N = lo->mesh->ndof;
   const size_t es = lo->prec == EG_F64 ? 8 : 4;
   cudaError_t e = cudaMalloc(&ls->V, es * (size_t)(restart + 1) * N);
@@ -568,14 +668,16 @@ extern "C" int eg_ls_create(eg_lo* lo, eg_pc* pc, int32_t restart, eg_ls** out) 
   if (e == cudaSuccess) e = cudaMalloc(&ls->z, es * N);
   if (e == cudaSuccess) e = cudaMalloc(&ls->xT, es * N);
   if (e == cudaSuccess) e = cudaMalloc(&ls->bT, es * N);
-  if (e == cudaSuccess) e = cudaMalloc(&ls->part, es * (size_t)ls->nblk * (restart + 2));
+  if (e == cudaSuccess) e = cudaMalloc(&ls->part, es * (size_t)ls->nblk * (restart + 2) * 2);
   if (e == cudaSuccess) e = cudaMalloc(&ls->h, es * 4 * (restart + 2));
   if (e == cudaSuccess) e = cudaMalloc(&ls->y, es * (restart + 1));
   // Hessenberg, Givens and least-squares state in FP64: H[(m+1) m] | cs[m] |
   // sn[m] | g[m+1] | y[m]
   if (e == cudaSuccess)
     e = cudaMalloc((void**)&ls->dH, sizeof(double) * ((size_t)(restart + 1) * restart + 4 * (restart + 1)));
-  if (e == cudaSuccess) e = cudaMalloc((void**)&ls->dflags, sizeof(int) * 8);
+  // flags[0..7] + two arrival counters of the fused reductions (zeroed)
+  if (e == cudaSuccess) e = cudaMalloc((void**)&ls->dflags, sizeof(int) * 16);
+  if (e == cudaSuccess) e = cudaMemset(ls->dflags, 0, sizeof(int) * 16);
   if (e == cudaSuccess) e = cudaMalloc((void**)&ls->dscal, sizeof(double) * 8);
   if (e == cudaSuccess) e = cudaMalloc((void**)&ls->xd, 8 * N);
   if (e == cudaSuccess) e = cudaMalloc((void**)&ls->bd, 8 * N);
