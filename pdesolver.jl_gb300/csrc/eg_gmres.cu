@@ -518,9 +518,9 @@ void launch_sub(eg_ls* ls, const T* V, const T* h, int cnt, T* w, const int* fl,
                                                      ls->dscal);
 }
 
-// one restart cycle, the update, and the set-up of the next cycle
+// the Arnoldi loop of one restart cycle as stream launches
 template <typename T>
-void enqueue_cycle(eg_ls* ls) {
+void enqueue_arnoldi(eg_ls* ls) {
   eg_mesh* m = ls->lo->mesh;
   const int64_t N = m->ndof;
   const int mm = ls->m, stride = mm + 2;
@@ -549,12 +549,30 @@ void enqueue_cycle(eg_ls* ls) {
     launch_sub<T>(ls, V, h2, j + 1, w, fl, F_REORTH, cnt + 1, 2, j, h1, h2, ww, hn);
     k_gm_scale<T><<<gridN(N), 256, 0, m->stream>>>(w, hn, N, V + (size_t)(j + 1) * N, ls->dflags, 0);
   }
+}
+
+// end of a cycle: y = H^-1 g, x += M^-1 V y, true residual, next set-up
+template <typename T>
+void enqueue_tail(eg_ls* ls) {
+  eg_mesh* m = ls->lo->mesh;
+  const int64_t N = m->ndof;
+  const int mm = ls->m;
+  T* V = (T*)ls->V;
+  T* w = (T*)ls->w;
+  T* z = (T*)ls->z;
   k_gm_lsq<<<1, 256, 0, m->stream>>>(mm, ls->dH, ls->dflags);
   k_gm_Vy<T><<<gridN(N), 256, 0, m->stream>>>(V, ls->dH + (size_t)(mm + 1) * mm + 3 * mm + 1, N, w,
                                               ls->dflags);
   eg_pc_apply_T(ls->pc, w, z);
   k_gm_add<T><<<gridN(N), 256, 0, m->stream>>>(z, (T*)ls->xT, N);
   enqueue_init<T>(ls, 0);
+}
+
+// one restart cycle, the update, and the set-up of the next cycle
+template <typename T>
+void enqueue_cycle(eg_ls* ls) {
+  enqueue_arnoldi<T>(ls);
+  enqueue_tail<T>(ls);
 }
 
 // capture fn into a graph; on failure fall back to eager launches
@@ -596,7 +614,8 @@ int gmres_T(eg_ls* ls, eg_ls_stats* st) {
   int fl[8] = {0, 0, 0, 0, ls->itermax, 0, 0, 0};
   EG_CUDA(cudaMemcpyAsync(ls->dscal, sc, sizeof(sc), cudaMemcpyHostToDevice, m->stream));
   EG_CUDA(cudaMemcpyAsync(ls->dflags, fl, sizeof(fl), cudaMemcpyHostToDevice, m->stream));
-  if (!ls->g_init && !ls->g_cycle && !ls->graphs_ok) {
+  const bool coop = eg_coop_supported() && !m->capturing;
+  if (!coop && !ls->g_init && !ls->g_cycle && !ls->graphs_ok) {
     cudaGraphExec_t gi = nullptr, gc = nullptr;
     bool ok = capture(m, [&]() { enqueue_init<T>(ls, 1); }, &gi, &ls->g_init_nodes);
     ok = ok && capture(m, [&]() { enqueue_cycle<T>(ls); }, &gc, &ls->g_cycle_nodes);
@@ -610,7 +629,10 @@ int gmres_T(eg_ls* ls, eg_ls_stats* st) {
     }
   }
   auto run_init = [&]() -> int {
-    if (ls->graphs_ok) {
+    if (coop) {
+      enqueue_init<T>(ls, 1);
+      m->launches += 8;
+    } else if (ls->graphs_ok) {
       EG_CUDA(cudaGraphLaunch((cudaGraphExec_t)ls->g_init, m->stream));
       m->launches += ls->g_init_nodes;
     } else {
@@ -620,7 +642,12 @@ int gmres_T(eg_ls* ls, eg_ls_stats* st) {
     return EG_OK;
   };
   auto run_cycle = [&]() -> int {
-    if (ls->graphs_ok) {
+    if (coop) {
+      int rc2 = eg_arnoldi_coop(ls);
+      if (rc2 != EG_OK) return rc2;
+      enqueue_tail<T>(ls);
+      m->launches += 12;
+    } else if (ls->graphs_ok) {
       EG_CUDA(cudaGraphLaunch((cudaGraphExec_t)ls->g_cycle, m->stream));
       m->launches += ls->g_cycle_nodes;
     } else {

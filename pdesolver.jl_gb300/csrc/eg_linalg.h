@@ -53,6 +53,10 @@ struct eg_ls {
   bool graphs_ok;  // capture succeeded (else the same launches run eagerly)
 };
 void eg_gmres_release(eg_ls* ls);
+// one Arnoldi cycle as a persistent cooperative kernel (eg_arnoldi.cu)
+#define EG_COOP_MAX_BLOCKS 1024
+int eg_arnoldi_coop(eg_ls* ls);
+bool eg_coop_supported();
 
 // kernels shared across translation units
 int eg_jacobian_launch(eg_lo* lo, const double* q);

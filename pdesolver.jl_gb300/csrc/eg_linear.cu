@@ -16,63 +16,11 @@
 #include "eg_internal.h"
 #include "eg_kernels.cuh"
 #include "eg_linalg.h"
+#include "eg_krylov.cuh"
 
 namespace {
 
 // ---------------------------------------------------------------- SpMV
-// Face-coupling part of row r of element e: sum over the element's interface
-// faces whose stencil holds row r's node of C (coupling block) x (neighbour's
-// stencil values).
-template <int DIM, typename T>
-__device__ __forceinline__ T coupling_row(const DevMesh& md, const T* __restrict__ cpl,
-                                          const int* __restrict__ spos, const T* __restrict__ x,
-                                          int e, int r, int n) {
-  constexpr int NV = DIM + 2;
-  constexpr int F = DIM + 1;
-  const int Np = md.Np, S = md.S, nb = S * NV;
-  const int j = r / NV, a = r - j * NV;
-  T acc = T(0);
-#pragma unroll
-  for (int f = 0; f < F; ++f) {
-    const int s = spos[f * Np + j];
-    if (s < 0) continue;
-    const EFace ef = md.eface[(size_t)e * F + f];
-    if (ef.slot >= md.I) continue;  // boundary face: no coupling
-    const int* itf = md.ifaces + 5 * ef.slot;
-    const int en = ef.side ? itf[0] : itf[1];
-    const int fn = ef.side ? itf[2] : itf[3];
-    // row (s, a) of the row-major coupling block: nb contiguous values
-    const T* C = cpl + (((size_t)ef.slot * 2 + ef.side) * nb + s * NV + a) * nb;
-    const T* xn = x + (size_t)en * n;
-    for (int sp = 0; sp < S; ++sp) {
-      const T* xs = xn + md.perm[fn * S + sp] * NV;
-#pragma unroll
-      for (int b = 0; b < NV; ++b) acc += C[sp * NV + b] * xs[b];
-    }
-  }
-  return acc;
-}
-
-// dense element-block row: sum_c A[c*n + r] xe[c]; NB > 0 fixes n at compile
-// time so the loads of a row are all in flight at once
-template <int NB, typename T>
-__device__ __forceinline__ T block_row(const T* __restrict__ A, const T* __restrict__ xe, int r, int n) {
-  T acc0 = T(0), acc1 = T(0), acc2 = T(0), acc3 = T(0);
-  if (NB > 0) {
-#pragma unroll
-    for (int c = 0; c < NB; c += 4) {
-      acc0 += A[(size_t)c * NB + r] * xe[c];
-      if (c + 1 < NB) acc1 += A[(size_t)(c + 1) * NB + r] * xe[c + 1];
-      if (c + 2 < NB) acc2 += A[(size_t)(c + 2) * NB + r] * xe[c + 2];
-      if (c + 3 < NB) acc3 += A[(size_t)(c + 3) * NB + r] * xe[c + 3];
-    }
-  } else {
-#pragma unroll 4
-    for (int c = 0; c < n; ++c) acc0 += A[(size_t)c * n + r] * xe[c];
-  }
-  return (acc0 + acc1) + (acc2 + acc3);
-}
-
 // y[e][r] = sum_c diag[e][c][r] x[e][c] + face couplings of row r.
 // One CTA per `epb` elements, one thread per row; x of the CTA's elements in
 // shared memory; coupling operands read from the neighbours (L2).
@@ -668,7 +616,13 @@ extern "C" int eg_ls_create(eg_lo* lo, eg_pc* pc, int32_t restart, eg_ls** out) 
   if (e == cudaSuccess) e = cudaMalloc(&ls->z, es * N);
   if (e == cudaSuccess) e = cudaMalloc(&ls->xT, es * N);
   if (e == cudaSuccess) e = cudaMalloc(&ls->bT, es * N);
-  if (e == cudaSuccess) e = cudaMalloc(&ls->part, es * (size_t)ls->nblk * (restart + 2) * 2);
+  {
+    // partial sums: stream kernels use nblk * (m + 2) * 2, the persistent
+    // Arnoldi kernel 4 * blocks * 33
+    size_t np = (size_t)ls->nblk * (restart + 2) * 2;
+    if (np < (size_t)4 * EG_COOP_MAX_BLOCKS * 33) np = (size_t)4 * EG_COOP_MAX_BLOCKS * 33;
+    if (e == cudaSuccess) e = cudaMalloc(&ls->part, es * np);
+  }
   if (e == cudaSuccess) e = cudaMalloc(&ls->h, es * 4 * (restart + 2));
   if (e == cudaSuccess) e = cudaMalloc(&ls->y, es * (restart + 1));
   // Hessenberg, Givens and least-squares state in FP64: H[(m+1) m] | cs[m] |
