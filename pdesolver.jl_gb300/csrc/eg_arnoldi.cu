@@ -34,7 +34,7 @@ namespace {
 
 enum { F_DONE = 0, F_JDONE = 1, F_ITS = 2, F_CONV = 3, F_ITERMAX = 4, F_REORTH = 5 };
 enum { S_TOL = 0, S_RESID = 1, S_BETA = 2, S_BNORM = 3 };
-constexpr int NT = 256;
+constexpr int NT = 512;
 constexpr int PSTRIDE = 33;  // partial slots per block
 
 template <typename T>
@@ -116,11 +116,11 @@ __device__ T block_sub_norm(const T* __restrict__ V, const T* __restrict__ h, in
   return t;
 }
 
-template <int DIM, typename T>
-__global__ void __launch_bounds__(NT) k_arnoldi_coop(CoopArgs<T> a) {
+template <int DIM, int NB, typename T>
+__global__ void __launch_bounds__(NT, 2) k_arnoldi_coop(CoopArgs<T> a) {
   cg::grid_group grid = cg::this_grid();
   const int nblk = gridDim.x, b = blockIdx.x, tid = threadIdx.x;
-  const int n = a.n, m = a.m;
+  const int n = NB > 0 ? NB : a.n, m = a.m;
   const int64_t N = a.N;
   // contiguous element range of this block
   const int epb = (a.E + nblk - 1) / nblk;
@@ -155,11 +155,7 @@ __global__ void __launch_bounds__(NT) k_arnoldi_coop(CoopArgs<T> a) {
     for (int t = tid; t < nrow; t += NT) {
       const int le = t / n, r = t - le * n;
       const int e = e0 + le;
-      const T* A = a.inv + (size_t)e * n * n;
-      const T* x = vj + (size_t)e * n;
-      T acc = T(0);
-      for (int c = 0; c < n; ++c) acc += A[(size_t)c * n + r] * x[c];
-      a.z[(size_t)e * n + r] = acc;
+      a.z[(size_t)e * n + r] = block_row<NB, T>(a.inv + (size_t)e * n * n, vj + (size_t)e * n, r, n);
     }
     grid.sync();
     // (2) w = v_j + C z on the block's rows
@@ -268,15 +264,20 @@ int launch_T(eg_ls* ls, int* max_blocks_cache) {
   a.n = ls->lo->n;
   a.E = m->E;
   a.N = m->ndof;
-  void* fn = m->dim == 2 ? (void*)k_arnoldi_coop<2, T> : (void*)k_arnoldi_coop<3, T>;
-  if (*max_blocks_cache <= 0) {
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, NT, 0);
-    *max_blocks_cache = sms * (per_sm < 2 ? per_sm : 2);
+  void* fn = nullptr;
+  switch (a.n) {
+#define EG_CASE(NBV) \
+  case NBV: fn = m->dim == 2 ? (void*)k_arnoldi_coop<2, NBV, T> : (void*)k_arnoldi_coop<3, NBV, T>; break;
+    EG_CASE(12) EG_CASE(24) EG_CASE(28) EG_CASE(40) EG_CASE(48) EG_CASE(60) EG_CASE(72) EG_CASE(30)
+#undef EG_CASE
+    default: fn = m->dim == 2 ? (void*)k_arnoldi_coop<2, 0, T> : (void*)k_arnoldi_coop<3, 0, T>;
   }
-  int nblk = *max_blocks_cache;
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, NT, 0);
+  (void)max_blocks_cache;
+  int nblk = sms * (per_sm < 2 ? per_sm : 2);
   if (nblk > m->E) nblk = m->E;
   if (nblk > EG_COOP_MAX_BLOCKS) nblk = EG_COOP_MAX_BLOCKS;
   if (nblk <= 0) {

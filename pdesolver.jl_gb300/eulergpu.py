@@ -425,11 +425,12 @@ def prolong(g_lo: GPUMesh, q_lo, g_hi: GPUMesh, q_hi):
     return q_hi
 
 
-def solve_steady(levels, q_lo, opts=None, precision=0, level_tol=None):
+def solve_steady(levels, q_lo, opts=None, precision=0, level_tol=None, level_opts=None):
     """Steady solve with p-continuation: Newton on levels[0] (a GPUMesh of the
     lowest degree) from q_lo, prolong the result to the next level, Newton
     again, up to levels[-1].  Intermediate levels stop at level_tol (default:
-    the final tolerance).  Returns (q of the last level, list of stats)."""
+    the final tolerance); level_opts[k] (a dict) overrides options of level k.
+    Returns (q of the last level, list of stats)."""
     opts = dict(opts or {})
     stats = []
     q = q_lo
@@ -443,5 +444,7 @@ def solve_steady(levels, q_lo, opts=None, precision=0, level_tol=None):
         o = dict(opts)
         if k < len(levels) - 1 and level_tol is not None:
             o["res_abstol"] = level_tol
+        if level_opts is not None and level_opts[k]:
+            o.update(level_opts[k])
         stats.append(g.newton(q, o, precision=precision))
     return q, stats
