@@ -292,6 +292,65 @@ __device__ __forceinline__ IRAvg<DIM, T> ir_average(const Gas& g, const T* qL, c
   return r;
 }
 
+// Per-node quantities of the Ismail-Roe averages: z1 = sqrt(rho/p),
+// zp = sqrt(rho p), their logarithms and the velocity.  Computed once per node
+// so a pair of nodes needs no square root and no logarithm.
+template <int DIM>
+struct IRNode {
+  double z1, zp, lz1, lzp, u, v, w;
+};
+
+template <int DIM>
+__device__ __forceinline__ IRNode<DIM> ir_node(const Gas& g, const double* q) {
+  IRNode<DIM> r;
+  const double p = pressure<DIM>(g, q);
+  const double rinv = 1.0 / q[0];
+  r.z1 = sqrt(q[0] / p);
+  r.zp = sqrt(q[0] * p);
+  r.lz1 = log(r.z1);
+  r.lzp = log(r.zp);
+  r.u = q[1] * rinv;
+  r.v = q[2] * rinv;
+  r.w = (DIM == 3) ? q[3] * rinv : 0.0;
+  return r;
+}
+
+// logarithmic mean from the values and their logarithms:
+// (aL - aR) / (ln aL - ln aR), or the reference's 5-term series in
+// u = ((aL - aR)/(aL + aR))^2 below 1e-3 (algebraically the reference's
+// logavg, bc_solvers.jl:942-956, with 2 divisions instead of 4 and no log)
+__device__ __forceinline__ double logavg_pre(double aL, double aR, double lL, double lR) {
+  const double s = aL + aR;
+  const double f = (aL - aR) / s;
+  const double u = f * f;
+  if (u < 1e-3) {
+    const double F = 1.0 + u * (1.0 / 3.0 + u * (1.0 / 5.0 + u * (1.0 / 7.0 + u * (1.0 / 9.0))));
+    return s / (2.0 * F);
+  }
+  return (aL - aR) / (lL - lR);
+}
+
+// Ismail-Roe averages of two nodes from their precomputed quantities
+template <int DIM>
+__device__ __forceinline__ IRAvg<DIM, double> ir_average_pre(const Gas& g, const IRNode<DIM>& L,
+                                                             const IRNode<DIM>& R) {
+  const double gamma = g.gamma, gamma_1 = g.gamma_1;
+  IRAvg<DIM, double> r;
+  const double zs = L.z1 + R.z1;
+  const double iz = 1.0 / zs;
+  const double lp = logavg_pre(L.zp, R.zp, L.lzp, R.lzp);
+  r.rho_hat = 0.5 * zs * lp;
+  r.u_hat = (L.z1 * L.u + R.z1 * R.u) * iz;
+  r.v_hat = (L.z1 * L.v + R.z1 * R.v) * iz;
+  r.w_hat = (DIM == 3) ? (L.z1 * L.w + R.z1 * R.w) * iz : 0.0;
+  r.p1_hat = (L.zp + R.zp) * iz;
+  const double p2_hat = ((gamma + 1) / (2 * gamma)) * lp / logavg_pre(L.z1, R.z1, L.lz1, R.lz1) +
+                        (gamma_1 / (2 * gamma)) * r.p1_hat;
+  r.h_hat = gamma * p2_hat / (r.rho_hat * gamma_1) +
+            0.5 * (r.u_hat * r.u_hat + r.v_hat * r.v_hat + r.w_hat * r.w_hat);
+  return r;
+}
+
 template <int DIM, typename T, typename Tn>
 __device__ __forceinline__ void ir_dir(const IRAvg<DIM, T>& a, const Tn* n, T* F) {
   constexpr int NV = DIM + 2;

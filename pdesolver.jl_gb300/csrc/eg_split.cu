@@ -7,7 +7,9 @@
 //   res_j -= 2 sum_d S_x[j,k,d] F_IR,d(q_j, q_k),  res_k += same   (k < j)
 // The IR flux is linear in its direction, so sum_d S_x[j,k,d] F_IR,d equals
 // one IR flux in the direction n_jk = S_x[j,k,:]; each pair (j,k) costs one
-// Ismail-Roe average and one projection.
+// Ismail-Roe average and one projection.  The square roots and logarithms of
+// the averages are per-node quantities, computed once per node (FP64 is the
+// scarce resource on GB300); a pair costs divisions and multiply-adds only.
 //
 // k_split_element: a CTA owns `epb` elements.  Phase 1: all threads walk the
 // element pairs, writing G_jk = 2 F_IR(q_j, q_k; n_jk) to shared memory.
@@ -37,7 +39,8 @@ __global__ void k_split_element(DevMesh md, const double* __restrict__ q,
   double* sq = sL + F * Nf * S + (F * S + 1) / 2;  // [epb][Np][NV]
   double* sG = sq + (size_t)epb * Np * NV;    // [epb][P][NV]
   double* sres = sG + (size_t)epb * P * NV;   // [epb][Np][NV]
-  short2* sPair = reinterpret_cast<short2*>(sres + (size_t)epb * Np * NV);  // [P]
+  double* sN = sres + (size_t)epb * Np * NV;  // [epb][Np][7] per-node IR quantities
+  short2* sPair = reinterpret_cast<short2*>(sN + (size_t)epb * Np * 7);  // [P]
   for (int k = threadIdx.x; k < DIM * Np * Np; k += blockDim.x) sQ[k] = md.Q[k];
   for (int k = threadIdx.x; k < F * Nf * S; k += blockDim.x) sL[k] = md.liftS[k];
   for (int k = threadIdx.x; k < F * S; k += blockDim.x) sPerm[k] = md.perm[k];
@@ -49,6 +52,13 @@ __global__ void k_split_element(DevMesh md, const double* __restrict__ q,
     sq[t] = q[(size_t)e0 * Np * NV + t];
   __syncthreads();
   const Gas g{md.gamma, md.gamma_1};
+  // per-node IR quantities (square roots and logarithms once per node)
+  for (int t = threadIdx.x; t < nloc * Np; t += blockDim.x) {
+    const eg::IRNode<DIM> nd = eg::ir_node<DIM>(g, sq + (size_t)t * NV);
+    double* o = sN + (size_t)t * 7;
+    o[0] = nd.z1; o[1] = nd.zp; o[2] = nd.lz1; o[3] = nd.lzp; o[4] = nd.u; o[5] = nd.v; o[6] = nd.w;
+  }
+  __syncthreads();
   // ---- phase 1: pair fluxes
   for (int t = threadIdx.x; t < nloc * P; t += blockDim.x) {
     const int le = t / P, pidx = t - le * P;
@@ -69,9 +79,11 @@ __global__ void k_split_element(DevMesh md, const double* __restrict__ q,
       }
       n[d] = s;  // 2 * S_x[j,k,d]
     }
-    const double* qj = sq + ((size_t)le * Np + j) * NV;
-    const double* qk = sq + ((size_t)le * Np + k) * NV;
-    auto av = eg::ir_average<DIM>(g, qj, qk);
+    const double* nj = sN + ((size_t)le * Np + j) * 7;
+    const double* nk = sN + ((size_t)le * Np + k) * 7;
+    const eg::IRNode<DIM> Lj{nj[0], nj[1], nj[2], nj[3], nj[4], nj[5], nj[6]};
+    const eg::IRNode<DIM> Lk{nk[0], nk[1], nk[2], nk[3], nk[4], nk[5], nk[6]};
+    auto av = eg::ir_average_pre<DIM>(g, Lj, Lk);
     double Fp[NV];
     eg::ir_dir<DIM>(av, n, Fp);
     double* G = sG + ((size_t)le * P + pidx) * NV;
@@ -123,7 +135,7 @@ int eg_launch_split_element(eg_mesh* m, const double* q, double* res) {
   auto smem_of = [&](int e) {
     return sizeof(double) * ((size_t)m->dim * Np * Np + (size_t)m->F * m->Nf * m->S +
                              (size_t)(m->F * m->S + 1) / 2 + (size_t)e * Np * nv +
-                             (size_t)e * P * nv + (size_t)e * Np * nv) +
+                             (size_t)e * P * nv + (size_t)e * Np * nv + (size_t)e * Np * 7) +
            sizeof(short2) * (size_t)P;
   };
   while (epb > 1 && smem_of(epb) > 160 * 1024) --epb;
