@@ -437,7 +437,7 @@ def run_ours(args, rank, world, dist):
 C3_WORKLOAD = ("explicit RK4: unit cube 24^3 hexes -> 6 tets (82,944 elements), warped (0.05 sin, "
                "seeded phase, quadratic geometry), diagonal-E p=2 (23 nodes), Ismail-Roe split-form "
                "volume + IR faces, free-stream boundaries, Mach 0.5 free stream with density * "
-               "(1 + N(0, 0.01)) seed 4; one step = one RK4 time step (4 FP64 residuals), dt 2e-3")
+               "(1 + N(0, 0.01)) seed 4; one step = one RK4 time step (4 FP64 residuals), dt 1e-3")
 
 
 def split_model(ms):
@@ -471,7 +471,7 @@ def run_c3(args, rank, world):
     g = eulergpu.GPUMesh(ms, opts)
     g.set_stream(stream.cuda_stream)
     qd = torch.from_numpy(q).cuda()
-    h = 2e-3
+    h = 1e-3   # the oracle is unstable at 2e-3 on this mesh, stable at 1.5e-3 on 12^3
     nsteps = max(args.steps, 1)
     for _ in range(args.warmup):
         g.rk4(qd, h, h)
@@ -525,6 +525,7 @@ def run_c3(args, rank, world):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
         "config": {"workload": C3_WORKLOAD, "elements": ms.numEl, "ndof": ms.numDof,
+                   "res_tol": "off (no per-step norm readback)",
                    "l2": "inputs (q 76 MB, metrics 137 MB) exceed the 129 MB L2",
                    "mesh_setup_s": t_mesh},
         "roofline": {"bound": "fp64", "achieved": flops / t_res / 1e12, "peak": fp64_peak,
@@ -626,11 +627,11 @@ def main():
     if args.only:
         run_kernels_only(args, args.only)
         return
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
     if args.workload == "c3" and args.impl == "ours":
         run_c3(args, rank, world)
         return
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
     dist = None
     if args.impl == "reference":
         run_reference(args, rank, world)
