@@ -319,6 +319,23 @@ typedef struct {
 int eg_rk4(eg_mesh* mesh, double* q, double h, double t_max, int32_t itermax, double res_tol,
            int32_t mem, eg_rk4_stats* stats);
 
+/* Largest mesh (unknowns) eg_rk4_static accepts. */
+#define EG_RK4_STATIC_MAX_DOF 524288
+
+/* eg_rk4 without allocation.  No reference counterpart: the reference's rk4
+   allocates its stage vectors in Julia; this entry point exists for callers
+   whose device memory is reserved up front (a process whose caching allocator
+   holds most of the HBM cannot count on a mid-run cudaMalloc, and cudaFree
+   synchronises the whole device).  Same arguments, kernels and results as
+   eg_rk4, for meshes of at most EG_RK4_STATIC_MAX_DOF unknowns (larger ones:
+   EG_ERR_INVALID); the work vectors live in one static 24 MiB device array
+   per device.  The first call on a device resolves that array's address with
+   the device current and should come before any stream capture.  Phase timers
+   must be off (EG_ERR_INVALID otherwise).  Calls that overlap in time on one
+   device race on the shared array. */
+int eg_rk4_static(eg_mesh* mesh, double* q, double h, double t_max, int32_t itermax,
+                  double res_tol, int32_t mem, eg_rk4_stats* stats);
+
 #ifdef __cplusplus
 }
 #endif

@@ -102,3 +102,10 @@ void eg_timer_free(eg_mesh* m);
 // kernels entry points used across translation units
 int eg_residual_device(eg_mesh* m, const double* q, double* res);
 int eg_check_status(eg_mesh* m);
+// phase timers enabled (they take CUDA events from a growing pool)
+bool eg_timing_on(const eg_mesh* m);
+// the RK4 stage kernels of eg_rk4 on m->stream (eg_solvers.cu)
+void eg_launch_rk4_stage(eg_mesh* m, const double* res, const double* xold, double c, double* ks,
+                         double* q);
+void eg_launch_rk4_final(eg_mesh* m, const double* k1, const double* k2, const double* k3,
+                         const double* res, double h, double* xold, double* q);

@@ -373,3 +373,17 @@ extern "C" int eg_prolong(eg_mesh* lo, const double* q_lo, eg_mesh* hi, double* 
   cudaFree(dT);
   return EG_OK;
 }
+
+// RK4 stage launches for other translation units: the kernels, grid and
+// launch counting of eg_rk4
+void eg_launch_rk4_stage(eg_mesh* m, const double* res, const double* xold, double c, double* ks,
+                         double* q) {
+  k_rk4_stage<<<grid64(m->ndof), 256, 0, m->stream>>>(res, m->Minv, xold, c, ks, q,
+                                                      (int64_t)m->E * m->Np, m->nv);
+}
+
+void eg_launch_rk4_final(eg_mesh* m, const double* k1, const double* k2, const double* k3,
+                         const double* res, double h, double* xold, double* q) {
+  k_rk4_final<<<grid64(m->ndof), 256, 0, m->stream>>>(k1, k2, k3, res, m->Minv, h, xold, q,
+                                                      (int64_t)m->E * m->Np, m->nv);
+}

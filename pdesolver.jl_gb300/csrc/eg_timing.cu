@@ -131,3 +131,5 @@ extern "C" int eg_sync(eg_mesh* m) {
   EG_CUDA(cudaStreamSynchronize(m->stream));
   return eg_check_status(m);
 }
+
+bool eg_timing_on(const eg_mesh* m) { return m->timer && m->timer->enabled; }

@@ -80,6 +80,7 @@ def _declare(lib):
     lib.eg_newton_solve.argtypes = [vp, vp, C.c_int32, C.POINTER(NewtonOpts), C.POINTER(NewtonStats)]
     lib.eg_rk4.argtypes = [vp, vp, C.c_double, C.c_double, C.c_int32, C.c_double, C.c_int32,
                            C.POINTER(Rk4Stats)]
+    lib.eg_rk4_static.argtypes = lib.eg_rk4.argtypes
 
 
 class LsStats(C.Structure):
