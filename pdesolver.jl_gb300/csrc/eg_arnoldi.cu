@@ -16,7 +16,7 @@
 //     all blocks take the same branches (no barrier can be missed);
 //   * block 0 alone writes the Hessenberg column, g and the flags that the
 //     host and the least-squares kernel read after the launch.
-// Per iteration: 3 grid barriers (5 with the second Gram-Schmidt pass).
+// Per iteration: 2 grid barriers (3 with the second Gram-Schmidt pass).
 // The operator is the right-preconditioned J M^-1 = I + C D^-1 (element blocks
 // cancel with their inverses).
 #include <cooperative_groups.h>
@@ -65,19 +65,53 @@ __device__ __forceinline__ double wsum(double v) {
   return v;
 }
 
-// partial dots of the block's rows: k < cnt against V[k], k == cnt: w.w
-// (when with_ww); warp q owns k = q, q+8, q+16, q+24, q+32
+// vector type for the streaming passes over a block's rows: 16-byte loads
+template <typename T> struct Vec;
+template <> struct Vec<float> {
+  using V = float4;
+  static constexpr int W = 4;
+  __device__ static float dot(V a, V b) { return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w; }
+  __device__ static V fma(V a, float h, V c) {
+    return make_float4(c.x - a.x * h, c.y - a.y * h, c.z - a.z * h, c.w - a.w * h);
+  }
+  __device__ static V scale(V a, float s) { return make_float4(a.x * s, a.y * s, a.z * s, a.w * s); }
+};
+template <> struct Vec<double> {
+  using V = double2;
+  static constexpr int W = 2;
+  __device__ static double dot(V a, V b) { return a.x * b.x + a.y * b.y; }
+  __device__ static V fma(V a, double h, V c) { return make_double2(c.x - a.x * h, c.y - a.y * h); }
+  __device__ static V scale(V a, double s) { return make_double2(a.x * s, a.y * s); }
+};
+
+// partial dots of the block's rows: k < cnt against V[k], k == cnt: x.x
+// (when with_xx); warp q owns k = q, q + 16, ...  Rows in units of
+// Vec<T>::W when `vec` (the row range and the vector stride are multiples of
+// W), else scalar.
 template <typename T>
-__device__ void block_dots(const T* __restrict__ V, const T* __restrict__ w, int cnt, int with_ww,
-                           int64_t N, int64_t r0, int nrow, T* __restrict__ pb) {
+__device__ void block_dots(const T* __restrict__ V, const T* __restrict__ x, int cnt, int with_xx,
+                           int64_t N, int64_t r0, int nrow, bool vec, T* __restrict__ pb) {
+  using VT = Vec<T>;
   const int lane = threadIdx.x & 31, q = threadIdx.x >> 5;
-  const int tot = cnt + (with_ww ? 1 : 0);
+  const int tot = cnt + (with_xx ? 1 : 0);
   for (int k = q; k < tot; k += NT / 32) {
-    const T* v = (k < cnt) ? V + (size_t)k * N + r0 : w + r0;
-    const T* x = w + r0;
-    T acc = T(0);
-    for (int i = lane; i < nrow; i += 32) acc += v[i] * x[i];
-    acc = wsum(acc);
+    const T* v = (k < cnt) ? V + (size_t)k * N + r0 : x + r0;
+    const T* xr = x + r0;
+    T acc0 = T(0), acc1 = T(0);
+    if (vec) {
+      const typename VT::V* v4 = reinterpret_cast<const typename VT::V*>(v);
+      const typename VT::V* x4 = reinterpret_cast<const typename VT::V*>(xr);
+      const int n4 = nrow / VT::W;
+      int i = lane;
+      for (; i + 32 < n4; i += 64) {
+        acc0 += VT::dot(v4[i], x4[i]);
+        acc1 += VT::dot(v4[i + 32], x4[i + 32]);
+      }
+      if (i < n4) acc0 += VT::dot(v4[i], x4[i]);
+    } else {
+      for (int i = lane; i < nrow; i += 32) acc0 += v[i] * xr[i];
+    }
+    const T acc = wsum(acc0 + acc1);
     if (lane == 0) pb[k] = acc;
   }
 }
@@ -94,28 +128,48 @@ __device__ void block_reduce_all(const T* __restrict__ part, int nblk, int cnt, 
   }
 }
 
-// w -= sum_k V[k] h[k] on the block's rows; returns the block's |w|^2 (thread 0)
+// y = (x - sum_{k<cnt} V[k] h[k]) * s on the block's rows, by threads
+// t0 .. NT-1 (x and y may alias)
 template <typename T>
-__device__ T block_sub_norm(const T* __restrict__ V, const T* __restrict__ h, int cnt, int64_t N,
-                            T* __restrict__ w, int64_t r0, int nrow, T* sred) {
-  T acc = T(0);
-  for (int i = threadIdx.x; i < nrow; i += NT) {
-    const int64_t row = r0 + i;
-    T a = w[row];
-    for (int k = 0; k < cnt; ++k) a -= V[(size_t)k * N + row] * h[k];
-    w[row] = a;
-    acc += a * a;
+__device__ void block_sub_scale(const T* __restrict__ V, const T* __restrict__ h, int cnt, int64_t N,
+                                const T* x, T s, T* y, int64_t r0, int nrow, bool vec, int t0) {
+  using VT = Vec<T>;
+  if (vec) {
+    const int n4 = nrow / VT::W;
+    for (int i = threadIdx.x - t0; i < n4; i += NT - t0) {
+      const int64_t row = r0 + (int64_t)i * VT::W;
+      typename VT::V a = *reinterpret_cast<const typename VT::V*>(x + row);
+      int k = 0;
+      for (; k + 4 <= cnt; k += 4) {
+        const typename VT::V v0 = *reinterpret_cast<const typename VT::V*>(V + (size_t)k * N + row);
+        const typename VT::V v1 = *reinterpret_cast<const typename VT::V*>(V + (size_t)(k + 1) * N + row);
+        const typename VT::V v2 = *reinterpret_cast<const typename VT::V*>(V + (size_t)(k + 2) * N + row);
+        const typename VT::V v3 = *reinterpret_cast<const typename VT::V*>(V + (size_t)(k + 3) * N + row);
+        a = VT::fma(v0, h[k], a);
+        a = VT::fma(v1, h[k + 1], a);
+        a = VT::fma(v2, h[k + 2], a);
+        a = VT::fma(v3, h[k + 3], a);
+      }
+      for (; k < cnt; ++k)
+        a = VT::fma(*reinterpret_cast<const typename VT::V*>(V + (size_t)k * N + row), h[k], a);
+      *reinterpret_cast<typename VT::V*>(y + row) = VT::scale(a, s);
+    }
+  } else {
+    for (int i = threadIdx.x - t0; i < nrow; i += NT - t0) {
+      const int64_t row = r0 + i;
+      T a = x[row];
+      for (int k = 0; k < cnt; ++k) a -= V[(size_t)k * N + row] * h[k];
+      y[row] = a * s;
+    }
   }
-  acc = wsum(acc);
-  if ((threadIdx.x & 31) == 0) sred[threadIdx.x >> 5] = acc;
-  __syncthreads();
-  T t = T(0);
-  if (threadIdx.x == 0)
-    for (int q = 0; q < NT / 32; ++q) t += sred[q];
-  __syncthreads();
-  return t;
 }
 
+// One Arnoldi cycle.  Gram-Schmidt: classical, with the norm of the
+// orthogonalised vector from the same reduction (|w'|^2 = w.w - |h|^2), and
+// a second classical pass (whose reduction also yields w'.w') when
+// |w'|^2 < |w|^2 / 2 (the DGKS criterion with eta = 1/sqrt 2).  The Givens
+// rotations and the least-squares right-hand side are carried in T by one
+// lane while the other warps form v_{j+1}.
 template <int DIM, int NB, typename T>
 __global__ void __launch_bounds__(NT, 2) k_arnoldi_coop(CoopArgs<T> a) {
   cg::grid_group grid = cg::this_grid();
@@ -127,14 +181,13 @@ __global__ void __launch_bounds__(NT, 2) k_arnoldi_coop(CoopArgs<T> a) {
   const int e0 = min(a.E, b * epb), e1 = min(a.E, e0 + epb);
   const int64_t r0 = (int64_t)e0 * n;
   const int nrow = (e1 - e0) * n;
-  T* P0 = a.part;                               // dots, first pass
-  T* P1 = a.part + (size_t)nblk * PSTRIDE;      // |w|^2, first pass
-  T* P2 = a.part + 2 * (size_t)nblk * PSTRIDE;  // dots, second pass
-  T* P3 = a.part + 3 * (size_t)nblk * PSTRIDE;  // |w|^2, second pass
-  __shared__ T sh1[33], sh2[33], sred[NT / 32], s_n2[1];
-  __shared__ double scs[32], ssn[32], sg[33], sHc[33];
+  const bool vec = NB > 0 ? (NB % Vec<T>::W) == 0 : (a.n % Vec<T>::W) == 0;
+  T* P0 = a.part;                               // first pass: dots and w.w
+  T* P2 = a.part + 2 * (size_t)nblk * PSTRIDE;  // second pass: dots and w'.w'
+  __shared__ T sh1[33], sh2[33];
+  __shared__ T scs[32], ssn[32], sg[33], sHc[33];
   __shared__ int s_done, s_its, s_reorth, s_jdone;
-  __shared__ T s_hn;
+  __shared__ T s_inv;
   __shared__ double s_tol;
   double* Hg = a.dH;
   double* csg = a.dH + (size_t)(m + 1) * m;
@@ -144,13 +197,14 @@ __global__ void __launch_bounds__(NT, 2) k_arnoldi_coop(CoopArgs<T> a) {
     s_done = a.flags[F_DONE];
     s_its = a.flags[F_ITS];
     s_tol = a.scal[S_TOL];
+    s_jdone = 0;
   }
-  for (int k = tid; k <= m; k += NT) sg[k] = gg[k];
-  if (tid == 0) s_jdone = 0;
+  for (int k = tid; k <= m; k += NT) sg[k] = T(gg[k]);
   __syncthreads();
   for (int j = 0; j < m; ++j) {
     if (s_done) break;
     const T* vj = a.V + (size_t)j * N;
+    T* vn = a.V + (size_t)(j + 1) * N;
     // (1) z = D^-1 v_j on the block's elements
     for (int t = tid; t < nrow; t += NT) {
       const int le = t / n, r = t - le * n;
@@ -166,70 +220,77 @@ __global__ void __launch_bounds__(NT, 2) k_arnoldi_coop(CoopArgs<T> a) {
       a.w[row] = vj[row] + coupling_row<DIM, T>(a.md, a.cpl, a.spos, a.z, e, r, n);
     }
     __syncthreads();
-    // (3) first Gram-Schmidt pass: dots with v_0..v_j and w.w
-    block_dots<T>(a.V, a.w, j + 1, 1, N, r0, nrow, P0 + (size_t)b * PSTRIDE);
+    // (3) first pass: h1 = V^T w and w.w in one reduction
+    block_dots<T>(a.V, a.w, j + 1, 1, N, r0, nrow, vec, P0 + (size_t)b * PSTRIDE);
     grid.sync();
     block_reduce_all<T>(P0, nblk, j + 2, sh1);
     __syncthreads();
-    T bn = block_sub_norm<T>(a.V, sh1, j + 1, N, a.w, r0, nrow, sred);
-    if (tid == 0) P1[b * PSTRIDE] = bn;
-    grid.sync();
-    block_reduce_all<T>(P1, nblk, 1, s_n2);
-    __syncthreads();
-    if (tid == 0) s_reorth = double(s_n2[0]) < 0.5 * double(sh1[j + 1]);
-    __syncthreads();
-    if (s_reorth) {
-      block_dots<T>(a.V, a.w, j + 1, 0, N, r0, nrow, P2 + (size_t)b * PSTRIDE);
-      grid.sync();
-      block_reduce_all<T>(P2, nblk, j + 1, sh2);
-      __syncthreads();
-      bn = block_sub_norm<T>(a.V, sh2, j + 1, N, a.w, r0, nrow, sred);
-      if (tid == 0) P3[b * PSTRIDE] = bn;
-      grid.sync();
-      block_reduce_all<T>(P3, nblk, 1, s_n2);
-    } else {
-      for (int k = tid; k <= j; k += NT) sh2[k] = T(0);
+    if (tid == 0) {
+      T hh = T(0);
+      for (int k = 0; k <= j; ++k) hh += sh1[k] * sh1[k];
+      const T ww = sh1[j + 1];
+      const T n2 = ww - hh;
+      s_reorth = n2 < T(0.5) * ww;
+      sh2[32] = n2;  // |w'|^2
     }
     __syncthreads();
-    // (4) Hessenberg column j and Givens rotation (identical in every block)
+    T n2;
+    if (s_reorth) {
+      // (4) second pass on w' = w - V h1: h2 = V^T w' and w'.w' in one reduction
+      block_sub_scale<T>(a.V, sh1, j + 1, N, a.w, T(1), a.w, r0, nrow, vec, 0);
+      __syncthreads();
+      block_dots<T>(a.V, a.w, j + 1, 1, N, r0, nrow, vec, P2 + (size_t)b * PSTRIDE);
+      grid.sync();
+      block_reduce_all<T>(P2, nblk, j + 2, sh2);
+      __syncthreads();
+      if (tid == 0) {
+        T hh = T(0);
+        for (int k = 0; k <= j; ++k) hh += sh2[k] * sh2[k];
+        const T r = sh2[j + 1] - hh;
+        sh2[32] = r > T(0) ? r : T(0);
+      }
+      __syncthreads();
+      n2 = sh2[32];
+    } else {
+      n2 = sh2[32];
+    }
+    const T hn = sqrt(n2);
+    const T inv = hn > T(0) ? T(1) / hn : T(0);
+    // (5) lane 0 of warp 0: Hessenberg column j and its Givens rotation
+    //     (identical in every block); warps 1.. : v_{j+1} = (w - V h) / hn
     if (tid == 0) {
-      const double hn = sqrt(double(s_n2[0]));
-      for (int k = 0; k <= j; ++k) sHc[k] = double(sh1[k]) + double(sh2[k]);
+      for (int k = 0; k <= j; ++k) sHc[k] = s_reorth ? sh1[k] + sh2[k] : sh1[k];
       sHc[j + 1] = hn;
       for (int k = 0; k < j; ++k) {
-        const double t0 = scs[k] * sHc[k] + ssn[k] * sHc[k + 1];
+        const T t0 = scs[k] * sHc[k] + ssn[k] * sHc[k + 1];
         sHc[k + 1] = -ssn[k] * sHc[k] + scs[k] * sHc[k + 1];
         sHc[k] = t0;
       }
-      const double den = hypot(sHc[j], sHc[j + 1]);
+      const T den = hypot(sHc[j], sHc[j + 1]);
       s_its += 1;
-      s_hn = T(hn);
-      if (!(den > 0.0) || !isfinite(den)) {
+      if (!(den > T(0)) || !isfinite(den)) {
         s_done = 1;  // breakdown: keep the j columns built so far
       } else {
         scs[j] = sHc[j] / den;
         ssn[j] = sHc[j + 1] / den;
         sHc[j] = den;
-        sHc[j + 1] = 0.0;
+        sHc[j + 1] = T(0);
         sg[j + 1] = -ssn[j] * sg[j];
         sg[j] = scs[j] * sg[j];
         s_jdone = j + 1;
-        const double resid = fabs(sg[j + 1]);
-        if (resid <= s_tol || hn == 0.0 || s_its >= a.flags[F_ITERMAX]) s_done = 1;
+        const double resid = fabs(double(sg[j + 1]));
+        if (resid <= s_tol || hn == T(0) || s_its >= a.flags[F_ITERMAX]) s_done = 1;
       }
       if (b == 0) {
         double* Hc = Hg + (size_t)j * (m + 1);
-        for (int k = 0; k <= j + 1; ++k) Hc[k] = sHc[k];
-        a.scal[S_RESID] = fabs(sg[j + 1]);
+        for (int k = 0; k <= j + 1; ++k) Hc[k] = double(sHc[k]);
+        a.scal[S_RESID] = fabs(double(sg[j + 1]));
       }
-    }
-    __syncthreads();
-    // (5) v_{j+1} = w / |w| on the block's rows
-    {
-      const T hn = s_hn;
-      const T inv = hn > T(0) ? T(1) / hn : T(0);
-      T* vn = a.V + (size_t)(j + 1) * N;
-      for (int i = tid; i < nrow; i += NT) vn[r0 + i] = a.w[r0 + i] * inv;
+    } else if (tid >= 32) {
+      if (s_reorth)
+        block_sub_scale<T>(a.V, sh2, j + 1, N, a.w, inv, vn, r0, nrow, vec, 32);
+      else
+        block_sub_scale<T>(a.V, sh1, j + 1, N, a.w, inv, vn, r0, nrow, vec, 32);
     }
     __syncthreads();
   }
@@ -237,10 +298,10 @@ __global__ void __launch_bounds__(NT, 2) k_arnoldi_coop(CoopArgs<T> a) {
     a.flags[F_ITS] = s_its;
     a.flags[F_JDONE] = s_jdone;
     a.flags[F_DONE] = s_done;
-    for (int k = 0; k <= m; ++k) gg[k] = sg[k];
+    for (int k = 0; k <= m; ++k) gg[k] = double(sg[k]);
     for (int k = 0; k < m; ++k) {
-      csg[k] = scs[k];
-      sng[k] = ssn[k];
+      csg[k] = double(scs[k]);
+      sng[k] = double(ssn[k]);
     }
   }
 }

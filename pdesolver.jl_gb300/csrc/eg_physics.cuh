@@ -315,19 +315,22 @@ __device__ __forceinline__ IRNode<DIM> ir_node(const Gas& g, const double* q) {
   return r;
 }
 
-// logarithmic mean from the values and their logarithms:
-// (aL - aR) / (ln aL - ln aR), or the reference's 5-term series in
-// u = ((aL - aR)/(aL + aR))^2 below 1e-3 (algebraically the reference's
-// logavg, bc_solvers.jl:942-956, with 2 divisions instead of 4 and no log)
-__device__ __forceinline__ double logavg_pre(double aL, double aR, double lL, double lR) {
-  const double s = aL + aR;
-  const double f = (aL - aR) / s;
-  const double u = f * f;
-  if (u < 1e-3) {
-    const double F = 1.0 + u * (1.0 / 3.0 + u * (1.0 / 5.0 + u * (1.0 / 7.0 + u * (1.0 / 9.0))));
-    return s / (2.0 * F);
-  }
-  return (aL - aR) / (lL - lR);
+// Logarithmic means for the Ismail-Roe average from precomputed logarithms.
+// The reference's logavg (bc_solvers.jl:942-956) is (aL + aR) / (2 F) with
+// u = f^2, f = (aL - aR)/(aL + aR), and F = 1 + u/3 + u^2/5 + u^3/7 + u^4/9
+// for u < 1e-3, else F = ln(aL/aR) / (2 f).  The average needs the log mean of
+// sqrt(rho p) (L_p), its reciprocal, and the reciprocal of the log mean of
+// sqrt(rho/p) (1/L_1); all three follow from 1/(aL + aR) and F:
+//   L = s/(2F) = (s/2) G(u),  1/L = 2 F / s,
+// with G = 1/F as its series 1 - u/3 - 4u^2/45 - 44u^3/945 - 428u^4/14175
+// (|G F - 1| < 5e-16 for u < 1e-3), and in the logarithmic branch
+//   1/L = (lL - lR)/d,  L = d^2 x and 1/L = (lL - lR)^2 x with x = 1/(d (lL - lR)).
+// A pair then costs two divisions on the series branch (1/s_1, 1/s_p).
+__device__ __forceinline__ double logmean_F(double u) {
+  return 1.0 + u * (1.0 / 3.0 + u * (1.0 / 5.0 + u * (1.0 / 7.0 + u * (1.0 / 9.0))));
+}
+__device__ __forceinline__ double logmean_G(double u) {
+  return 1.0 - u * (1.0 / 3.0 + u * (4.0 / 45.0 + u * (44.0 / 945.0 + u * (428.0 / 14175.0))));
 }
 
 // Ismail-Roe averages of two nodes from their precomputed quantities
@@ -336,17 +339,38 @@ __device__ __forceinline__ IRAvg<DIM, double> ir_average_pre(const Gas& g, const
                                                              const IRNode<DIM>& R) {
   const double gamma = g.gamma, gamma_1 = g.gamma_1;
   IRAvg<DIM, double> r;
-  const double zs = L.z1 + R.z1;
-  const double iz = 1.0 / zs;
-  const double lp = logavg_pre(L.zp, R.zp, L.lzp, R.lzp);
-  r.rho_hat = 0.5 * zs * lp;
-  r.u_hat = (L.z1 * L.u + R.z1 * R.u) * iz;
-  r.v_hat = (L.z1 * L.v + R.z1 * R.v) * iz;
-  r.w_hat = (DIM == 3) ? (L.z1 * L.w + R.z1 * R.w) * iz : 0.0;
-  r.p1_hat = (L.zp + R.zp) * iz;
-  const double p2_hat = ((gamma + 1) / (2 * gamma)) * lp / logavg_pre(L.z1, R.z1, L.lz1, R.lz1) +
-                        (gamma_1 / (2 * gamma)) * r.p1_hat;
-  r.h_hat = gamma * p2_hat / (r.rho_hat * gamma_1) +
+  // sqrt(rho/p): r1 = 1/(z1L + z1R) is also the weight of the velocity averages
+  const double s1 = L.z1 + R.z1, d1 = L.z1 - R.z1;
+  const double r1 = 1.0 / s1;
+  double inv_l1;
+  if (d1 * d1 < 1e-3 * (s1 * s1)) {
+    const double f = d1 * r1;
+    inv_l1 = 2.0 * logmean_F(f * f) * r1;
+  } else {
+    inv_l1 = (L.lz1 - R.lz1) / d1;
+  }
+  // sqrt(rho p)
+  const double sp = L.zp + R.zp, dp = L.zp - R.zp;
+  double lp, inv_lp;
+  if (dp * dp < 1e-3 * (sp * sp)) {
+    const double rp = 1.0 / sp;
+    const double f = dp * rp, u = f * f;
+    lp = 0.5 * sp * logmean_G(u);
+    inv_lp = 2.0 * logmean_F(u) * rp;
+  } else {
+    const double dl = L.lzp - R.lzp;
+    const double x = 1.0 / (dp * dl);
+    lp = dp * dp * x;
+    inv_lp = dl * dl * x;
+  }
+  r.rho_hat = 0.5 * s1 * lp;
+  r.u_hat = (L.z1 * L.u + R.z1 * R.u) * r1;
+  r.v_hat = (L.z1 * L.v + R.z1 * R.v) * r1;
+  r.w_hat = (DIM == 3) ? (L.z1 * L.w + R.z1 * R.w) * r1 : 0.0;
+  r.p1_hat = sp * r1;
+  const double p2_hat = ((gamma + 1) / (2 * gamma)) * lp * inv_l1 + (gamma_1 / (2 * gamma)) * r.p1_hat;
+  // h = gamma p2 / (rho_hat (gamma - 1)) + |u|^2/2, 1/rho_hat = 2 r1 / L_p
+  r.h_hat = (gamma / gamma_1) * p2_hat * (2.0 * r1 * inv_lp) +
             0.5 * (r.u_hat * r.u_hat + r.v_hat * r.v_hat + r.w_hat * r.w_hat);
   return r;
 }
