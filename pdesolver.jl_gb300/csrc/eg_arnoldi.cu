@@ -34,7 +34,8 @@ namespace {
 
 enum { F_DONE = 0, F_JDONE = 1, F_ITS = 2, F_CONV = 3, F_ITERMAX = 4, F_REORTH = 5 };
 enum { S_TOL = 0, S_RESID = 1, S_BETA = 2, S_BNORM = 3 };
-constexpr int NT = 512;
+constexpr int NT = 1024;  // one block per SM
+constexpr int NB_MAX = 64;  // coupling-block rows handled by the face-side pass
 constexpr int PSTRIDE = 33;  // partial slots per block
 
 template <typename T>
@@ -43,6 +44,8 @@ struct CoopArgs {
   const T* inv;      // [E][n][n] block inverses (column-major)
   const T* cpl;      // [I][2][nb][nb] coupling blocks (row-major)
   const int* spos;   // [F][Np]
+  const int* fside;  // [E][F] coupling block of each element face, or -1
+  T* cfs;            // [I][2][nb] coupling products of each face side
   T* V;              // [(m+1)][N]
   T* w;              // [N]
   T* z;              // [N]
@@ -51,8 +54,62 @@ struct CoopArgs {
   int* flags;
   double* scal;
   int m, n, E;
+  int nb, S, F, nv, ec;  // coupling block size, stencil size, faces, variables, elements per chunk
   int64_t N;
 };
+
+// NV consecutive values of a coupling row (16-byte loads for 2-D FP32)
+template <int NV, typename T>
+__device__ __forceinline__ void load_row_piece(const T* __restrict__ p, T* out) {
+  if constexpr (NV == 4 && sizeof(T) == 4) {
+    const float4 v = *reinterpret_cast<const float4*>(p);
+    out[0] = v.x; out[1] = v.y; out[2] = v.z; out[3] = v.w;
+  } else {
+#pragma unroll
+    for (int b = 0; b < NV; ++b) out[b] = p[b];
+  }
+}
+
+// Push of the coupling of elements c0 .. c0+nl-1 to their neighbours: for
+// each interface face f of element e with coupling block fs = slot*2 + side,
+// the neighbour's block fs ^ 1 (rows: the neighbour's stencil, columns: e's
+// stencil on f) times e's values z_e (shared memory) goes to cfs[fs ^ 1].
+// A group of G lanes (16 when nb <= 16, else 32) owns one face; lane gl
+// streams rows gl, gl + G, ... of the row-major block.
+template <int DIM, typename T>
+__device__ void face_push(const CoopArgs<T>& a, const T* __restrict__ sZ, const int* __restrict__ sPerm,
+                          int c0, int nl, T* __restrict__ cfs) {
+  constexpr int NV = DIM + 2;
+  const int nb = a.nb, F = a.F, S = a.S, n = a.n;
+  const int G = nb <= 16 ? 16 : 32, gpw = 32 / G;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int grp = lane / G, gl = lane - grp * G;
+  const int ntask = nl * F;
+  for (int t = warp * gpw + grp; t < ntask; t += (NT / 32) * gpw) {
+    const int le = t / F, f = t - le * F;
+    const int fs = a.fside[(int64_t)(c0 + le) * F + f];
+    if (fs < 0) continue;
+    const int tgt = fs ^ 1;
+    const T* zs = sZ + (size_t)le * n;
+    const int* pf = sPerm + f * S;
+    for (int i = gl; i < nb; i += G) {
+      const T* Cr = a.cpl + ((size_t)tgt * nb + i) * nb;
+      T acc0 = T(0), acc1 = T(0);
+#pragma unroll 4
+      for (int sp = 0; sp < S; ++sp) {
+        T c[NV];
+        load_row_piece<NV, T>(Cr + sp * NV, c);
+        const T* zz = zs + pf[sp] * NV;
+#pragma unroll
+        for (int b = 0; b < NV; ++b) {
+          if (b & 1) acc1 += c[b] * zz[b];
+          else acc0 += c[b] * zz[b];
+        }
+      }
+      cfs[(size_t)tgt * nb + i] = acc0 + acc1;
+    }
+  }
+}
 
 __device__ __forceinline__ float wsum(float v) {
 #pragma unroll
@@ -171,7 +228,7 @@ __device__ void block_sub_scale(const T* __restrict__ V, const T* __restrict__ h
 // rotations and the least-squares right-hand side are carried in T by one
 // lane while the other warps form v_{j+1}.
 template <int DIM, int NB, typename T>
-__global__ void __launch_bounds__(NT, 2) k_arnoldi_coop(CoopArgs<T> a) {
+__global__ void __launch_bounds__(NT, 1) k_arnoldi_coop(CoopArgs<T> a) {
   cg::grid_group grid = cg::this_grid();
   const int nblk = gridDim.x, b = blockIdx.x, tid = threadIdx.x;
   const int n = NB > 0 ? NB : a.n, m = a.m;
@@ -184,6 +241,9 @@ __global__ void __launch_bounds__(NT, 2) k_arnoldi_coop(CoopArgs<T> a) {
   const bool vec = NB > 0 ? (NB % Vec<T>::W) == 0 : (a.n % Vec<T>::W) == 0;
   T* P0 = a.part;                               // first pass: dots and w.w
   T* P2 = a.part + 2 * (size_t)nblk * PSTRIDE;  // second pass: dots and w'.w'
+  extern __shared__ __align__(16) unsigned char dsmem[];
+  T* sZ = reinterpret_cast<T*>(dsmem);  // [ec][n] D^-1 v_j of a chunk of the block's elements
+  __shared__ int sPerm[64], sSpos[128];
   __shared__ T sh1[33], sh2[33];
   __shared__ T scs[32], ssn[32], sg[33], sHc[33];
   __shared__ int s_done, s_its, s_reorth, s_jdone;
@@ -200,24 +260,45 @@ __global__ void __launch_bounds__(NT, 2) k_arnoldi_coop(CoopArgs<T> a) {
     s_jdone = 0;
   }
   for (int k = tid; k <= m; k += NT) sg[k] = T(gg[k]);
+  for (int k = tid; k < a.F * a.S; k += NT) sPerm[k] = a.md.perm[k];
+  for (int k = tid; k < a.F * a.md.Np; k += NT) sSpos[k] = a.spos[k];
   __syncthreads();
   for (int j = 0; j < m; ++j) {
     if (s_done) break;
     const T* vj = a.V + (size_t)j * N;
     T* vn = a.V + (size_t)(j + 1) * N;
-    // (1) z = D^-1 v_j on the block's elements
-    for (int t = tid; t < nrow; t += NT) {
-      const int le = t / n, r = t - le * n;
-      const int e = e0 + le;
-      a.z[(size_t)e * n + r] = block_row<NB, T>(a.inv + (size_t)e * n * n, vj + (size_t)e * n, r, n);
+    // (1) per chunk of the block's elements: z = D^-1 v_j into shared
+    //     memory, then the push of C z to the neighbours' face sides
+    for (int c0 = e0; c0 < e1; c0 += a.ec) {
+      const int nl = min(a.ec, e1 - c0);
+      for (int t = tid; t < nl * n; t += NT) {
+        const int le = t / n, r = t - le * n;
+        const int e = c0 + le;
+        sZ[t] = block_row<NB, T>(a.inv + (size_t)e * n * n, vj + (size_t)e * n, r, n);
+      }
+      __syncthreads();
+      face_push<DIM, T>(a, sZ, sPerm, c0, nl, a.cfs);
+      __syncthreads();
     }
     grid.sync();
-    // (2) w = v_j + C z on the block's rows
-    for (int t = tid; t < nrow; t += NT) {
-      const int le = t / n, r = t - le * n;
-      const int e = e0 + le;
-      const int64_t row = (int64_t)e * n + r;
-      a.w[row] = vj[row] + coupling_row<DIM, T>(a.md, a.cpl, a.spos, a.z, e, r, n);
+    // (2) w = v_j + sum over the faces whose stencil holds the row's node of
+    //     the pushed product (own rows)
+    {
+      constexpr int NV = DIM + 2;
+      for (int t = tid; t < nrow; t += NT) {
+        const int le = t / n, r = t - le * n;
+        const int j = r / NV, av = r - j * NV;
+        const int e = e0 + le;
+        const int64_t row = (int64_t)e * n + r;
+        T acc = vj[row];
+        for (int f = 0; f < a.F; ++f) {
+          const int sp = sSpos[f * a.md.Np + j];
+          if (sp < 0) continue;
+          const int fs = a.fside[(int64_t)e * a.F + f];
+          if (fs >= 0) acc += a.cfs[(size_t)fs * a.nb + sp * NV + av];
+        }
+        a.w[row] = acc;
+      }
     }
     __syncthreads();
     // (3) first pass: h1 = V^T w and w.w in one reduction
@@ -314,6 +395,12 @@ int launch_T(eg_ls* ls, int* max_blocks_cache) {
   a.inv = (const T*)ls->pc->inv;
   a.cpl = (const T*)ls->lo->cpl;
   a.spos = ls->lo->spos;
+  a.fside = ls->lo->fside;
+  a.cfs = (T*)ls->cfs;
+  a.nb = ls->lo->nb;
+  a.S = m->S;
+  a.F = m->F;
+  a.nv = m->nv;
   a.V = (T*)ls->V;
   a.w = (T*)ls->w;
   a.z = (T*)ls->z;
@@ -336,17 +423,26 @@ int launch_T(eg_ls* ls, int* max_blocks_cache) {
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, NT, 0);
   (void)max_blocks_cache;
-  int nblk = sms * (per_sm < 2 ? per_sm : 2);
+  // elements per block, and per shared-memory chunk of D^-1 v values
+  const size_t side_bytes = (size_t)a.n * sizeof(T);
+  int nblk = sms;
   if (nblk > m->E) nblk = m->E;
   if (nblk > EG_COOP_MAX_BLOCKS) nblk = EG_COOP_MAX_BLOCKS;
+  const int epb = (m->E + nblk - 1) / nblk;
+  int ec = (int)((40 * 1024) / side_bytes);
+  if (ec < 1) ec = 1;
+  if (ec > epb) ec = epb;
+  a.ec = ec;
+  const size_t smem = (size_t)ec * side_bytes;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, NT, smem);
+  if (per_sm < 1) nblk = 0;
   if (nblk <= 0) {
     eg_set_error("persistent Arnoldi kernel cannot be resident");
     return EG_ERR_UNSUPPORTED;
   }
   void* args[] = {&a};
-  EG_CUDA(cudaLaunchCooperativeKernel(fn, dim3(nblk), dim3(NT), args, 0, m->stream));
+  EG_CUDA(cudaLaunchCooperativeKernel(fn, dim3(nblk), dim3(NT), args, smem, m->stream));
   m->launches += 1;
   return EG_OK;
 }
@@ -359,6 +455,12 @@ int launch_T(eg_ls* ls, int* max_blocks_cache) {
 int eg_arnoldi_coop(eg_ls* ls) {
   static int cache_f = 0, cache_d = 0;
   return ls->lo->prec == EG_F64 ? launch_T<double>(ls, &cache_d) : launch_T<float>(ls, &cache_f);
+}
+
+bool eg_coop_usable(const eg_ls* ls) {
+  const eg_mesh* m = ls->lo->mesh;
+  return ls->lo->nb <= NB_MAX && m->F * m->S <= 64 && m->F * m->Np <= 128 && m->I > 0 &&
+         eg_coop_supported();
 }
 
 bool eg_coop_supported() {

@@ -614,7 +614,7 @@ int gmres_T(eg_ls* ls, eg_ls_stats* st) {
   int fl[8] = {0, 0, 0, 0, ls->itermax, 0, 0, 0};
   EG_CUDA(cudaMemcpyAsync(ls->dscal, sc, sizeof(sc), cudaMemcpyHostToDevice, m->stream));
   EG_CUDA(cudaMemcpyAsync(ls->dflags, fl, sizeof(fl), cudaMemcpyHostToDevice, m->stream));
-  const bool coop = eg_coop_supported() && !m->capturing;
+  const bool coop = eg_coop_usable(ls) && !m->capturing;
   if (!coop && !ls->g_init && !ls->g_cycle && !ls->graphs_ok) {
     cudaGraphExec_t gi = nullptr, gc = nullptr;
     bool ok = capture(m, [&]() { enqueue_init<T>(ls, 1); }, &gi, &ls->g_init_nodes);

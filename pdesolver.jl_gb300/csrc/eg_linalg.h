@@ -12,6 +12,7 @@ struct eg_lo {
   void* cpl;       // [I][2][nb][nb] column-major coupling blocks
   void* dF;        // [(I+B)][Nf][2][nv][nv] point flux Jacobians
   int32_t* spos;   // [F][Np]: stencil position of node j on face f, or -1
+  int32_t* fside;  // [E][F]: coupling block (slot * 2 + side) of face f of e, or -1
   void* xT;        // [ndof] operand in the operator precision
   void* yT;        // [ndof]
   double* xd;      // [ndof] FP64 staging
@@ -34,6 +35,7 @@ struct eg_ls {
   void* V;         // [(m+1)][ndof]
   void* w;         // [ndof]
   void* z;         // [ndof]
+  void* cfs;       // [I][2][nb] coupling products of each face side (persistent Arnoldi)
   void* xT;        // [ndof]
   void* bT;        // [ndof]
   void* part;      // [nblk][m+2] partial sums (operator precision)
@@ -57,6 +59,9 @@ void eg_gmres_release(eg_ls* ls);
 #define EG_COOP_MAX_BLOCKS 1024
 int eg_arnoldi_coop(eg_ls* ls);
 bool eg_coop_supported();
+// the persistent kernel handles this system (device support, coupling blocks
+// of at most 64 rows, small face tables)
+bool eg_coop_usable(const eg_ls* ls);
 
 // kernels shared across translation units
 int eg_jacobian_launch(eg_lo* lo, const double* q);

@@ -387,7 +387,7 @@ int eg_pc_apply_T(eg_pc* pc, const void* x, void* y, const int* done) {
 
 static void lo_free(eg_lo* lo) {
   if (!lo) return;
-  void* bufs[] = {lo->diag, lo->cpl, lo->dF, lo->spos, lo->xT, lo->yT, lo->xd, lo->yd};
+  void* bufs[] = {lo->diag, lo->cpl, lo->dF, lo->spos, lo->fside, lo->xT, lo->yT, lo->xd, lo->yd};
   for (void* b : bufs)
     if (b) cudaFree(b);
   delete lo;
@@ -425,6 +425,17 @@ extern "C" int eg_lo_create(eg_mesh* m, int32_t precision, eg_lo** out) {
   for (int f = 0; f < m->F; ++f)
     for (int s = 0; s < m->S; ++s) spos[(size_t)f * m->Np + perm[(size_t)f * m->S + s]] = s;
   e = cudaMemcpy(lo->spos, spos.data(), sizeof(int32_t) * spos.size(), cudaMemcpyHostToDevice);
+  // coupling block (slot * 2 + side) of every element face, -1 on boundaries
+  if (e == cudaSuccess) {
+    std::vector<EFace> ef((size_t)m->E * m->F);
+    e = cudaMemcpy(ef.data(), m->eface, sizeof(EFace) * ef.size(), cudaMemcpyDeviceToHost);
+    std::vector<int32_t> fside(ef.size(), -1);
+    for (size_t t = 0; t < ef.size(); ++t)
+      if (ef[t].slot >= 0 && ef[t].slot < m->I) fside[t] = ef[t].slot * 2 + ef[t].side;
+    if (e == cudaSuccess) e = cudaMalloc((void**)&lo->fside, sizeof(int32_t) * fside.size());
+    if (e == cudaSuccess)
+      e = cudaMemcpy(lo->fside, fside.data(), sizeof(int32_t) * fside.size(), cudaMemcpyHostToDevice);
+  }
   if (e != cudaSuccess) {
     lo_free(lo);
     return eg_cuda_fail(e, "eg_lo_create");
@@ -587,7 +598,7 @@ static void ls_free(eg_ls* ls) {
   if (!ls) return;
   eg_gmres_release(ls);
   void* bufs[] = {ls->V, ls->w, ls->z, ls->xT, ls->bT, ls->part, ls->h, ls->y, ls->xd, ls->bd,
-                  ls->dH, ls->dflags, ls->dscal};
+                  ls->dH, ls->dflags, ls->dscal, ls->cfs};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (ls->hh) cudaFreeHost(ls->hh);
@@ -614,6 +625,8 @@ extern "C" int eg_ls_create(eg_lo* lo, eg_pc* pc, int32_t restart, eg_ls** out) 
   cudaError_t e = cudaMalloc(&ls->V, es * (size_t)(restart + 1) * N);
   if (e == cudaSuccess) e = cudaMalloc(&ls->w, es * N);
   if (e == cudaSuccess) e = cudaMalloc(&ls->z, es * N);
+  if (e == cudaSuccess && lo->mesh->I)
+    e = cudaMalloc(&ls->cfs, es * (size_t)lo->mesh->I * 2 * lo->nb);
   if (e == cudaSuccess) e = cudaMalloc(&ls->xT, es * N);
   if (e == cudaSuccess) e = cudaMalloc(&ls->bT, es * N);
   {
