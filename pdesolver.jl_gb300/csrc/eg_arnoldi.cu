@@ -1,22 +1,27 @@
-// eg_arnoldi.cu -- one GMRES restart cycle (the Arnoldi loop) as a single
-// persistent cooperative kernel.
+// eg_arnoldi.cu -- the restarted GMRES solve of a Newton system as one
+// persistent cooperative kernel (all restart cycles, one launch).
 //
 // The Krylov vectors of the Newton systems are small (1.5 MB in FP32 for the
-// 8192-triangle p=3 problem), so an Arnoldi step is dominated by
-// synchronisation, not by HBM traffic.  One launch per cycle replaces the ~13
-// launches per iteration of the stream version:
+// 8192-triangle p=3 problem), so an Arnoldi step is bound by synchronisation
+// and by streaming the operator (D^-1 and the coupling blocks), not by the
+// vector work.  One launch per solve replaces ~13 launches per iteration and
+// a host round trip per restart:
 //   * block b owns a contiguous range of elements (and their rows) for the
-//     whole cycle, so the block-Jacobi apply, the coupling apply, the
-//     Gram-Schmidt updates and the scaling of the new basis vector touch only
-//     its own rows; a grid barrier is needed only where data crosses blocks
-//     (neighbour values of z = D^-1 v, and the dot-product partials);
+//     whole solve, so the block-Jacobi apply, the Gram-Schmidt updates, the
+//     scaling of the new basis vector and the solution update touch only its
+//     own rows;
+//   * the face coupling is pushed: the owner of element e computes, for each
+//     interface face, the neighbour's coupling block times e's values (held
+//     in shared memory) into a face-side buffer, read after one grid barrier
+//     by the neighbour's owner; a grid barrier is otherwise needed only for
+//     the dot-product partials;
 //   * every block reduces the dot-product partials in the same order, so the
-//     Hessenberg column, the re-orthogonalisation test (DGKS) and the Givens
-//     rotation are bit-identical in every block: no broadcast is needed and
-//     all blocks take the same branches (no barrier can be missed);
-//   * block 0 alone writes the Hessenberg column, g and the flags that the
-//     host and the least-squares kernel read after the launch.
-// Per iteration: 2 grid barriers (3 with the second Gram-Schmidt pass).
+//     Hessenberg column, the re-orthogonalisation test (DGKS), the Givens
+//     rotation and the convergence decision are bit-identical in every block:
+//     no broadcast is needed and all blocks take the same branches (no
+//     barrier can be missed).
+// Per Arnoldi iteration: 2 grid barriers (3 with the second Gram-Schmidt
+// pass); per restart: 2 more (residual push, residual norm).
 // The operator is the right-preconditioned J M^-1 = I + C D^-1 (element blocks
 // cancel with their inverses).
 #include <cooperative_groups.h>
@@ -32,8 +37,8 @@ namespace cg = cooperative_groups;
 
 namespace {
 
-enum { F_DONE = 0, F_JDONE = 1, F_ITS = 2, F_CONV = 3, F_ITERMAX = 4, F_REORTH = 5 };
-enum { S_TOL = 0, S_RESID = 1, S_BETA = 2, S_BNORM = 3 };
+enum { F_DONE = 0, F_JDONE = 1, F_ITS = 2, F_CONV = 3, F_ITERMAX = 4, F_REORTH = 5, F_CYCLES = 6 };
+enum { S_TOL = 0, S_RESID = 1, S_BETA = 2, S_BNORM = 3, S_RELTOL = 4, S_ABSTOL = 5, S_BETA0 = 6 };
 constexpr int NT = 1024;  // one block per SM
 constexpr int NB_MAX = 64;  // coupling-block rows handled by the face-side pass
 constexpr int PSTRIDE = 33;  // partial slots per block
@@ -42,15 +47,16 @@ template <typename T>
 struct CoopArgs {
   DevMesh md;
   const T* inv;      // [E][n][n] block inverses (column-major)
+  const T* diag;     // [E][n][n] element blocks of J (column-major)
   const T* cpl;      // [I][2][nb][nb] coupling blocks (row-major)
   const int* spos;   // [F][Np]
   const int* fside;  // [E][F] coupling block of each element face, or -1
   T* cfs;            // [I][2][nb] coupling products of each face side
+  const T* bvec;     // [N] right-hand side
+  T* x;              // [N] solution (in: initial guess)
   T* V;              // [(m+1)][N]
   T* w;              // [N]
-  T* z;              // [N]
   T* part;           // [4][gridDim][PSTRIDE]
-  double* dH;        // H | cs | sn | g | y
   int* flags;
   double* scal;
   int m, n, E;
@@ -221,19 +227,81 @@ __device__ void block_sub_scale(const T* __restrict__ V, const T* __restrict__ h
   }
 }
 
-// One Arnoldi cycle.  Gram-Schmidt: classical, with the norm of the
-// orthogonalised vector from the same reduction (|w'|^2 = w.w - |h|^2), and
-// a second classical pass (whose reduction also yields w'.w') when
-// |w'|^2 < |w|^2 / 2 (the DGKS criterion with eta = 1/sqrt 2).  The Givens
-// rotations and the least-squares right-hand side are carried in T by one
-// lane while the other warps form v_{j+1}.
+// u = sum_{k<cnt} V[k] y[k] on the block's rows
+template <typename T>
+__device__ void block_lincomb(const T* __restrict__ V, const T* __restrict__ y, int cnt, int64_t N,
+                              T* __restrict__ u, int64_t r0, int nrow) {
+  for (int i = threadIdx.x; i < nrow; i += NT) {
+    const int64_t row = r0 + i;
+    T a0 = T(0), a1 = T(0);
+    int k = 0;
+    for (; k + 2 <= cnt; k += 2) {
+      a0 += V[(size_t)k * N + row] * y[k];
+      a1 += V[(size_t)(k + 1) * N + row] * y[k + 1];
+    }
+    if (k < cnt) a0 += V[(size_t)k * N + row] * y[k];
+    u[row] = a0 + a1;
+  }
+}
+
+// Element block times a vector held per element (z_e = A_e x_e) for a chunk
+// of the block's elements, the elements' own values staged in shared memory,
+// followed by the push of the face couplings C x_e to the neighbours'
+// face sides (cfs).  Rows of A x go to out (own rows).
 template <int DIM, int NB, typename T>
-__global__ void __launch_bounds__(NT, 1) k_arnoldi_coop(CoopArgs<T> a) {
+__device__ void chunk_apply_push(const CoopArgs<T>& a, const T* __restrict__ A, const T* __restrict__ x,
+                                 bool stage_product, T* __restrict__ sZ, const int* __restrict__ sPerm,
+                                 int c0, int nl, T* __restrict__ out) {
+  const int n = NB > 0 ? NB : a.n;
+  if (stage_product) {
+    // sZ = A x (the coupling acts on the product): z = D^-1 v
+    for (int t = threadIdx.x; t < nl * n; t += NT) {
+      const int le = t / n, r = t - le * n;
+      const int e = c0 + le;
+      sZ[t] = block_row<NB, T>(A + (size_t)e * n * n, x + (size_t)e * n, r, n);
+    }
+    __syncthreads();
+  } else {
+    // sZ = x (the coupling acts on x), out = A x: D x for the residual
+    for (int t = threadIdx.x; t < nl * n; t += NT) sZ[t] = x[(size_t)c0 * n + t];
+    __syncthreads();
+    for (int t = threadIdx.x; t < nl * n; t += NT) {
+      const int le = t / n, r = t - le * n;
+      const int e = c0 + le;
+      out[(size_t)e * n + r] = block_row<NB, T>(A + (size_t)e * n * n, sZ + (size_t)le * n, r, n);
+    }
+  }
+  face_push<DIM, T>(a, sZ, sPerm, c0, nl, a.cfs);
+  __syncthreads();
+}
+
+// The whole right-preconditioned GMRES(m) solve of J x = b as one persistent
+// cooperative kernel (reference: the restarted GMRES behind linearSolve,
+// ls_standard.jl:321-371, with the element block-Jacobi preconditioner of
+// NewtonBDiagPC, preconditioning.jl:7-139).
+//   * cycle start: r = b - J x (element blocks D and the face push), beta =
+//     |r|, converged when beta <= max(reltol |b|, abstol) (the true residual),
+//     v_0 = r / beta;
+//   * Arnoldi on J M^-1 = I + C D^-1: classical Gram-Schmidt with the norm of
+//     the orthogonalised vector from the same reduction (|w'|^2 = w.w -
+//     |h|^2) and a second classical pass (its reduction also yields w'.w')
+//     when |w'|^2 < |w|^2 / 2 (DGKS with eta = 1/sqrt 2); Givens rotations in
+//     T by one lane while the other warps form v_{j+1};
+//   * cycle end: y = R^-1 g (FP64 back substitution, one warp), x += D^-1 V y
+//     on the block's own rows.
+// Block b owns a contiguous element range (and its rows) for the whole
+// solve; grid barriers separate the phases whose data crosses blocks (the
+// pushed face products, the dot-product partials).  Every block reduces the
+// partials in the same order, so the scalars (Hessenberg entries, rotations,
+// the reorthogonalisation test, the convergence decision) are bit-identical
+// in every block and all blocks take the same branches.
+template <int DIM, int NB, typename T>
+__global__ void __launch_bounds__(NT, 1) k_gmres_coop(CoopArgs<T> a) {
   cg::grid_group grid = cg::this_grid();
+  constexpr int NV = DIM + 2;
   const int nblk = gridDim.x, b = blockIdx.x, tid = threadIdx.x;
-  const int n = NB > 0 ? NB : a.n, m = a.m;
+  const int n = NB > 0 ? NB : a.n, m = a.m, M1 = a.m + 1;
   const int64_t N = a.N;
-  // contiguous element range of this block
   const int epb = (a.E + nblk - 1) / nblk;
   const int e0 = min(a.E, b * epb), e1 = min(a.E, e0 + epb);
   const int64_t r0 = (int64_t)e0 * n;
@@ -242,170 +310,224 @@ __global__ void __launch_bounds__(NT, 1) k_arnoldi_coop(CoopArgs<T> a) {
   T* P0 = a.part;                               // first pass: dots and w.w
   T* P2 = a.part + 2 * (size_t)nblk * PSTRIDE;  // second pass: dots and w'.w'
   extern __shared__ __align__(16) unsigned char dsmem[];
-  T* sZ = reinterpret_cast<T*>(dsmem);  // [ec][n] D^-1 v_j of a chunk of the block's elements
+  T* sZ = reinterpret_cast<T*>(dsmem);  // [ec][n] per-element values of a chunk
   __shared__ int sPerm[64], sSpos[128];
   __shared__ T sh1[33], sh2[33];
-  __shared__ T scs[32], ssn[32], sg[33], sHc[33];
-  __shared__ int s_done, s_its, s_reorth, s_jdone;
-  __shared__ T s_inv;
-  __shared__ double s_tol;
-  double* Hg = a.dH;
-  double* csg = a.dH + (size_t)(m + 1) * m;
-  double* sng = csg + m;
-  double* gg = sng + m;
-  if (tid == 0) {
-    s_done = a.flags[F_DONE];
-    s_its = a.flags[F_ITS];
-    s_tol = a.scal[S_TOL];
-    s_jdone = 0;
-  }
-  for (int k = tid; k <= m; k += NT) sg[k] = T(gg[k]);
+  __shared__ T scs[32], ssn[32], sg[33], sHc[33], syT[33];
+  __shared__ T sR[32 * 33];  // rotated Hessenberg columns: sR[j * (m+1) + k]
+  __shared__ double sy[33], sdi[33];
+  __shared__ int s_done, s_its, s_reorth, s_jdone, s_conv, s_cycles;
+  __shared__ T s_beta;
+  __shared__ double s_tol, s_bnorm;
   for (int k = tid; k < a.F * a.S; k += NT) sPerm[k] = a.md.perm[k];
   for (int k = tid; k < a.F * a.md.Np; k += NT) sSpos[k] = a.spos[k];
+  // |b|
+  block_dots<T>(a.V, a.bvec, 0, 1, N, r0, nrow, vec, P0 + (size_t)b * PSTRIDE);
+  grid.sync();
+  block_reduce_all<T>(P0, nblk, 1, sh1);
   __syncthreads();
-  for (int j = 0; j < m; ++j) {
-    if (s_done) break;
-    const T* vj = a.V + (size_t)j * N;
-    T* vn = a.V + (size_t)(j + 1) * N;
-    // (1) per chunk of the block's elements: z = D^-1 v_j into shared
-    //     memory, then the push of C z to the neighbours' face sides
+  if (tid == 0) {
+    s_bnorm = sqrt(double(sh1[0]));
+    s_tol = fmax(a.scal[S_RELTOL] * s_bnorm, a.scal[S_ABSTOL]);
+    s_its = 0;
+    s_cycles = 0;
+  }
+  __syncthreads();
+  for (;;) {
+    // ---- r = b - J x (own rows); the pushed products cross blocks
     for (int c0 = e0; c0 < e1; c0 += a.ec) {
       const int nl = min(a.ec, e1 - c0);
-      for (int t = tid; t < nl * n; t += NT) {
-        const int le = t / n, r = t - le * n;
-        const int e = c0 + le;
-        sZ[t] = block_row<NB, T>(a.inv + (size_t)e * n * n, vj + (size_t)e * n, r, n);
-      }
-      __syncthreads();
-      face_push<DIM, T>(a, sZ, sPerm, c0, nl, a.cfs);
-      __syncthreads();
+      chunk_apply_push<DIM, NB, T>(a, a.diag, a.x, false, sZ, sPerm, c0, nl, a.w);
     }
     grid.sync();
-    // (2) w = v_j + sum over the faces whose stencil holds the row's node of
-    //     the pushed product (own rows)
-    {
-      constexpr int NV = DIM + 2;
+    for (int t = tid; t < nrow; t += NT) {
+      const int le = t / n, r = t - le * n;
+      const int j = r / NV, av = r - j * NV;
+      const int e = e0 + le;
+      const int64_t row = (int64_t)e * n + r;
+      T acc = a.w[row];
+      for (int f = 0; f < a.F; ++f) {
+        const int sp = sSpos[f * a.md.Np + j];
+        if (sp < 0) continue;
+        const int fs = a.fside[(int64_t)e * a.F + f];
+        if (fs >= 0) acc += a.cfs[(size_t)fs * a.nb + sp * NV + av];
+      }
+      a.w[row] = a.bvec[row] - acc;
+    }
+    __syncthreads();
+    block_dots<T>(a.V, a.w, 0, 1, N, r0, nrow, vec, P0 + (size_t)b * PSTRIDE);
+    grid.sync();
+    block_reduce_all<T>(P0, nblk, 1, sh1);
+    __syncthreads();
+    if (tid == 0) {
+      const T beta = sqrt(sh1[0]);
+      s_beta = beta;
+      if (s_cycles == 0 && b == 0) a.scal[S_BETA0] = double(beta);
+      const bool conv = !(double(beta) > s_tol);
+      s_conv = conv ? 1 : 0;
+      s_done = (conv || s_its >= a.flags[F_ITERMAX] || !isfinite(double(beta))) ? 1 : 0;
+      s_jdone = 0;
+      sg[0] = beta;
+      for (int k = 1; k <= m; ++k) sg[k] = T(0);
+    }
+    __syncthreads();
+    if (s_done) break;
+    block_sub_scale<T>(a.V, sh1, 0, N, a.w, T(1) / s_beta, a.V, r0, nrow, vec, 0);
+    __syncthreads();
+    // ---- Arnoldi
+    for (int j = 0; j < m; ++j) {
+      if (s_done) break;
+      const T* vj = a.V + (size_t)j * N;
+      T* vn = a.V + (size_t)(j + 1) * N;
+      // (1) per chunk: z = D^-1 v_j (shared memory), push C z to the neighbours
+      for (int c0 = e0; c0 < e1; c0 += a.ec) {
+        const int nl = min(a.ec, e1 - c0);
+        chunk_apply_push<DIM, NB, T>(a, a.inv, vj, true, sZ, sPerm, c0, nl, nullptr);
+      }
+      grid.sync();
+      // (2) w = v_j + the pushed products of the faces holding the row's node
       for (int t = tid; t < nrow; t += NT) {
         const int le = t / n, r = t - le * n;
-        const int j = r / NV, av = r - j * NV;
+        const int jn = r / NV, av = r - jn * NV;
         const int e = e0 + le;
         const int64_t row = (int64_t)e * n + r;
         T acc = vj[row];
         for (int f = 0; f < a.F; ++f) {
-          const int sp = sSpos[f * a.md.Np + j];
+          const int sp = sSpos[f * a.md.Np + jn];
           if (sp < 0) continue;
           const int fs = a.fside[(int64_t)e * a.F + f];
           if (fs >= 0) acc += a.cfs[(size_t)fs * a.nb + sp * NV + av];
         }
         a.w[row] = acc;
       }
-    }
-    __syncthreads();
-    // (3) first pass: h1 = V^T w and w.w in one reduction
-    block_dots<T>(a.V, a.w, j + 1, 1, N, r0, nrow, vec, P0 + (size_t)b * PSTRIDE);
-    grid.sync();
-    block_reduce_all<T>(P0, nblk, j + 2, sh1);
-    __syncthreads();
-    if (tid == 0) {
-      T hh = T(0);
-      for (int k = 0; k <= j; ++k) hh += sh1[k] * sh1[k];
-      const T ww = sh1[j + 1];
-      const T n2 = ww - hh;
-      s_reorth = n2 < T(0.5) * ww;
-      sh2[32] = n2;  // |w'|^2
-    }
-    __syncthreads();
-    T n2;
-    if (s_reorth) {
-      // (4) second pass on w' = w - V h1: h2 = V^T w' and w'.w' in one reduction
-      block_sub_scale<T>(a.V, sh1, j + 1, N, a.w, T(1), a.w, r0, nrow, vec, 0);
       __syncthreads();
-      block_dots<T>(a.V, a.w, j + 1, 1, N, r0, nrow, vec, P2 + (size_t)b * PSTRIDE);
+      // (3) first pass: h1 = V^T w and w.w in one reduction
+      block_dots<T>(a.V, a.w, j + 1, 1, N, r0, nrow, vec, P0 + (size_t)b * PSTRIDE);
       grid.sync();
-      block_reduce_all<T>(P2, nblk, j + 2, sh2);
+      block_reduce_all<T>(P0, nblk, j + 2, sh1);
       __syncthreads();
       if (tid == 0) {
         T hh = T(0);
-        for (int k = 0; k <= j; ++k) hh += sh2[k] * sh2[k];
-        const T r = sh2[j + 1] - hh;
-        sh2[32] = r > T(0) ? r : T(0);
+        for (int k = 0; k <= j; ++k) hh += sh1[k] * sh1[k];
+        const T ww = sh1[j + 1];
+        const T n2 = ww - hh;
+        s_reorth = n2 < T(0.5) * ww;
+        sh2[32] = n2;  // |w'|^2
       }
       __syncthreads();
-      n2 = sh2[32];
-    } else {
-      n2 = sh2[32];
+      if (s_reorth) {
+        // (4) second pass on w' = w - V h1: h2 = V^T w' and w'.w' in one reduction
+        block_sub_scale<T>(a.V, sh1, j + 1, N, a.w, T(1), a.w, r0, nrow, vec, 0);
+        __syncthreads();
+        block_dots<T>(a.V, a.w, j + 1, 1, N, r0, nrow, vec, P2 + (size_t)b * PSTRIDE);
+        grid.sync();
+        block_reduce_all<T>(P2, nblk, j + 2, sh2);
+        __syncthreads();
+        if (tid == 0) {
+          T hh = T(0);
+          for (int k = 0; k <= j; ++k) hh += sh2[k] * sh2[k];
+          const T r = sh2[j + 1] - hh;
+          sh2[32] = r > T(0) ? r : T(0);
+        }
+        __syncthreads();
+      }
+      const T hn = sqrt(sh2[32]);
+      const T inv = hn > T(0) ? T(1) / hn : T(0);
+      // (5) lane 0: Hessenberg column j and its Givens rotation (identical in
+      //     every block); warps 1.. : v_{j+1} = (w - V h) / hn
+      if (tid == 0) {
+        for (int k = 0; k <= j; ++k) sHc[k] = s_reorth ? sh1[k] + sh2[k] : sh1[k];
+        sHc[j + 1] = hn;
+        for (int k = 0; k < j; ++k) {
+          const T t0 = scs[k] * sHc[k] + ssn[k] * sHc[k + 1];
+          sHc[k + 1] = -ssn[k] * sHc[k] + scs[k] * sHc[k + 1];
+          sHc[k] = t0;
+        }
+        const T den = hypot(sHc[j], sHc[j + 1]);
+        s_its += 1;
+        if (!(den > T(0)) || !isfinite(den)) {
+          s_done = 1;  // breakdown: keep the j columns built so far
+        } else {
+          scs[j] = sHc[j] / den;
+          ssn[j] = sHc[j + 1] / den;
+          sHc[j] = den;
+          sHc[j + 1] = T(0);
+          sg[j + 1] = -ssn[j] * sg[j];
+          sg[j] = scs[j] * sg[j];
+          s_jdone = j + 1;
+          for (int k = 0; k <= j; ++k) sR[j * M1 + k] = sHc[k];
+          const double resid = fabs(double(sg[j + 1]));
+          if (resid <= s_tol || hn == T(0) || s_its >= a.flags[F_ITERMAX]) s_done = 1;
+        }
+      } else if (tid >= 32) {
+        if (s_reorth)
+          block_sub_scale<T>(a.V, sh2, j + 1, N, a.w, inv, vn, r0, nrow, vec, 32);
+        else
+          block_sub_scale<T>(a.V, sh1, j + 1, N, a.w, inv, vn, r0, nrow, vec, 32);
+      }
+      __syncthreads();
     }
-    const T hn = sqrt(n2);
-    const T inv = hn > T(0) ? T(1) / hn : T(0);
-    // (5) lane 0 of warp 0: Hessenberg column j and its Givens rotation
-    //     (identical in every block); warps 1.. : v_{j+1} = (w - V h) / hn
-    if (tid == 0) {
-      for (int k = 0; k <= j; ++k) sHc[k] = s_reorth ? sh1[k] + sh2[k] : sh1[k];
-      sHc[j + 1] = hn;
-      for (int k = 0; k < j; ++k) {
-        const T t0 = scs[k] * sHc[k] + ssn[k] * sHc[k + 1];
-        sHc[k + 1] = -ssn[k] * sHc[k] + scs[k] * sHc[k + 1];
-        sHc[k] = t0;
+    // ---- y = R^-1 g (FP64 back substitution by warp 0), x += D^-1 V y
+    if (tid < 32) {
+      const int nn = s_jdone, lane = tid;
+      for (int k = lane; k < nn; k += 32) {
+        sdi[k] = 1.0 / double(sR[k * M1 + k]);
+        sy[k] = double(sg[k]);
       }
-      const T den = hypot(sHc[j], sHc[j + 1]);
-      s_its += 1;
-      if (!(den > T(0)) || !isfinite(den)) {
-        s_done = 1;  // breakdown: keep the j columns built so far
-      } else {
-        scs[j] = sHc[j] / den;
-        ssn[j] = sHc[j + 1] / den;
-        sHc[j] = den;
-        sHc[j + 1] = T(0);
-        sg[j + 1] = -ssn[j] * sg[j];
-        sg[j] = scs[j] * sg[j];
-        s_jdone = j + 1;
-        const double resid = fabs(double(sg[j + 1]));
-        if (resid <= s_tol || hn == T(0) || s_its >= a.flags[F_ITERMAX]) s_done = 1;
+      __syncwarp();
+      for (int k = nn - 1; k >= 0; --k) {
+        const double yk = sy[k] * sdi[k];
+        __syncwarp();
+        if (lane == 0) sy[k] = yk;
+        for (int i = lane; i < k; i += 32) sy[i] -= double(sR[k * M1 + i]) * yk;
+        __syncwarp();
       }
-      if (b == 0) {
-        double* Hc = Hg + (size_t)j * (m + 1);
-        for (int k = 0; k <= j + 1; ++k) Hc[k] = double(sHc[k]);
-        a.scal[S_RESID] = fabs(double(sg[j + 1]));
-      }
-    } else if (tid >= 32) {
-      if (s_reorth)
-        block_sub_scale<T>(a.V, sh2, j + 1, N, a.w, inv, vn, r0, nrow, vec, 32);
-      else
-        block_sub_scale<T>(a.V, sh1, j + 1, N, a.w, inv, vn, r0, nrow, vec, 32);
+      for (int k = lane; k < nn; k += 32) syT[k] = T(sy[k]);
+      if (lane == 0) s_cycles += 1;
+    }
+    __syncthreads();
+    block_lincomb<T>(a.V, syT, s_jdone, N, a.w, r0, nrow);
+    __syncthreads();
+    for (int t = tid; t < nrow; t += NT) {
+      const int le = t / n, r = t - le * n;
+      const int e = e0 + le;
+      a.x[(size_t)e * n + r] += block_row<NB, T>(a.inv + (size_t)e * n * n, a.w + (size_t)e * n, r, n);
     }
     __syncthreads();
   }
   if (b == 0 && tid == 0) {
     a.flags[F_ITS] = s_its;
     a.flags[F_JDONE] = s_jdone;
-    a.flags[F_DONE] = s_done;
-    for (int k = 0; k <= m; ++k) gg[k] = double(sg[k]);
-    for (int k = 0; k < m; ++k) {
-      csg[k] = double(scs[k]);
-      sng[k] = double(ssn[k]);
-    }
+    a.flags[F_DONE] = 1;
+    a.flags[F_CONV] = s_conv;
+    a.flags[F_CYCLES] = s_cycles;
+    a.scal[S_BETA] = double(s_beta);
+    a.scal[S_RESID] = double(s_beta);
+    a.scal[S_BNORM] = s_bnorm;
+    a.scal[S_TOL] = s_tol;
   }
 }
 
 template <typename T>
-int launch_T(eg_ls* ls, int* max_blocks_cache) {
+int launch_T(eg_ls* ls) {
   eg_mesh* m = ls->lo->mesh;
   CoopArgs<T> a;
   a.md = dev_mesh(m);
   a.inv = (const T*)ls->pc->inv;
+  a.diag = (const T*)ls->lo->diag;
   a.cpl = (const T*)ls->lo->cpl;
   a.spos = ls->lo->spos;
   a.fside = ls->lo->fside;
   a.cfs = (T*)ls->cfs;
+  a.bvec = (const T*)ls->bT;
+  a.x = (T*)ls->xT;
   a.nb = ls->lo->nb;
   a.S = m->S;
   a.F = m->F;
   a.nv = m->nv;
   a.V = (T*)ls->V;
   a.w = (T*)ls->w;
-  a.z = (T*)ls->z;
   a.part = (T*)ls->part;
-  a.dH = ls->dH;
   a.flags = ls->dflags;
   a.scal = ls->dscal;
   a.m = ls->m;
@@ -415,30 +537,28 @@ int launch_T(eg_ls* ls, int* max_blocks_cache) {
   void* fn = nullptr;
   switch (a.n) {
 #define EG_CASE(NBV) \
-  case NBV: fn = m->dim == 2 ? (void*)k_arnoldi_coop<2, NBV, T> : (void*)k_arnoldi_coop<3, NBV, T>; break;
+  case NBV: fn = m->dim == 2 ? (void*)k_gmres_coop<2, NBV, T> : (void*)k_gmres_coop<3, NBV, T>; break;
     EG_CASE(12) EG_CASE(24) EG_CASE(28) EG_CASE(40) EG_CASE(48) EG_CASE(60) EG_CASE(72) EG_CASE(30)
 #undef EG_CASE
-    default: fn = m->dim == 2 ? (void*)k_arnoldi_coop<2, 0, T> : (void*)k_arnoldi_coop<3, 0, T>;
+    default: fn = m->dim == 2 ? (void*)k_gmres_coop<2, 0, T> : (void*)k_gmres_coop<3, 0, T>;
   }
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  (void)max_blocks_cache;
-  // elements per block, and per shared-memory chunk of D^-1 v values
-  const size_t side_bytes = (size_t)a.n * sizeof(T);
+  // one block per SM; elements per block, and per shared-memory chunk
+  const size_t elem_bytes = (size_t)a.n * sizeof(T);
   int nblk = sms;
   if (nblk > m->E) nblk = m->E;
   if (nblk > EG_COOP_MAX_BLOCKS) nblk = EG_COOP_MAX_BLOCKS;
   const int epb = (m->E + nblk - 1) / nblk;
-  int ec = (int)((40 * 1024) / side_bytes);
+  int ec = (int)((40 * 1024) / elem_bytes);
   if (ec < 1) ec = 1;
   if (ec > epb) ec = epb;
   a.ec = ec;
-  const size_t smem = (size_t)ec * side_bytes;
+  const size_t smem = (size_t)ec * elem_bytes;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, NT, smem);
-  if (per_sm < 1) nblk = 0;
-  if (nblk <= 0) {
-    eg_set_error("persistent Arnoldi kernel cannot be resident");
+  if (per_sm < 1 || nblk <= 0) {
+    eg_set_error("persistent GMRES kernel cannot be resident");
     return EG_ERR_UNSUPPORTED;
   }
   void* args[] = {&a};
@@ -449,12 +569,11 @@ int launch_T(eg_ls* ls, int* max_blocks_cache) {
 
 }  // namespace
 
-// one Arnoldi cycle (up to ls->m iterations) of the right-preconditioned
-// GMRES as one cooperative launch; partial sums need 4 * grid * 33 values of
-// ls->part, which eg_ls_create sizes for up to 2 blocks per SM.
-int eg_arnoldi_coop(eg_ls* ls) {
-  static int cache_f = 0, cache_d = 0;
-  return ls->lo->prec == EG_F64 ? launch_T<double>(ls, &cache_d) : launch_T<float>(ls, &cache_f);
+// the whole GMRES solve (all restart cycles) as one cooperative launch;
+// partial sums need 4 * grid * 33 values of ls->part (eg_ls_create sizes
+// them for EG_COOP_MAX_BLOCKS blocks)
+int eg_gmres_coop(eg_ls* ls) {
+  return ls->lo->prec == EG_F64 ? launch_T<double>(ls) : launch_T<float>(ls);
 }
 
 bool eg_coop_usable(const eg_ls* ls) {

@@ -23,14 +23,14 @@
 
 namespace {
 
-enum { F_DONE = 0, F_JDONE = 1, F_ITS = 2, F_CONV = 3, F_ITERMAX = 4, F_REORTH = 5 };
+enum { F_DONE = 0, F_JDONE = 1, F_ITS = 2, F_CONV = 3, F_ITERMAX = 4, F_REORTH = 5, F_CYCLES = 6 };
 
 // a cycle kernel runs unless the cycle is done, or its optional condition
 // flag (need >= 0) is zero
 __device__ __forceinline__ bool gm_skip(const int* flags, int need) {
   return flags && (flags[F_DONE] || (need >= 0 && !flags[need]));
 }
-enum { S_TOL = 0, S_RESID = 1, S_BETA = 2, S_BNORM = 3, S_RELTOL = 4, S_ABSTOL = 5 };
+enum { S_TOL = 0, S_RESID = 1, S_BETA = 2, S_BNORM = 3, S_RELTOL = 4, S_ABSTOL = 5, S_BETA0 = 6 };
 
 // per-block partial sums of V[k] . w for k < cnt (skips when *done)
 template <typename T, int NT>
@@ -523,7 +523,7 @@ template <typename T>
 void enqueue_arnoldi(eg_ls* ls) {
   eg_mesh* m = ls->lo->mesh;
   const int64_t N = m->ndof;
-  const int mm = ls->m, stride = mm + 2;
+  const int mm = ls->m;
   T* V = (T*)ls->V;
   T* w = (T*)ls->w;
   T* z = (T*)ls->z;
@@ -531,7 +531,6 @@ void enqueue_arnoldi(eg_ls* ls) {
   T* h1 = h;
   T* h2 = h + (mm + 2);
   T* hn = h + 2 * (mm + 2);
-  T* part = (T*)ls->part;
   const int* fl = ls->dflags;
   for (int j = 0; j < mm; ++j) {
     T* vj = V + (size_t)j * N;
@@ -615,7 +614,31 @@ int gmres_T(eg_ls* ls, eg_ls_stats* st) {
   EG_CUDA(cudaMemcpyAsync(ls->dscal, sc, sizeof(sc), cudaMemcpyHostToDevice, m->stream));
   EG_CUDA(cudaMemcpyAsync(ls->dflags, fl, sizeof(fl), cudaMemcpyHostToDevice, m->stream));
   const bool coop = eg_coop_usable(ls) && !m->capturing;
-  if (!coop && !ls->g_init && !ls->g_cycle && !ls->graphs_ok) {
+  if (coop) {
+    // the whole solve in one persistent launch
+    const int rc = eg_gmres_coop(ls);
+    if (rc != EG_OK) return rc;
+    int flags[8];
+    double scal[8];
+    EG_CUDA(cudaMemcpyAsync(ls->hh, ls->dscal, sizeof(scal), cudaMemcpyDeviceToHost, m->stream));
+    EG_CUDA(cudaMemcpyAsync(ls->hh + 8, ls->dflags, sizeof(flags), cudaMemcpyDeviceToHost, m->stream));
+    EG_CUDA(cudaStreamSynchronize(m->stream));
+    std::memcpy(scal, ls->hh, sizeof(scal));
+    std::memcpy(flags, ls->hh + 8, sizeof(flags));
+    if (!std::isfinite(scal[S_BETA])) {
+      eg_set_error("GMRES: non-finite residual");
+      return EG_ERR_NONFINITE;
+    }
+    if (st) {
+      st->iters = flags[F_ITS];
+      st->restarts = flags[F_CYCLES];
+      st->converged = flags[F_CONV];
+      st->res0 = scal[S_BETA0];
+      st->res_final = scal[S_BETA];
+    }
+    return EG_OK;
+  }
+  if (!ls->g_init && !ls->g_cycle && !ls->graphs_ok) {
     cudaGraphExec_t gi = nullptr, gc = nullptr;
     bool ok = capture(m, [&]() { enqueue_init<T>(ls, 1); }, &gi, &ls->g_init_nodes);
     ok = ok && capture(m, [&]() { enqueue_cycle<T>(ls); }, &gc, &ls->g_cycle_nodes);
@@ -629,10 +652,7 @@ int gmres_T(eg_ls* ls, eg_ls_stats* st) {
     }
   }
   auto run_init = [&]() -> int {
-    if (coop) {
-      enqueue_init<T>(ls, 1);
-      m->launches += 8;
-    } else if (ls->graphs_ok) {
+    if (ls->graphs_ok) {
       EG_CUDA(cudaGraphLaunch((cudaGraphExec_t)ls->g_init, m->stream));
       m->launches += ls->g_init_nodes;
     } else {
@@ -642,12 +662,7 @@ int gmres_T(eg_ls* ls, eg_ls_stats* st) {
     return EG_OK;
   };
   auto run_cycle = [&]() -> int {
-    if (coop) {
-      int rc2 = eg_arnoldi_coop(ls);
-      if (rc2 != EG_OK) return rc2;
-      enqueue_tail<T>(ls);
-      m->launches += 12;
-    } else if (ls->graphs_ok) {
+    if (ls->graphs_ok) {
       EG_CUDA(cudaGraphLaunch((cudaGraphExec_t)ls->g_cycle, m->stream));
       m->launches += ls->g_cycle_nodes;
     } else {

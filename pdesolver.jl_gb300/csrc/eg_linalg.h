@@ -55,9 +55,9 @@ struct eg_ls {
   bool graphs_ok;  // capture succeeded (else the same launches run eagerly)
 };
 void eg_gmres_release(eg_ls* ls);
-// one Arnoldi cycle as a persistent cooperative kernel (eg_arnoldi.cu)
+// the whole GMRES solve as one persistent cooperative kernel (eg_arnoldi.cu)
 #define EG_COOP_MAX_BLOCKS 1024
-int eg_arnoldi_coop(eg_ls* ls);
+int eg_gmres_coop(eg_ls* ls);
 bool eg_coop_supported();
 // the persistent kernel handles this system (device support, coupling blocks
 // of at most 64 rows, small face tables)
