@@ -46,7 +46,7 @@ WORKLOAD = ("steady Euler solve: annulus 64x64 (8192 triangles), SBP-Gamma p=3, 
             "Newton-GMRES(30) + element block-Jacobi + pseudo-transient continuation to "
             "|R|_{M^-1} < 1e-10, p-continuation 1 -> 3")
 NEWTON_OPTS = {"res_abstol": 1e-10, "res_reltol": 1e-14, "itermax": 200, "krylov_reltol": 1e-2,
-               "newton_globalize_euler": True, "euler_tau": 0.5}
+               "newton_globalize_euler": True, "euler_tau": 5.0}
 LEVEL_TOL = 1e-4
 LEVELS = (1, 3)
 
@@ -172,7 +172,7 @@ def _oracle():
 # Newton / GMRES iteration counts of one full solve per level, as measured on
 # the GPU for this workload; they scale the bounded CPU sample of the
 # reference arm (the GPU arm uses the counts of its own run)
-DEFAULT_COUNTS = {1: (77, 8212), 3: (32, 8041)}
+DEFAULT_COUNTS = {1: (19, 4746), 3: (23, 7755)}
 
 
 def cpu_solve_estimate(threads, counts, n_gmres=100):
@@ -408,6 +408,7 @@ def run_ours(args, rank, world, dist):
                                "t_jacobian_ms": s.t_jacobian, "t_pc_ms": s.t_pc,
                                "t_krylov_ms": s.t_krylov} for p, s in zip(LEVELS, stats_mixed)],
                    "fp64_solves_per_s": fp64_rate, "mixed_over_fp64": value / world / fp64_rate,
+                   "fp64_counts": {str(p): [s.iters, s.krylov_iters] for p, s in zip(LEVELS, stats64)},
                    "functional_r1_mixed": f_mixed, "functional_r1_fp64": f64,
                    "functional_rel_diff": abs(f_mixed - f64) / abs(f64)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",

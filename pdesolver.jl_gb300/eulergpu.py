@@ -171,22 +171,37 @@ class GPUMesh:
 
     # ---- array helpers -----------------------------------------------------
     @staticmethod
-    def _ptr(a):
-        """(pointer, mem flag) of a numpy array (host) or a CUDA tensor."""
+    def _ptr(a, n):
+        """(pointer, mem flag) of a numpy array (host) or a CUDA tensor of n
+        float64 values; the library sees raw pointers, so the size is
+        checked here."""
         if isinstance(a, np.ndarray):
             if not (a.flags.c_contiguous and a.dtype == np.float64):
                 raise ValueError("expected a C-contiguous float64 array")
+            if a.size != n:
+                raise ValueError(f"expected {n} values, got an array of {a.size}")
             return C.c_void_p(a.ctypes.data), abi.EG_MEM_HOST
         # torch tensor on the device
         if a.dtype.__repr__() != "torch.float64" or not a.is_contiguous():
             raise ValueError("expected a contiguous float64 tensor")
+        if a.numel() != n:
+            raise ValueError(f"expected {n} values, got a tensor of {a.numel()}")
         if a.device.type != "cuda":
             return C.c_void_p(a.data_ptr()), abi.EG_MEM_HOST
         return C.c_void_p(a.data_ptr()), abi.EG_MEM_DEVICE
 
+    @staticmethod
+    def _dev(t, n, dtype_name):
+        """device pointer of a contiguous CUDA tensor of n values of dtype_name."""
+        if getattr(t, "device", None) is None or t.device.type != "cuda":
+            raise ValueError("expected a CUDA tensor")
+        if t.dtype.__repr__() != dtype_name or not t.is_contiguous() or t.numel() != n:
+            raise ValueError(f"expected a contiguous {dtype_name} tensor of {n} values")
+        return C.c_void_p(t.data_ptr())
+
     def eval_residual(self, q, res, t=0.0):
-        pq, mq = self._ptr(q)
-        pr, mr = self._ptr(res)
+        pq, mq = self._ptr(q, self.ndof)
+        pr, mr = self._ptr(res, self.ndof)
         if mq != mr:
             raise ValueError("q and res must both be host or both be device arrays")
         check(self.lib.eg_eval_residual(self.handle, pq, pr, t, mq))
@@ -202,8 +217,8 @@ class GPUMesh:
 
     def eval_residual_async(self, q_dev, res_dev):
         """enqueue R(q) with device tensors, no host synchronisation."""
-        check(self.lib.eg_eval_residual_async(self.handle, C.c_void_p(q_dev.data_ptr()),
-                                              C.c_void_p(res_dev.data_ptr())))
+        check(self.lib.eg_eval_residual_async(self.handle, self._dev(q_dev, self.ndof, "torch.float64"),
+                                              self._dev(res_dev, self.ndof, "torch.float64")))
 
     def sync(self):
         check(self.lib.eg_sync(self.handle))
@@ -221,7 +236,7 @@ class GPUMesh:
 
     def functional_pressure(self, q, bc_group=0):
         """integral of p over the faces of a boundary-condition group."""
-        pq, mq = self._ptr(q)
+        pq, mq = self._ptr(q, self.ndof)
         out = C.c_double()
         check(self.lib.eg_calc_functional(self.handle, pq, bc_group, mq, C.byref(out)))
         return out.value
@@ -229,7 +244,7 @@ class GPUMesh:
     def newton(self, q, opts=None, precision=0):
         """steady Newton solve in place (reference newton.jl:54); returns stats.
         Raises EulerGPUError(EG_ERR_NOT_CONVERGED) if the tolerances are not met."""
-        pq, mq = self._ptr(q)
+        pq, mq = self._ptr(q, self.ndof)
         o = NewtonOpts.from_opts(opts, precision)
         st = NewtonStats()
         rc = self.lib.eg_newton_solve(self.handle, pq, mq, C.byref(o), C.byref(st))
@@ -239,13 +254,13 @@ class GPUMesh:
 
     def rk4(self, q, h, t_max, itermax=0, res_tol=-1.0):
         """classical RK4 in place (reference rk4.jl:404); returns stats."""
-        pq, mq = self._ptr(q)
+        pq, mq = self._ptr(q, self.ndof)
         st = Rk4Stats()
         check(self.lib.eg_rk4(self.handle, pq, h, t_max, itermax, res_tol, mq, C.byref(st)))
         return st
 
     def calc_norm(self, r, strongres=True):
-        pr, mr = self._ptr(r)
+        pr, mr = self._ptr(r, self.ndof)
         out = C.c_double()
         check(self.lib.eg_calc_norm(self.handle, pr, int(strongres), mr, C.byref(out)))
         return out.value
@@ -302,19 +317,26 @@ class LinearOperator:
         self.nb = op.stencilsize * gmesh.mesh.numDofPerNode
 
     def calc(self, q):
-        pq, mq = GPUMesh._ptr(q)
+        pq, mq = GPUMesh._ptr(q, self.g.ndof)
         check(self.lib.eg_lo_calc(self.handle, pq, mq))
 
     def apply(self, x, y):
-        px, mx = GPUMesh._ptr(x)
-        py, _ = GPUMesh._ptr(y)
+        px, mx = GPUMesh._ptr(x, self.g.ndof)
+        py, my = GPUMesh._ptr(y, self.g.ndof)
+        if mx != my:
+            raise ValueError("x and y must both be host or both be device arrays")
         check(self.lib.eg_lo_apply(self.handle, px, py, mx))
         return y
 
+    @property
+    def native_dtype(self):
+        return "torch.float32" if self.precision == 1 else "torch.float64"
+
     def apply_native(self, x_dev, y_dev):
         """y = J x on device tensors of the operator's precision (enqueued)."""
-        check(self.lib.eg_lo_apply_native(self.handle, C.c_void_p(x_dev.data_ptr()),
-                                          C.c_void_p(y_dev.data_ptr())))
+        n, dt = self.g.ndof, self.native_dtype
+        check(self.lib.eg_lo_apply_native(self.handle, GPUMesh._dev(x_dev, n, dt),
+                                          GPUMesh._dev(y_dev, n, dt)))
 
     def blocks(self):
         ms = self.g.mesh
@@ -350,15 +372,18 @@ class BlockJacobiPC:
         check(self.lib.eg_pc_calc(self.handle))
 
     def apply(self, x, y):
-        px, mx = GPUMesh._ptr(x)
-        py, _ = GPUMesh._ptr(y)
+        px, mx = GPUMesh._ptr(x, self.lo.g.ndof)
+        py, my = GPUMesh._ptr(y, self.lo.g.ndof)
+        if mx != my:
+            raise ValueError("x and y must both be host or both be device arrays")
         check(self.lib.eg_pc_apply(self.handle, px, py, mx))
         return y
 
     def apply_native(self, x_dev, y_dev):
         """y = M^-1 x on device tensors of the operator's precision (enqueued)."""
-        check(self.lib.eg_pc_apply_native(self.handle, C.c_void_p(x_dev.data_ptr()),
-                                          C.c_void_p(y_dev.data_ptr())))
+        n, dt = self.lo.g.ndof, self.lo.native_dtype
+        check(self.lib.eg_pc_apply_native(self.handle, GPUMesh._dev(x_dev, n, dt),
+                                          GPUMesh._dev(y_dev, n, dt)))
 
     def close(self):
         if getattr(self, "handle", None):
@@ -386,8 +411,10 @@ class LinearSolver:
         check(self.lib.eg_ls_set_tolerances(self.handle, reltol, abstol, dtol, itermax))
 
     def solve(self, b, x):
-        pb, mb = GPUMesh._ptr(b)
-        px, _ = GPUMesh._ptr(x)
+        pb, mb = GPUMesh._ptr(b, self.lo.g.ndof)
+        px, mx = GPUMesh._ptr(x, self.lo.g.ndof)
+        if mb != mx:
+            raise ValueError("b and x must both be host or both be device arrays")
         st = LsStats()
         check(self.lib.eg_ls_solve(self.handle, pb, px, mb, C.byref(st)))
         return st
@@ -418,8 +445,8 @@ def prolongation_matrix(op_lo, op_hi, nv):
 def prolong(g_lo: GPUMesh, q_lo, g_hi: GPUMesh, q_hi):
     """q_hi <- degree prolongation of q_lo (same elements, on the device)."""
     T = prolongation_matrix(g_lo.mesh.sbp, g_hi.mesh.sbp, g_lo.mesh.numDofPerNode)
-    pl, ml = GPUMesh._ptr(q_lo)
-    ph, mh = GPUMesh._ptr(q_hi)
+    pl, ml = GPUMesh._ptr(q_lo, g_lo.ndof)
+    ph, mh = GPUMesh._ptr(q_hi, g_hi.ndof)
     if ml != mh:
         raise ValueError("q_lo and q_hi must both be host or both be device arrays")
     check(g_lo.lib.eg_prolong(g_lo.handle, pl, g_hi.handle, ph, C.c_void_p(T.ctypes.data), ml))

@@ -35,3 +35,17 @@ def test_mesh_create_rejects_bad_sizes(gpu_lib):
     p = abi.EgParams.make()
     h = C.c_void_p()
     assert gpu_lib.eg_mesh_create(C.byref(d), C.byref(p), C.byref(h)) == abi.EG_ERR_INVALID
+
+
+def test_host_arrays_are_size_checked():
+    """the library takes raw pointers; the Python host layer refuses arrays
+    whose size is not the mesh's number of unknowns (before any device call)."""
+    import numpy as np
+    import pytest
+    from pdesolver_gb300 import eulergpu
+    with pytest.raises(ValueError):
+        eulergpu.GPUMesh._ptr(np.zeros(10), 12)
+    with pytest.raises(ValueError):
+        eulergpu.GPUMesh._ptr(np.zeros(12, dtype=np.float32), 12)
+    ptr, mem = eulergpu.GPUMesh._ptr(np.zeros(12), 12)
+    assert mem == 0 and ptr.value

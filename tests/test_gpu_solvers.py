@@ -141,6 +141,18 @@ def test_rk4_matches_oracle(gpu_lib, oracle):
     assert np.abs(qg - qo).max() <= 1e-11 * np.abs(qo).max()
 
 
+def test_wrong_sized_state_is_refused(gpu_lib):
+    """a state of another degree's mesh is refused before any device work."""
+    import torch
+    ms, opts, q = problems.config1(n=3, p=1, seed=3)
+    ms3, opts3, _ = problems.config1(n=3, p=3, seed=3)
+    g3 = eulergpu.GPUMesh(ms3, opts3)
+    with pytest.raises(ValueError):
+        g3.functional_pressure(q, 0)
+    with pytest.raises(ValueError):
+        g3.functional_pressure(torch.from_numpy(q).cuda(), 0)
+
+
 def test_functional_matches_oracle(gpu_lib, oracle):
     ms, opts, q = problems.config1()
     g = eulergpu.GPUMesh(ms, opts)
