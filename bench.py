@@ -86,6 +86,34 @@ def krylov_kernel_bytes(ms, es):
     return spmv, pc
 
 
+def gmres_bytes(ms, its, m, es):
+    """Algorithmic bytes of one GMRES(m) solve in the persistent kernel with
+    `its` Arnoldi iterations (full cycles but the last), es bytes per value.
+    Arnoldi iteration j (basis v_0..v_j): the inverse blocks and the coupling
+    blocks once (the operator I + C D^-1), v_j read and w written by the
+    operator, one Gram-Schmidt pass (dots: v_0..v_j and w read; update:
+    v_0..v_j and w read, v_{j+1} written), i.e. (2 j + 7) vectors.  Per cycle:
+    the residual b - J x (element and coupling blocks, x, b, r and v_0: 5
+    vectors) and the update x += D^-1 V y (jdone + 3 vectors and the inverse
+    blocks); one more residual ends the solve.  No cache reuse is credited,
+    and the second Gram-Schmidt passes are not counted."""
+    nv = ms.numDofPerNode
+    n = ms.sbp.numnodes * nv
+    nb = ms.sbp.stencilsize * nv
+    N = ms.numDof
+    blocks = ms.numEl * n * n
+    cpl = 2 * ms.numInterfaces * nb * nb
+    total, left = 0, its
+    while left > 0:
+        jd = min(m, left)
+        total += sum(blocks + cpl + (2 * j + 7) * N for j in range(jd))
+        total += blocks + cpl + 5 * N            # residual at the cycle start
+        total += blocks + (jd + 3) * N           # x += D^-1 V y
+        left -= jd
+    total += blocks + cpl + 5 * N                # final residual
+    return es * total
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled during the timed region."""
 
@@ -352,6 +380,27 @@ def run_ours(args, rank, world, dist):
         t_pc += c.elapsed_time(d) / reps
     b_spmv, b_pc = krylov_kernel_bytes(ms3, 4)
 
+    # the persistent GMRES kernel (one launch per linear solve) on the same
+    # system: 300 iterations (10 full cycles), L2 flushed before each solve
+    ls = eulergpu.LinearSolver(pc, lo, restart=30)
+    gm_its = 300
+    ls.set_tolerances(reltol=1e-30, abstol=0.0, itermax=gm_its)
+    bvec = torch.randn(ms3.numDof, dtype=torch.float64, device="cuda")
+    xvec = torch.zeros_like(bvec)
+    ls.solve(bvec, xvec)
+    gm_ms = []
+    for _ in range(3):
+        xvec.zero_()
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        st_gm = ls.solve(bvec, xvec)
+        b.record()
+        torch.cuda.synchronize()
+        gm_ms.append(a.elapsed_time(b))
+    t_gm = statistics.median(gm_ms)
+    b_gm = gmres_bytes(ms3, st_gm.iters, 30, 4)
+
     # FP64 residual evaluations/s (L2 flushed between evaluations)
     ms2, opts2, qr = problems.config2()
     gres = eulergpu.GPUMesh(ms2, opts2)
@@ -381,13 +430,16 @@ def run_ours(args, rank, world, dist):
         return
     peaks, src = measured_peaks()
     fp64_peak = measure_fp64_peak(torch)
-    dom_name, dom_ms, dom_bytes = (("k_spmv", t_spmv, b_spmv) if t_spmv >= t_pc
-                                   else ("k_block_apply", t_pc, b_pc))
+    dom_name, dom_ms, dom_bytes = "k_gmres_coop", t_gm, b_gm
     achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
     traffic = None
     try:
+        # DRAM bytes per Arnoldi iteration from an ncu capture of the same
+        # kernel on the same system (profiles/), scaled to this launch
         with open(os.path.join(ROOT, "profiles", "krylov_c2_traffic.json")) as f:
-            traffic = json.load(f).get(dom_name)
+            per_it = json.load(f).get("k_gmres_coop_bytes_per_iteration")
+        if per_it:
+            traffic = per_it * st_gm.iters
     except (OSError, ValueError):
         pass
     counts = {p: (s.iters, s.krylov_iters) for p, s in zip(LEVELS, stats_mixed)}
@@ -413,9 +465,12 @@ def run_ours(args, rank, world, dist):
                    "functional_rel_diff": abs(f_mixed - f64) / abs(f64)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "peak_source": src,
-                     "kernel": dom_name + " (FP32, in the Krylov loop)",
-                     "algorithmic_bytes_per_launch": dom_bytes, "kernel_ms": dom_ms},
-        "krylov_kernels_ms": {"k_spmv": t_spmv, "k_block_apply": t_pc},
+                     "kernel": dom_name + " (FP32: one launch = one GMRES(30) solve of the p=3 "
+                               "Newton system at the converged state, %d iterations)" % st_gm.iters,
+                     "algorithmic_bytes_per_launch": dom_bytes, "kernel_ms": dom_ms,
+                     "us_per_iteration": 1e3 * dom_ms / max(st_gm.iters, 1)},
+        "krylov_kernels_ms": {"k_spmv (stream path)": t_spmv, "k_block_apply (stream path)": t_pc,
+                              "k_spmv_GBs": b_spmv / (t_spmv * 1e-3) / 1e9},
         "residual": {"evals_per_s": 1e3 / res_ms, "ms_per_eval": res_ms,
                      "phases_ms": {"k_face_flux": t_face, "k_element": t_elem},
                      "hbm_frac": rbytes / ((t_face + t_elem) * 1e-3) / 1e9 / peaks["hbm_gbs"],
