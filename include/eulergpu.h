@@ -292,7 +292,9 @@ typedef struct {
 /* newton / newtonInner (reference src/NonlinearSolvers/newton.jl:54-304):
    q <- q + dq until calcNorm(R(q), M^-1) < res_abstol, or the relative
    norm < res_reltol, or ||dq|| <= step_tol.  q is FP64 in host or device
-   memory. */
+   memory.  The Jacobian, preconditioner, Krylov basis and work vectors are
+   kept by the mesh after the first solve (for this precision and restart
+   length), so later solves on the mesh allocate nothing. */
 int eg_newton_solve(eg_mesh* mesh, double* q, int32_t mem, const eg_newton_opts* opts,
                     eg_newton_stats* stats);
 
@@ -311,6 +313,11 @@ typedef struct {
   double t;                 /* final time                                   */
   double res_norm;          /* last stage-1 norm sqrt(sum (M^-1 R)^2 M)     */
 } eg_rk4_stats;
+
+/* Frees the Newton work objects a mesh keeps between solves (the reference
+   frees its linear solver with `free(ls)`, LinearSolvers.jl).  Mesh destroy
+   frees them too. */
+int eg_newton_release(eg_mesh* mesh);
 
 /* rk4 (reference src/NonlinearSolvers/rk4.jl:144-336, 404-456): classical
    4-stage RK4 on dq/dt = M^-1 R(q) with step h for round(t_max/h) steps

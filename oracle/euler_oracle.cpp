@@ -531,7 +531,7 @@ double dot(const std::vector<double>& a, const std::vector<double>& b) {
 // options (read_input.jl:559-569): GMRES(30), right PC, MGS.
 int gmres(const eg_mesh_desc* d, int n, int nb, const double* diag, const double* cpl,
           const BlockLU& pc, const std::vector<double>& b, std::vector<double>& x, int m,
-          double reltol, double abstol, int itermax, int* iters_out) {
+          double reltol, double abstol, int itermax, int* iters_out, bool* conv_out = nullptr) {
   const size_t N = b.size();
   std::vector<std::vector<double>> V(m + 1, std::vector<double>(N));
   std::vector<double> w(N), z(N);
@@ -543,6 +543,7 @@ int gmres(const eg_mesh_desc* d, int n, int nb, const double* diag, const double
     jac_apply(d, n, nb, diag, cpl, x.data(), w.data());
     for (size_t i = 0; i < N; ++i) w[i] = b[i] - w[i];
     const double beta = std::sqrt(dot(w, w));
+    if (conv_out) *conv_out = !(beta > tol);
     if (!(beta > tol) || its >= itermax) break;
     for (size_t i = 0; i < N; ++i) V[0][i] = w[i] / beta;
     std::fill(g.begin(), g.end(), 0.0);
@@ -595,6 +596,9 @@ int gmres(const eg_mesh_desc* d, int n, int nb, const double* diag, const double
 constexpr double PTC_MAX_GROWTH = 1.5;
 // a pseudo-time step that raises |R| by more than this factor is rejected
 constexpr double PTC_MAX_INCREASE = 10.0;
+// a step whose Krylov solve did not converge and that leaves |R| above this
+// fraction of its previous value shrinks the pseudo-time step 4x
+constexpr double PTC_STALL = 0.5;
 
 double strong_norm(const eg_mesh_desc* d, const double* r) {
   const int nv = d->dim + 2, Np = d->nodes_per_el;
@@ -664,8 +668,9 @@ int oracle_newton(const eg_mesh_desc* d, const eg_params* p, double* q, const eg
     if (!lu.factor(d, diag.data(), n)) return EG_ERR_LU_PIVOT;
     for (size_t i = 0; i < N; ++i) { b[i] = -res[i]; dq[i] = 0; }
     int its = 0;
+    bool kconv = false;
     gmres(d, n, nb, diag.data(), cpl.data(), lu, b, dq, o->gmres_restart > 0 ? o->gmres_restart : 30,
-          o->krylov_reltol, 1e-30, o->krylov_itermax > 0 ? o->krylov_itermax : 1000, &its);
+          o->krylov_reltol, 1e-30, o->krylov_itermax > 0 ? o->krylov_itermax : 1000, &its, &kconv);
     s.krylov_iters += its;
     double sn2 = 0;
     for (size_t i = 0; i < N; ++i) { qsave[i] = q[i]; q[i] += dq[i]; sn2 += dq[i] * dq[i]; }
@@ -686,9 +691,16 @@ int oracle_newton(const eg_mesh_desc* d, const eg_params* p, double* q, const eg
       norm_prev = 0.0;   // no SER update right after a rejection
       continue;
     }
+    // the Krylov solve hit its iteration limit and the step gained little:
+    // keep the step, shrink the pseudo-time step (PTC_STALL)
+    const bool stalled = o->globalize_euler && !kconv && nn > PTC_STALL * norm;
     norm = nn;
     s.res_norm = norm;
     conv = norm < o->res_abstol || norm / rel < o->res_reltol || s.step_norm <= o->step_tol;
+    if (stalled && !conv) {
+      tau_l *= 0.25;
+      norm_prev = 0.0;
+    }
   }
   s.converged = conv;
   if (stats) *stats = s;

@@ -26,7 +26,9 @@
 // cancel with their inverses).
 #include <cooperative_groups.h>
 
+#include <algorithm>
 #include <cmath>
+#include <mutex>
 
 #include "eg_internal.h"
 #include "eg_kernels.cuh"
@@ -41,6 +43,15 @@ enum { F_DONE = 0, F_JDONE = 1, F_ITS = 2, F_CONV = 3, F_ITERMAX = 4, F_REORTH =
 enum { S_TOL = 0, S_RESID = 1, S_BETA = 2, S_BNORM = 3, S_RELTOL = 4, S_ABSTOL = 5, S_BETA0 = 6 };
 constexpr int NT = 1024;  // one block per SM
 constexpr int NB_MAX = 64;  // coupling-block rows handled by the face-side pass
+// systems whose element blocks take at most this many bytes run on one block
+constexpr size_t kSmallOperatorBytes = size_t(2) << 20;
+
+// one multi-block persistent solve in flight per device: two grids that each
+// wait in grid barriers must never hold parts of the GPU at the same time
+std::mutex& coop_mutex(int dev) {
+  static std::mutex mu[64];
+  return mu[dev & 63];
+}
 constexpr int PSTRIDE = 33;  // partial slots per block
 
 template <typename T>
@@ -545,9 +556,12 @@ int launch_T(eg_ls* ls) {
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  // one block per SM; elements per block, and per shared-memory chunk
+  // grid: one block for a small system (a one-block grid is resident or not
+  // at all, so several run side by side on other streams); otherwise up to
+  // one block per SM with at least 32 elements each, one such grid at a time
   const size_t elem_bytes = (size_t)a.n * sizeof(T);
-  int nblk = sms;
+  const size_t op_bytes = (size_t)m->E * a.n * a.n * sizeof(T);
+  int nblk = op_bytes <= kSmallOperatorBytes ? 1 : std::max(2, std::min(sms, (m->E + 31) / 32));
   if (nblk > m->E) nblk = m->E;
   if (nblk > EG_COOP_MAX_BLOCKS) nblk = EG_COOP_MAX_BLOCKS;
   const int epb = (m->E + nblk - 1) / nblk;
@@ -562,8 +576,15 @@ int launch_T(eg_ls* ls) {
     return EG_ERR_UNSUPPORTED;
   }
   void* args[] = {&a};
+  if (nblk == 1) {
+    EG_CUDA(cudaLaunchCooperativeKernel(fn, dim3(1), dim3(NT), args, smem, m->stream));
+    m->launches += 1;
+    return EG_OK;
+  }
+  std::lock_guard<std::mutex> lock(coop_mutex(dev));
   EG_CUDA(cudaLaunchCooperativeKernel(fn, dim3(nblk), dim3(NT), args, smem, m->stream));
   m->launches += 1;
+  EG_CUDA(cudaStreamSynchronize(m->stream));  // the grid has finished before the next one starts
   return EG_OK;
 }
 

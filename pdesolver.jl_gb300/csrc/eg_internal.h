@@ -47,7 +47,8 @@ struct EFace {
 // phase ids of the device timers (eg_timings fields)
 enum { EG_PHASE_FACE = 0, EG_PHASE_ELEMENT = 1, EG_PHASE_NORM = 2, EG_PHASE_OTHER = 3, EG_NPHASE = 4 };
 
-struct TimerState;  // event pool (eg_timing.cu)
+struct TimerState;     // event pool (eg_timing.cu)
+struct eg_newton_ws;   // cached Newton work objects (eg_solvers.cu)
 
 struct eg_mesh {
   // sizes
@@ -92,7 +93,12 @@ struct eg_mesh {
   int64_t launches;         // kernel launches since creation
   int32_t h_bndry_offsets[64];  // host copy of the BC-group offsets
   bool capturing;           // a CUDA graph is being captured on `stream`
+  eg_newton_ws* nws;        // Newton operator / preconditioner / solver / vectors, kept
+                            // between solves (released by eg_newton_release or destroy)
+  double* prolong_T;        // device copy of the last prolongation matrix (eg_prolong)
+  size_t prolong_T_n;
 };
+void eg_newton_ws_free(eg_mesh* m);
 
 // phase timers: bracket a group of launches on m->stream
 void eg_phase_begin(eg_mesh* m, int phase);

@@ -82,6 +82,8 @@ static void freestream_state(const DevParams& p, int dim, double* sol) {
 
 static void free_mesh(eg_mesh* m) {
   if (!m) return;
+  eg_newton_ws_free(m);
+  if (m->prolong_T) cudaFree(m->prolong_T);
   void* bufs[] = {m->Q, m->w, m->interp, m->perm, m->nbrperm, m->wface, m->lift, m->liftS,
                   m->nbrinv, m->dxidx,
                   m->jac, m->Minv, m->ifaces, m->nrm_face, m->bfaces, m->bc_of_b,

@@ -299,12 +299,13 @@ int eg_launch_residual(eg_mesh* m, const double* q, double* res) {
   size_t smem;
   element_launch_shape(m, &epb, &threads, &smem);
   const int blocks = (m->E + epb - 1) / epb;
-  static bool attr_set = false;
-  if (!attr_set) {
+  // once per process (thread-safe static initialisation)
+  static const bool attr_set = [] {
     cudaFuncSetAttribute(k_element<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     cudaFuncSetAttribute(k_element<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr_set = true;
-  }
+    return true;
+  }();
+  (void)attr_set;
   if (m->dim == 2)
     k_element<2><<<blocks, threads, smem, m->stream>>>(md, q, m->fflux, res, m->status, epb);
   else

@@ -108,6 +108,85 @@ double ms_since(std::chrono::steady_clock::time_point t0) {
 // added here; the reference has neither)
 constexpr double PTC_MAX_GROWTH = 1.5;
 constexpr double PTC_MAX_INCREASE = 10.0;
+// a step whose Krylov solve did not reach its tolerance and that leaves |R|
+// above this fraction of its previous value shrinks the pseudo-time step 4x
+// (recovery added here: restarted GMRES with the element block-Jacobi
+// preconditioner stagnates on the nearly steady Jacobian of fine meshes, and
+// the reference's SER update would keep the pseudo-time step there)
+constexpr double PTC_STALL = 0.5;
+
+// Newton work objects of a mesh, kept between solves so that repeated solves
+// (continuation levels, batches, serving) allocate nothing after the first:
+// cudaFree synchronises the device and would serialise concurrent streams.
+struct eg_newton_ws {
+  int prec = -1, restart = 0;
+  eg_lo* lo = nullptr;
+  eg_pc* pc = nullptr;
+  eg_ls* ls = nullptr;
+  double* res = nullptr;    // [N] residual
+  double* dq = nullptr;     // [N] Newton step
+  double* qsave = nullptr;  // [N] state before the step (pseudo-time rejection)
+  double* qd = nullptr;     // [N] device state for host inputs (lazily)
+};
+
+void eg_newton_ws_free(eg_mesh* m) {
+  eg_newton_ws* w = m ? m->nws : nullptr;
+  if (!w) return;
+  if (w->ls) eg_ls_destroy(w->ls);
+  if (w->pc) eg_pc_destroy(w->pc);
+  if (w->lo) eg_lo_destroy(w->lo);
+  double* bufs[] = {w->res, w->dq, w->qsave, w->qd};
+  for (double* b : bufs)
+    if (b) cudaFree(b);
+  delete w;
+  m->nws = nullptr;
+}
+
+extern "C" int eg_newton_release(eg_mesh* m) {
+  if (!m) return EG_ERR_INVALID;
+  EG_CUDA(cudaStreamSynchronize(m->stream));
+  eg_newton_ws_free(m);
+  return EG_OK;
+}
+
+namespace {
+// the mesh's Newton work objects for (precision, restart), created on first use
+int newton_ws(eg_mesh* m, int prec, int restart, bool host, eg_newton_ws** out) {
+  eg_newton_ws* w = m->nws;
+  if (w && (w->prec != prec || w->restart != restart)) {
+    EG_CUDA(cudaStreamSynchronize(m->stream));
+    eg_newton_ws_free(m);
+    w = nullptr;
+  }
+  const int64_t N = m->ndof;
+  if (!w) {
+    w = new eg_newton_ws();
+    m->nws = w;
+    w->prec = prec;
+    w->restart = restart;
+    cudaError_t ce = cudaMalloc((void**)&w->res, 8 * N);
+    if (ce == cudaSuccess) ce = cudaMalloc((void**)&w->dq, 8 * N);
+    if (ce == cudaSuccess) ce = cudaMalloc((void**)&w->qsave, 8 * N);
+    if (ce != cudaSuccess) {
+      eg_newton_ws_free(m);
+      return eg_cuda_fail(ce, "eg_newton_solve");
+    }
+    int st = eg_lo_create(m, prec, &w->lo);
+    if (st == EG_OK) st = eg_pc_create(w->lo, &w->pc);
+    if (st == EG_OK) st = eg_ls_create(w->lo, w->pc, restart, &w->ls);
+    if (st != EG_OK) {
+      eg_newton_ws_free(m);
+      return st;
+    }
+  }
+  if (host && !w->qd) {
+    cudaError_t ce = cudaMalloc((void**)&w->qd, 8 * N);
+    if (ce != cudaSuccess) return eg_cuda_fail(ce, "eg_newton_solve");
+  }
+  *out = w;
+  return EG_OK;
+}
+}  // namespace
 
 extern "C" int eg_newton_solve(eg_mesh* m, double* q, int32_t mem, const eg_newton_opts* o,
                                eg_newton_stats* stats) {
@@ -116,63 +195,35 @@ extern "C" int eg_newton_solve(eg_mesh* m, double* q, int32_t mem, const eg_newt
     return EG_ERR_INVALID;
   }
   const int64_t N = m->ndof;
-  double* qd = q;
-  double* res = nullptr;
-  double* dq = nullptr;
-  eg_lo* lo = nullptr;
-  eg_pc* pc = nullptr;
-  eg_ls* ls = nullptr;
   eg_newton_stats s;
   std::memset(&s, 0, sizeof(s));
-  int st = EG_OK;
-  auto cleanup = [&]() {
-    if (ls) eg_ls_destroy(ls);
-    if (pc) eg_pc_destroy(pc);
-    if (lo) eg_lo_destroy(lo);
-    if (res) cudaFree(res);
-    if (dq) cudaFree(dq);
-    if (qd != q && qd) cudaFree(qd);
-  };
-  cudaError_t ce = cudaMalloc((void**)&res, 8 * N);
-  if (ce == cudaSuccess) ce = cudaMalloc((void**)&dq, 8 * N);
-  if (ce == cudaSuccess && mem == EG_MEM_HOST) {
-    ce = cudaMalloc((void**)&qd, 8 * N);
-    if (ce == cudaSuccess) ce = cudaMemcpyAsync(qd, q, 8 * N, cudaMemcpyHostToDevice, m->stream);
+  eg_newton_ws* w = nullptr;
+  int st = newton_ws(m, o->precision, o->gmres_restart > 0 ? o->gmres_restart : 30, mem == EG_MEM_HOST, &w);
+  if (st != EG_OK) return st;
+  eg_lo* lo = w->lo;
+  eg_pc* pc = w->pc;
+  eg_ls* ls = w->ls;
+  double* res = w->res;
+  double* dq = w->dq;
+  double* qd = mem == EG_MEM_HOST ? w->qd : q;
+  cudaError_t ce = cudaSuccess;
+  if (mem == EG_MEM_HOST) {
+    ce = cudaMemcpyAsync(qd, q, 8 * N, cudaMemcpyHostToDevice, m->stream);
+    if (ce != cudaSuccess) return eg_cuda_fail(ce, "eg_newton_solve");
   }
-  if (ce != cudaSuccess) {
-    if (mem == EG_MEM_HOST && ce != cudaSuccess) qd = (qd == q) ? q : qd;
-    cleanup();
-    return eg_cuda_fail(ce, "eg_newton_solve");
-  }
-  st = eg_lo_create(m, o->precision, &lo);
-  if (st == EG_OK) st = eg_pc_create(lo, &pc);
-  if (st == EG_OK) st = eg_ls_create(lo, pc, o->gmres_restart > 0 ? o->gmres_restart : 30, &ls);
-  if (st == EG_OK) st = eg_ls_set_tolerances(ls, o->krylov_reltol, 1e-30, -1, o->krylov_itermax > 0 ? o->krylov_itermax : 1000);
-  if (st != EG_OK) {
-    cleanup();
-    return st;
-  }
+  st = eg_ls_set_tolerances(ls, o->krylov_reltol, 1e-30, -1, o->krylov_itermax > 0 ? o->krylov_itermax : 1000);
+  if (st != EG_OK) return st;
   auto t0 = std::chrono::steady_clock::now();
   double norm = 0;
   st = residual_and_norm(m, qd, res, &norm);
   s.t_residual += ms_since(t0);
-  if (st != EG_OK) {
-    cleanup();
-    return st;
-  }
+  if (st != EG_OK) return st;
   s.res_norm0 = norm;
   s.res_norm = norm;
   const double norm_rel = norm;
   bool conv = norm < o->res_abstol || (norm_rel > 0 && norm / norm_rel < o->res_reltol && false);
   const int g = grid64(N);
-  double* qsave = nullptr;
-  if (o->globalize_euler) {
-    ce = cudaMalloc((void**)&qsave, 8 * N);
-    if (ce != cudaSuccess) {
-      cleanup();
-      return eg_cuda_fail(ce, "eg_newton_solve");
-    }
-  }
+  double* qsave = o->globalize_euler ? w->qsave : nullptr;
   double tau_l = o->euler_tau, norm_prev = 0.0;
   // per-iteration trace on stderr (the reference's newton_verbosity output)
   const bool verbose = std::getenv("EG_NEWTON_VERBOSE") != nullptr;
@@ -242,12 +293,16 @@ extern "C" int eg_newton_solve(eg_mesh* m, double* q, int32_t mem, const eg_newt
       continue;
     }
     if (st != EG_OK) break;
+    const bool stalled = o->globalize_euler && !ks.converged && nn > PTC_STALL * norm;
     norm = nn;
     s.res_norm = norm;
     conv = norm < o->res_abstol || (norm / norm_rel < o->res_reltol) ||
            (s.step_norm <= o->step_tol);
+    if (stalled && !conv) {
+      tau_l *= 0.25;
+      norm_prev = 0.0;  // no SER growth right after
+    }
   }
-  if (qsave) cudaFree(qsave);
   s.converged = conv ? 1 : 0;
   if (st == EG_OK && mem == EG_MEM_HOST) {
     ce = cudaMemcpyAsync(q, qd, 8 * N, cudaMemcpyDeviceToHost, m->stream);
@@ -255,7 +310,6 @@ extern "C" int eg_newton_solve(eg_mesh* m, double* q, int32_t mem, const eg_newt
     if (ce != cudaSuccess) st = eg_cuda_fail(ce, "eg_newton_solve copy-out");
   }
   if (stats) *stats = s;
-  cleanup();
   if (st == EG_OK && !conv) {
     eg_set_error("Newton did not converge in %d iterations (|R| = %g)", o->itermax, s.res_norm);
     return EG_ERR_NOT_CONVERGED;
@@ -354,9 +408,17 @@ extern "C" int eg_prolong(eg_mesh* lo, const double* q_lo, eg_mesh* hi, double* 
     return EG_ERR_INVALID;
   }
   const int nlo = lo->Np * lo->nv, nhi = hi->Np * hi->nv;
-  double* dT = nullptr;
-  EG_CUDA(cudaMalloc((void**)&dT, sizeof(double) * (size_t)nlo * nhi));
-  EG_CUDA(cudaMemcpyAsync(dT, T, sizeof(double) * (size_t)nlo * nhi, cudaMemcpyHostToDevice, hi->stream));
+  const size_t nT = (size_t)nlo * nhi;
+  if (hi->prolong_T_n < nT) {  // device copy of T, kept by the fine mesh
+    EG_CUDA(cudaStreamSynchronize(hi->stream));
+    if (hi->prolong_T) cudaFree(hi->prolong_T);
+    hi->prolong_T = nullptr;
+    hi->prolong_T_n = 0;
+    EG_CUDA(cudaMalloc((void**)&hi->prolong_T, sizeof(double) * nT));
+    hi->prolong_T_n = nT;
+  }
+  double* dT = hi->prolong_T;
+  EG_CUDA(cudaMemcpyAsync(dT, T, sizeof(double) * nT, cudaMemcpyHostToDevice, hi->stream));
   const double* src = q_lo;
   double* dst = q_hi;
   if (mem == EG_MEM_HOST) {
@@ -370,7 +432,6 @@ extern "C" int eg_prolong(eg_mesh* lo, const double* q_lo, eg_mesh* hi, double* 
   if (mem == EG_MEM_HOST)
     EG_CUDA(cudaMemcpyAsync(q_hi, dst, 8 * (size_t)hi->ndof, cudaMemcpyDeviceToHost, hi->stream));
   EG_CUDA(cudaStreamSynchronize(hi->stream));
-  cudaFree(dT);
   return EG_OK;
 }
 

@@ -142,19 +142,16 @@ int eg_launch_split_element(eg_mesh* m, const double* q, double* res) {
   const size_t smem = smem_of(epb);
   const int threads = epb * Np;
   const int blocks = (m->E + epb - 1) / epb;
-  static bool attr_set[4] = {false, false, false, false};
-  if (m->dim == 2) {
-    if (!attr_set[2]) {
-      cudaFuncSetAttribute(k_split_element<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-      attr_set[2] = true;
-    }
+  // once per process (thread-safe static initialisation)
+  static const bool attr_set = [] {
+    cudaFuncSetAttribute(k_split_element<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_split_element<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    return true;
+  }();
+  (void)attr_set;
+  if (m->dim == 2)
     k_split_element<2><<<blocks, threads, smem, m->stream>>>(md, q, m->fflux, res, m->status, epb);
-  } else {
-    if (!attr_set[3]) {
-      cudaFuncSetAttribute(k_split_element<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-      attr_set[3] = true;
-    }
+  else
     k_split_element<3><<<blocks, threads, smem, m->stream>>>(md, q, m->fflux, res, m->status, epb);
-  }
   return EG_OK;
 }

@@ -81,6 +81,7 @@ def _declare(lib):
     lib.eg_rk4.argtypes = [vp, vp, C.c_double, C.c_double, C.c_int32, C.c_double, C.c_int32,
                            C.POINTER(Rk4Stats)]
     lib.eg_rk4_static.argtypes = lib.eg_rk4.argtypes
+    lib.eg_newton_release.argtypes = [vp]
 
 
 class LsStats(C.Structure):
@@ -251,6 +252,10 @@ class GPUMesh:
         self.last_newton = st
         check(rc)
         return st
+
+    def release_newton(self):
+        """free the Newton work objects the mesh keeps between solves."""
+        check(self.lib.eg_newton_release(self.handle))
 
     def rk4(self, q, h, t_max, itermax=0, res_tol=-1.0):
         """classical RK4 in place (reference rk4.jl:404); returns stats."""

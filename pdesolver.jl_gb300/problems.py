@@ -88,3 +88,30 @@ def config3(n=24, p=2, seed=4, warp=0.05, warp_seed=3):
     q = free_stream(3, ms.coords.shape[:2], Ma=0.5)
     q[..., 0] *= 1.0 + rng.normal(0.0, 0.01, size=q.shape[:2])
     return ms, opts, np.ascontiguousarray(q)
+
+
+def config4_specs(count=96, seed=5):
+    """Batched workload: `count` annulus problems with n ~ logU(8, 96) (E = 2 n^2),
+    SBP-Gamma p ~ U{1, 2, 3, 4}, vortex M_in ~ U(0.3, 0.7), each started from
+    the free stream times (1 + U(-0.01, 0.01)) with its own seed."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for _ in range(count):
+        n = int(round(np.exp(rng.uniform(np.log(8.0), np.log(96.0)))))
+        p = int(rng.integers(1, 5))
+        M = float(rng.uniform(0.3, 0.7))
+        specs.append({"n": n, "p": p, "M_in": M, "seed": int(rng.integers(0, 2**31 - 1))})
+    return specs
+
+
+def config4_problem(spec):
+    """[(mesh, opts)] of the continuation levels (p = 1, then p when p > 1) and
+    the initial state of the first level."""
+    ps = (1,) if spec["p"] == 1 else (1, spec["p"])
+    levels, q0 = [], None
+    for p in ps:
+        ms, opts, q = config2(n=spec["n"], p=p, seed=spec["seed"], M_in=spec["M_in"])
+        levels.append((ms, opts))
+        if q0 is None:
+            q0 = q
+    return levels, q0
