@@ -409,6 +409,11 @@ def run_ours(args, rank, world, dist):
     rd = torch.zeros_like(qd)
     for _ in range(3):
         gres.eval_residual_async(qd, rd)
+    # launch shape of the element kernel picked by the autotuner
+    res_tune = gres.autotune(qd, reps=10)
+    res_cfg = gres.launch_config()
+    for _ in range(3):
+        gres.eval_residual_async(qd, rd)
     gres.set_timing(True)
     gres.reset_timings()
     nres = 30
@@ -473,6 +478,9 @@ def run_ours(args, rank, world, dist):
                               "k_spmv_GBs": b_spmv / (t_spmv * 1e-3) / 1e9},
         "residual": {"evals_per_s": 1e3 / res_ms, "ms_per_eval": res_ms,
                      "phases_ms": {"k_face_flux": t_face, "k_element": t_elem},
+                     "element_launch_config": res_cfg,
+                     "autotune_ms": [[c["elements_per_cta"], int(c["volume_mma"]), ms]
+                                     for c, ms in res_tune],
                      "hbm_frac": rbytes / ((t_face + t_elem) * 1e-3) / 1e9 / peaks["hbm_gbs"],
                      "fp64_tflops": rflops / ((t_face + t_elem) * 1e-3) / 1e12,
                      "fp64_frac_of_dgemm": rflops / ((t_face + t_elem) * 1e-3) / 1e12 / fp64_peak,
@@ -527,6 +535,9 @@ def run_c3(args, rank, world):
     g = eulergpu.GPUMesh(ms, opts)
     g.set_stream(stream.cuda_stream)
     qd = torch.from_numpy(q).cuda()
+    # elements per CTA of the split-form kernel picked by the autotuner
+    tune = g.autotune(qd, reps=5)
+    cfg = g.launch_config()
     h = 1e-3   # the oracle is unstable at 2e-3 on this mesh, stable at 1.5e-3 on 12^3
     nsteps = max(args.steps, 1)
     for _ in range(args.warmup):
@@ -592,6 +603,8 @@ def run_c3(args, rank, world):
         "roofline_hbm": {"achieved": nbytes / t_res / 1e9, "peak": peaks["hbm_gbs"],
                          "frac": nbytes / t_res / 1e9 / peaks["hbm_gbs"]},
         "phases_ms": {"k_face_flux": t_face, "k_split_element": t_elem},
+        "element_launch_config": cfg,
+        "autotune_ms": [[c["elements_per_cta"], ms_] for c, ms_ in tune],
         "cpu_baseline": {"value": 1.0 / (4 * t_cpu_res), "unit": "steps/s", "cores": used,
                          "kind": "port", "sample": "one full split-form residual on 1 core "
                                                    "(%.1f s), 4 per RK4 step" % t_cpu_res},
@@ -733,6 +746,180 @@ def run_c4(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+C5_WORKLOAD = ("serving: Poisson arrivals of steady-solve requests at 0.8 x the measured "
+               "capacity, 80% 2-D annuli from the batched distribution (n ~ logU(8, 96), "
+               "SBP-Gamma p ~ U{1..4}, vortex M_in ~ U(0.3, 0.7)), 20% 3-D warped cubes "
+               "(n ~ U{8..24}, 6 n^3 diagonal-E tets, p ~ U{1, 2}, free stream Mach ~ U(0.3, 0.7)); "
+               "Roe, free stream * (1 + U(-0.01, 0.01)) starts, Newton-GMRES(30) + block-Jacobi + "
+               "pseudo-transient continuation to |R| < 1e-10 with p-continuation; 150 GB HBM "
+               "budget; seed 6")
+
+
+def _c5_build_meshes(keys, workers):
+    """Host meshes of every geometry key, built by a spawn process pool (the
+    client side of the stream: requests arrive with their meshes)."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    keys = sorted(set(keys), key=lambda k: -(k[1] ** k[0]) * k[2])
+    with cf.ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as ex:
+        built = list(ex.map(problems.request_meshes, keys, chunksize=1))
+    return dict(zip(keys, built))
+
+
+def _c5_requests(specs, meshes, rate, arrivals=True):
+    from pdesolver_gb300 import serve
+    t, out = 0.0, []
+    for k, sp in enumerate(specs):
+        key = problems.geometry_key(sp)
+        levels, q0 = problems.request_problem(sp, meshes[key])
+        if arrivals:
+            t += sp["gap"] / rate
+        out.append(serve.SolveRequest(rid=k, levels=levels, q0=q0, opts=NEWTON_OPTS, key=key,
+                                      arrival=t if arrivals else 0.0, level_tol=LEVEL_TOL))
+    return out
+
+
+def c5_cpu_rates(threads=1, n_gmres=20):
+    """Oracle phase times per element (residual, Jacobian, block LU, one
+    GMRES iteration) for the 2-D degrees (32 x 32 annulus) and the 3-D
+    degrees (4^3 x 6 warped cube)."""
+    from pdesolver_gb300 import eulergpu
+    lib = _oracle()
+    used = lib.oracle_set_threads(int(threads))
+    rates = {}
+    for key in [(2, 32, p) for p in (1, 2, 3, 4)] + [(3, 4, p) for p in (1, 2)]:
+        ms = problems.request_meshes(key)[-1]
+        lv, q = problems.request_problem({"dim": key[0], "n": key[1], "p": key[2], "M_in": 0.5,
+                                          "seed": 1}, [ms])
+        desc = abi.MeshDesc(ms)
+        P = eulergpu.params_from_opts(lv[0][1])
+        out = np.zeros(4)
+        assert lib.oracle_newton_phase_times(C.byref(desc.desc), C.byref(P), abi.dptr(q), n_gmres,
+                                             abi.dptr(out)) == 0
+        rates[(key[0], key[2])] = [x / ms.numEl for x in out]
+    return rates, used
+
+
+def run_c5(args, rank, world):
+    """Serving: a Poisson stream of steady-solve requests (one step = the
+    stream); mixed precision, and the plain FP64 path on the same arrivals."""
+    import torch
+    from pdesolver_gb300 import serve
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    budget = int(150e9)
+    all_specs = problems.config5_specs(count=2000, seed=6)
+    specs = all_specs[:args.requests]
+    probe_specs = problems.config5_specs(count=args.probe, seed=7)
+    t0 = time.perf_counter()
+    meshes = _c5_build_meshes([problems.geometry_key(s) for s in specs + probe_specs],
+                              max(1, min(16, os.cpu_count() or 1)))
+    t_build = time.perf_counter() - t0
+    torch.cuda.set_device(dev)
+    torch.cuda.init()
+    summaries, results, servers = {}, {}, {}
+    # capacity: the probe requests all queued at once (closed loop), mixed precision
+    probe = _c5_requests(probe_specs, meshes, 1.0, arrivals=False)
+    srv = serve.SteadySolveServer(budget, slots=args.workers, precision=1)
+    pres = srv.serve(probe)
+    srv.close()
+    capacity = serve.latency_summary(pres)["solves_per_s"]
+    rate = 0.8 * capacity
+    with ClockSampler(dev) as clk:
+        for name, prec in (("mixed", 1), ("fp64", 0)):
+            reqs = _c5_requests(specs, meshes, rate)
+            srv = serve.SteadySolveServer(budget, slots=args.workers, precision=prec)
+            torch.cuda.synchronize()
+            res = srv.serve(reqs)
+            torch.cuda.synchronize()
+            srv.close()
+            s = serve.latency_summary(res)
+            s.update(peak_bytes_estimated=srv.peak_bytes, peak_requests_on_device=srv.peak_running,
+                     retried=sum(1 for r in res if r.retries),
+                     errors=sorted({r.error[:200] for r in res if r.error})[:4])
+            summaries[name] = s
+            results[name] = res
+    mixed = summaries["mixed"]
+    # the two precisions agree on every request's functional
+    fdiff = [abs(a.functional - b.functional) / abs(b.functional)
+             for a, b in zip(results["mixed"], results["fp64"])
+             if a.error is None and b.error is None and b.functional]
+    if rank != 0:
+        return
+    rates, used = c5_cpu_rates(1)
+    cpu_t, n_ok = 0.0, 0
+    for sp, r in zip(specs, results["mixed"]):
+        if r.error is not None:
+            continue
+        n_ok += 1
+        levels = meshes[problems.geometry_key(sp)]
+        for ms, st in zip(levels, r.stats):
+            rr = rates[(ms.dim, ms.sbp.p)]
+            cpu_t += ms.numEl * (st["iters"] * (rr[0] + rr[1] + rr[2]) + rr[0] + st["krylov_iters"] * rr[3])
+    h2d = sum(r.q0.nbytes for r in _c5_requests(specs, meshes, rate))
+    d2h = sum(r.q.nbytes for r in results["mixed"] if r.q is not None)
+    line = {
+        "metric": "served steady solves/s (p50/p99 latency)", "value": mixed["solves_per_s"] * world,
+        "unit": "solves/s", "n_gpus": world, "steps": 1, "warmup": 1,
+        "ms_per_step": 1e3 * mixed["span_s"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic",
+        "config": {"workload": C5_WORKLOAD, "requests": len(specs),
+                   "sample": f"the first {len(specs)} of the 2000-request stream",
+                   "requests_3d": sum(1 for s in specs if s["dim"] == 3),
+                   "slots": args.workers, "hbm_budget_bytes": budget,
+                   "capacity_probe": {"requests": len(probe), "solves_per_s": capacity,
+                                      "seed": 7},
+                   "arrival_rate_per_s": rate, "host_mesh_build_s": t_build,
+                   "timing": "host clock: completion minus arrival per request; solves/s = "
+                             "completed / (last completion - first arrival)",
+                   "l2": "per-request working sets up to 14 GB; inputs exceed the 129 MB L2",
+                   "parallelism": f"{args.workers} slots (host threads x streams), replicas x{world}"},
+        "serving": {"mixed": mixed, "fp64": summaries["fp64"],
+                    "functional_rel_diff_mixed_vs_fp64_max": max(fdiff) if fdiff else None},
+        "cpu_baseline": {"value": n_ok / cpu_t if cpu_t else None, "unit": "solves/s", "cores": used,
+                         "kind": "port",
+                         "sample": "oracle phase times per element (32x32 annulus per 2-D degree, "
+                                   "4^3x6 cube per 3-D degree) scaled by each request's elements "
+                                   "and this run's Newton/GMRES counts, no queueing"},
+        "e2e": {"value": mixed["solves_per_s"] * world, "unit": "solves/s",
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_tune(args):
+    """Autotuner sweep of the element kernel per operator and degree: weak
+    form (Roe) on the 64 x 64 annulus with SBP-Gamma p = 1..4 and on the
+    warped 24^3 x 6 cube with diagonal-E tets p = 1, 2; split form (IR) on the
+    same cubes.  Prints one JSON line with every candidate's time."""
+    import torch
+    from pdesolver_gb300 import eulergpu
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    cases = [("2d weak gamma", p, problems.config2(p=p)) for p in (1, 2, 3, 4)]
+    for p in (1, 2):
+        ms, opts, q = problems.config3(n=24, p=p)
+        cases.append(("3d split diage", p, (ms, opts, q)))
+        cases.append(("3d weak diage", p, (ms, dict(opts, Flux_name="RoeFlux", volume_integral_type=1), q)))
+    out = []
+    for name, p, (ms, opts, q) in cases:
+        g = eulergpu.GPUMesh(ms, opts)
+        qd = torch.from_numpy(q).cuda()
+        table = g.autotune(qd, reps=10)
+        best = g.launch_config()
+        default = [ms_ for c, ms_ in table if c["elements_per_cta"] == max(1, 256 // ms.sbp.numnodes)
+                   and not c["volume_mma"]]
+        cpu_core = [ms_ for c, ms_ in table if not c["volume_mma"]]
+        mma = [ms_ for c, ms_ in table if c["volume_mma"]]
+        out.append({"operator": name, "p": p, "Np": ms.sbp.numnodes, "elements": ms.numEl,
+                    "best": best, "best_ms": min(ms_ for _, ms_ in table),
+                    "builtin_ms": default[0] if default else None,
+                    "best_cuda_core_ms": min(cpu_core) if cpu_core else None,
+                    "best_mma_ms": min(mma) if mma else None,
+                    "table": [[c["elements_per_cta"], int(c["volume_mma"]), ms_] for c, ms_ in table]})
+        g.close()
+    print(json.dumps({"autotune": out}), flush=True)
+
+
 def run_kernels_only(args, which):
     """Short run of the isolated kernels for profiling captures: the FP32
     operator / block-Jacobi applies of the C2 problem (p=3, initial state), or
@@ -805,10 +992,13 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4"],
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5", "tune"],
                     help="c2: steady Newton solves (headline); c3: 3-D entropy-stable RK4; "
-                         "c4: batch of 96 steady solves")
-    ap.add_argument("--workers", type=int, default=8, help="host threads of the c4 batch")
+                         "c4: batch of 96 steady solves; c5: served stream of steady solves")
+    ap.add_argument("--workers", type=int, default=8,
+                    help="host threads of the c4 batch / serving slots of c5")
+    ap.add_argument("--requests", type=int, default=2000, help="c5: requests of the stream served")
+    ap.add_argument("--probe", type=int, default=32, help="c5: requests of the capacity probe")
     ap.add_argument("--only", default=None, choices=["krylov", "residual", "gmres", "split"],
                     help="run only the isolated kernels (for profiler captures)")
     args = ap.parse_args()
@@ -822,6 +1012,12 @@ def main():
         return
     if args.workload == "c4" and args.impl == "ours":
         run_c4(args, rank, world)
+        return
+    if args.workload == "tune" and args.impl == "ours":
+        run_tune(args)
+        return
+    if args.workload == "c5" and args.impl == "ours":
+        run_c5(args, rank, world)
         return
     dist = None
     if args.impl == "reference":

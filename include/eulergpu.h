@@ -314,6 +314,68 @@ typedef struct {
   double res_norm;          /* last stage-1 norm sqrt(sum (M^-1 R)^2 M)     */
 } eg_rk4_stats;
 
+/* New physics parameters for an existing mesh (the reference changes
+   eqn.params / opts between solves, e.g. the Mach number of a sweep).  The
+   boundary Dirichlet states are re-evaluated; the mesh stream is synchronised.
+   The Newton work objects the mesh keeps stay valid. */
+int eg_mesh_set_params(eg_mesh* mesh, const eg_params* params);
+
+/*
+ * Device-memory estimate from mesh counts (reference src/estimateMem.jl:1-78,
+ * which sums the mesh and solution array sizes from numEl, numInterfaces,
+ * nodes per element and dofs per node).  Here the sums cover every device
+ * array this library allocates for the mesh (eg_mesh_create), the caller's
+ * q and res, and, when newton_precision is EG_F64 or EG_F32, the Newton work
+ * objects of eg_newton_solve (Jacobian, block-Jacobi inverses, GMRES basis,
+ * Newton vectors).  Each array is rounded up to 512 bytes.
+ */
+typedef struct {
+  int32_t dim, num_el, nodes_per_el, nodes_per_face, stencil_size;
+  int32_t num_interfaces, num_bndry, num_orient;
+  int32_t newton_precision;   /* EG_F64, EG_F32, or -1: mesh and state only   */
+  int32_t gmres_restart;      /* restart length of the Newton GMRES (1..31)   */
+  int32_t host_state;         /* 1: Newton is given host q (a staging vector) */
+  int32_t prolong_from_nodes; /* Np of the coarser level this mesh is
+                                 prolonged from (eg_prolong), 0: none         */
+} eg_mem_query;
+
+typedef struct {
+  uint64_t mesh, eqn, jacobian, pc, krylov, newton, total;  /* bytes          */
+  int64_t allocations;        /* device arrays counted                        */
+} eg_mem_estimate;
+
+int eg_estimate_mem(const eg_mem_query* query, eg_mem_estimate* out);
+
+/*
+ * Launch configuration of the element kernel (no reference counterpart: the
+ * reference's element loops are plain Julia).  elements_per_cta: elements a
+ * CTA owns (0: built-in choice, 256 / Np for the weak form); volume_mma: 1 runs
+ * the weak-form volume contraction Q^T F on the FP64 tensor cores (mma.sync
+ * m8n8k4) instead of CUDA cores (weak form only).  Results of the two
+ * contraction kinds agree to FP64 round-off.
+ */
+typedef struct {
+  int32_t elements_per_cta;
+  int32_t volume_mma;
+  int32_t reserved[2];
+} eg_launch_config;
+
+typedef struct {
+  eg_launch_config config;
+  double ms;                 /* mean element-kernel time of the candidate       */
+} eg_tune_entry;
+
+int eg_set_launch_config(eg_mesh* mesh, const eg_launch_config* config);
+int eg_get_launch_config(eg_mesh* mesh, eg_launch_config* config);
+/* Autotuner: times every admissible configuration (elements per CTA 1, 2,
+   4, ... up to 1024 threads, times CUDA-core / tensor-core contraction) on
+   the state q_dev (device, [E][Np][nv]) over `reps` launches each, with CUDA
+   events on the mesh stream, and keeps the fastest on the mesh.  Up to
+   max_entries timings go to `table` (n_entries set to their count).
+   Synchronises the mesh stream; not allowed during stream capture. */
+int eg_autotune(eg_mesh* mesh, const double* q_dev, int32_t reps, eg_tune_entry* table,
+                int32_t max_entries, int32_t* n_entries);
+
 /* Frees the Newton work objects a mesh keeps between solves (the reference
    frees its linear solver with `free(ls)`, LinearSolvers.jl).  Mesh destroy
    frees them too. */

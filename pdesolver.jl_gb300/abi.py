@@ -69,6 +69,32 @@ class EgMeshDesc(C.Structure):
     ]
 
 
+class EgMemQuery(C.Structure):
+    """eg_mem_query: the mesh counts eg_estimate_mem reads."""
+    _fields_ = [(k, C.c_int32) for k in (
+        "dim", "num_el", "nodes_per_el", "nodes_per_face", "stencil_size", "num_interfaces",
+        "num_bndry", "num_orient", "newton_precision", "gmres_restart", "host_state",
+        "prolong_from_nodes")]
+
+
+class EgMemEstimate(C.Structure):
+    _fields_ = [("mesh", C.c_uint64), ("eqn", C.c_uint64), ("jacobian", C.c_uint64),
+                ("pc", C.c_uint64), ("krylov", C.c_uint64), ("newton", C.c_uint64),
+                ("total", C.c_uint64), ("allocations", C.c_int64)]
+
+    def asdict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class EgLaunchConfig(C.Structure):
+    _fields_ = [("elements_per_cta", C.c_int32), ("volume_mma", C.c_int32),
+                ("reserved", C.c_int32 * 2)]
+
+
+class EgTuneEntry(C.Structure):
+    _fields_ = [("config", EgLaunchConfig), ("ms", C.c_double)]
+
+
 def _f64(a):
     return np.ascontiguousarray(a, dtype=np.float64)
 

@@ -570,6 +570,9 @@ int launch_T(eg_ls* ls) {
   if (ec > epb) ec = epb;
   a.ec = ec;
   const size_t smem = (size_t)ec * elem_bytes;
+  // the default dynamic limit is 48 KB minus the kernel's static shared
+  // memory (11.6 KB in FP64), below the chunk size above
+  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, NT, smem);
   if (per_sm < 1 || nblk <= 0) {
     eg_set_error("persistent GMRES kernel cannot be resident");

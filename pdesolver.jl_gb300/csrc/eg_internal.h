@@ -97,6 +97,10 @@ struct eg_mesh {
                             // between solves (released by eg_newton_release or destroy)
   double* prolong_T;        // device copy of the last prolongation matrix (eg_prolong)
   size_t prolong_T_n;
+  // launch configuration of the element kernels (eg_set_launch_config /
+  // eg_autotune); 0 = the built-in choice
+  int elem_epb;             // elements per CTA
+  int vol_mma;              // weak-form Q^T F on the FP64 tensor cores (mma.sync m8n8k4)
 };
 void eg_newton_ws_free(eg_mesh* m);
 
@@ -107,6 +111,12 @@ void eg_timer_free(eg_mesh* m);
 
 // kernels entry points used across translation units
 int eg_residual_device(eg_mesh* m, const double* q, double* res);
+// the element kernel alone (volume + face lifting from m->fflux), with the
+// mesh's launch configuration
+int eg_launch_element(eg_mesh* m, const double* q, double* res);
+// effective launch shape of the element kernel: elements per CTA, threads,
+// dynamic shared memory; EG_ERR_INVALID if the configuration does not fit
+int eg_element_shape(const eg_mesh* m, int epb, int mma, int* threads, size_t* smem);
 int eg_check_status(eg_mesh* m);
 // phase timers enabled (they take CUDA events from a growing pool)
 bool eg_timing_on(const eg_mesh* m);

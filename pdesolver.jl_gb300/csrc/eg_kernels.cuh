@@ -85,5 +85,5 @@ __device__ __forceinline__ void face_lift_smem(const DevMesh& md, const double* 
 
 DevMesh dev_mesh(const eg_mesh* m);
 int eg_launch_residual(eg_mesh* m, const double* q, double* res);
-int eg_launch_split_element(eg_mesh* m, const double* q, double* res);
+int eg_launch_split_element(eg_mesh* m, const double* q, double* res, int epb);
 int eg_launch_norm(eg_mesh* m, const double* r, int strongres, double* out_dev);

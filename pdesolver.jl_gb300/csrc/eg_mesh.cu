@@ -80,6 +80,40 @@ static void freestream_state(const DevParams& p, int dim, double* sol) {
   }
 }
 
+// the kernels' copy of the physics parameters (reference ParamType fields,
+// types.jl:236-260; E_free from calcFreeStream, common_funcs.jl:312-345)
+static DevParams dev_params(const eg_params& pa) {
+  DevParams p;
+  p.gamma = pa.gamma;
+  p.gamma_1 = pa.gamma - 1;
+  p.Ma = pa.Ma;
+  p.aoa = pa.aoa;
+  p.rho_free = pa.rho_free;
+  p.p_free = pa.p_free;
+  p.E_free = pa.p_free / p.gamma_1 + 0.5 * pa.rho_free * pa.Ma * pa.Ma;
+  p.r_in = pa.vortex_r_in;
+  p.rho_in = pa.vortex_rho_in;
+  p.M_in = pa.vortex_M_in;
+  p.R = 287.058;
+  p.cv = p.R / p.gamma_1;
+  return p;
+}
+
+// Dirichlet state of every boundary face node from the boundary coordinates
+// and each face's boundary condition
+static void boundary_states(const DevParams& p, int dim, int B, int Nf, const int32_t* bc_of_b,
+                            const double* coords_bndry, double* qg) {
+  const int nv = dim + 2;
+  for (int b = 0; b < B; ++b)
+    for (int i = 0; i < Nf; ++i) {
+      double* s = &qg[((size_t)b * Nf + i) * nv];
+      if (bc_of_b[b] == EG_BC_VORTEX)
+        vortex_state(p, coords_bndry + ((size_t)b * Nf + i) * dim, s);
+      else
+        freestream_state(p, dim, s);
+    }
+}
+
 static void free_mesh(eg_mesh* m) {
   if (!m) return;
   eg_newton_ws_free(m);
@@ -139,19 +173,8 @@ extern "C" int eg_mesh_create(const eg_mesh_desc* d, const eg_params* params, eg
   m->nv = d->dim + 2;
   m->ndof = (int64_t)m->E * m->Np * m->nv;
   m->params = *params;
-  DevParams& p = m->dp;
-  p.gamma = params->gamma;
-  p.gamma_1 = params->gamma - 1;
-  p.Ma = params->Ma;
-  p.aoa = params->aoa;
-  p.rho_free = params->rho_free;
-  p.p_free = params->p_free;
-  p.E_free = params->p_free / p.gamma_1 + 0.5 * params->rho_free * params->Ma * params->Ma;
-  p.r_in = params->vortex_r_in;
-  p.rho_in = params->vortex_rho_in;
-  p.M_in = params->vortex_M_in;
-  p.R = 287.058;
-  p.cv = p.R / p.gamma_1;
+  m->dp = dev_params(*params);
+  const DevParams& p = m->dp;
 
   const int dim = m->dim, E = m->E, Np = m->Np, Nf = m->Nf, S = m->S, F = m->F, I = m->I,
             B = m->B, nv = m->nv;
@@ -265,14 +288,7 @@ extern "C" int eg_mesh_create(const eg_mesh_desc* d, const eg_params* params, eg
         if (d->interp[((size_t)f * Nf + i) * S + s] != (i == s ? 1.0 : 0.0)) m->sparse_face = 0;
   // Dirichlet states at the boundary face nodes
   std::vector<double> qg((size_t)B * Nf * nv, 0.0);
-  for (int b = 0; b < B; ++b)
-    for (int i = 0; i < Nf; ++i) {
-      double* s = &qg[((size_t)b * Nf + i) * nv];
-      if (bc_of_b[b] == EG_BC_VORTEX)
-        vortex_state(p, d->coords_bndry + ((size_t)b * Nf + i) * dim, s);
-      else
-        freestream_state(p, dim, s);
-    }
+  boundary_states(p, dim, B, Nf, bc_of_b.data(), d->coords_bndry, qg.data());
   std::vector<double> minv((size_t)E * Np);
   for (int e = 0; e < E; ++e)
     for (int j = 0; j < Np; ++j) minv[(size_t)e * Np + j] = d->jac[(size_t)e * Np + j] / d->w[j];
@@ -336,3 +352,43 @@ extern "C" int eg_mesh_destroy(eg_mesh* m) {
 }
 
 extern "C" int64_t eg_mesh_num_dof(const eg_mesh* m) { return m ? m->ndof : -1; }
+
+// New physics parameters on an existing mesh (the reference mutates
+// eqn.params / opts between solves).  The boundary Dirichlet states are
+// re-evaluated from the device copy of the boundary coordinates; the mesh
+// stream is synchronised before and after, so no launch sees a half update.
+extern "C" int eg_mesh_set_params(eg_mesh* m, const eg_params* params) {
+  if (!m || !params) {
+    eg_set_error("eg_mesh_set_params: NULL argument");
+    return EG_ERR_INVALID;
+  }
+  if (params->volume_integral_type != 1 && params->volume_integral_type != 2) {
+    eg_set_error("eg_mesh_set_params: volume_integral_type must be 1 or 2");
+    return EG_ERR_INVALID;
+  }
+  if (m->capturing) {
+    eg_set_error("eg_mesh_set_params: the mesh stream is being captured");
+    return EG_ERR_INVALID;
+  }
+  const int B = m->B, Nf = m->Nf, dim = m->dim;
+  std::vector<int32_t> bc(B);
+  std::vector<double> xb((size_t)B * Nf * dim), qg((size_t)B * Nf * m->nv, 0.0);
+  EG_CUDA(cudaStreamSynchronize(m->stream));
+  if (B > 0) {
+    EG_CUDA(cudaMemcpyAsync(bc.data(), m->bc_of_b, sizeof(int32_t) * B, cudaMemcpyDeviceToHost,
+                            m->stream));
+    EG_CUDA(cudaMemcpyAsync(xb.data(), m->coords_bndry, sizeof(double) * xb.size(),
+                            cudaMemcpyDeviceToHost, m->stream));
+    EG_CUDA(cudaStreamSynchronize(m->stream));
+  }
+  const DevParams p = dev_params(*params);
+  boundary_states(p, dim, B, Nf, bc.data(), xb.data(), qg.data());
+  if (B > 0) {
+    EG_CUDA(cudaMemcpyAsync(m->qg_bndry, qg.data(), sizeof(double) * qg.size(),
+                            cudaMemcpyHostToDevice, m->stream));
+    EG_CUDA(cudaStreamSynchronize(m->stream));
+  }
+  m->params = *params;
+  m->dp = p;
+  return EG_OK;
+}

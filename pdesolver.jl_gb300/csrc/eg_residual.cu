@@ -89,10 +89,64 @@ __global__ void k_face_flux(DevMesh md, const double* __restrict__ q, double* __
   for (int c = 0; c < NV; ++c) out[c] = fl[c];
 }
 
+// Weak-form volume contraction of the CTA's elements on the FP64 tensor
+// cores: R[j][(le, c)] = sum_kk A[j][kk] B[kk][(le, c)] with
+// A = [Q_1^T | ... | Q_DIM^T] (Np x DIM Np, A[j][k Np + i] = Q_k(i, j)) and B
+// the parametric fluxes of the elements stacked by column (B[k Np + i][le NV
+// + c] = F_k,i,c of element le).  Each warp owns 8 x 8 output tiles and runs
+// mma.sync m8n8k4 (FP64) over K in steps of 4; rows, columns and K beyond
+// the problem are zero padding.  Fragment layout of m8n8k4 .f64 (PTX ISA):
+// lane l holds A[l / 4][l % 4], B[l % 4][l / 4] and C[l / 4][2 (l % 4) + {0,1}].
+template <int DIM>
+__device__ __forceinline__ void volume_mma(const double* sQ, const double* sF, double* sres,
+                                           int Np, int nloc) {
+  constexpr int NV = DIM + 2;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  const int K = DIM * Np, Kp = (K + 3) & ~3;
+  const int ncol = nloc * NV;
+  const int mt = (Np + 7) >> 3, nt = (ncol + 7) >> 3;
+  const int gq = lane >> 2, t4 = lane & 3;
+  for (int tile = warp; tile < mt * nt; tile += nwarp) {
+    const int tm = tile % mt, tn = tile / mt;
+    const int row = tm * 8 + gq;          // A row of this lane, C row
+    const int bcol = tn * 8 + gq;         // B column of this lane
+    const bool brow_ok = bcol < ncol;
+    const int ble = brow_ok ? bcol / NV : 0, bc = bcol - ble * NV;
+    const double* Bp = sF + (size_t)ble * DIM * Np * NV + bc;   // + kk * NV
+    const double* Ap = sQ + (size_t)row * Np;                    // + k Np Np + i
+    double c0 = 0.0, c1 = 0.0;
+    for (int k0 = 0; k0 < Kp; k0 += 4) {
+      const int kk = k0 + t4;             // A column / B row of this lane
+      double a = 0.0, b = 0.0;
+      if (kk < K) {
+        const int k = kk / Np, i = kk - k * Np;
+        if (row < Np) a = Ap[(size_t)k * Np * Np + i];
+        if (brow_ok) b = Bp[(size_t)kk * NV];
+      }
+      asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};"
+                   : "+d"(c0), "+d"(c1)
+                   : "d"(a), "d"(b));
+    }
+    const int col0 = tn * 8 + t4 * 2;
+    if (row < Np) {
+      if (col0 < ncol) {
+        const int le = col0 / NV, c = col0 - le * NV;
+        sres[((size_t)le * Np + row) * NV + c] = c0;
+      }
+      if (col0 + 1 < ncol) {
+        const int le = (col0 + 1) / NV, c = col0 + 1 - le * NV;
+        sres[((size_t)le * Np + row) * NV + c] = c1;
+      }
+    }
+  }
+}
+
 // Shared-memory layout of k_element:
 //   Q[dim][Np][Np] | liftS[F][Nf][S] | perm[F][S] (ints, padded) | Fbuf[epb][dim][Np][NV]
 //   | sres[epb][Np][NV]
-template <int DIM>
+// MMA: the volume contraction runs on the FP64 tensor cores (volume_mma);
+// the block is then a whole number of warps.
+template <int DIM, bool MMA>
 __global__ void k_element(DevMesh md, const double* __restrict__ q,
                           const double* __restrict__ fflux, double* __restrict__ res,
                           unsigned int* __restrict__ status, int epb) {
@@ -133,7 +187,9 @@ __global__ void k_element(DevMesh md, const double* __restrict__ q,
     }
   }
   __syncthreads();
-  if (active) {
+  if (MMA) {
+    volume_mma<DIM>(sQ, sF, sres, Np, nloc);
+  } else if (active) {
     double acc[NV];
 #pragma unroll
     for (int c = 0; c < NV; ++c) acc[c] = 0.0;
@@ -265,15 +321,91 @@ DevMesh dev_mesh(const eg_mesh* m) {
   return d;
 }
 
-int element_launch_shape(const eg_mesh* m, int* epb, int* threads, size_t* smem) {
-  const int nv = m->nv;
+// Launch shape of the element kernel with `epb` elements per CTA (0: the
+// built-in choice, 256 / Np weak form; the split form as many as fit 160 KB).
+// Weak form: one thread per (element, node), rounded up to whole warps with
+// the tensor-core contraction.  Split form: the pair table of every element
+// in shared memory.
+int eg_element_shape(const eg_mesh* m, int epb, int mma, int* threads, size_t* smem) {
+  const int nv = m->nv, Np = m->Np;
+  const size_t common = sizeof(double) * ((size_t)m->dim * Np * Np + (size_t)m->F * m->Nf * m->S +
+                                          (size_t)(m->F * m->S + 1) / 2);
+  if (m->params.volume_integral_type == 2) {
+    if (mma) {
+      eg_set_error("launch config: the split form has no tensor-core contraction");
+      return EG_ERR_INVALID;
+    }
+    const int P = Np * (Np - 1) / 2;
+    auto smem_of = [&](int e) {
+      return common + sizeof(double) * ((size_t)e * Np * nv + (size_t)e * P * nv +
+                                        (size_t)e * Np * nv + (size_t)e * Np * 7) +
+             sizeof(short2) * (size_t)P;
+    };
+    if (epb <= 0) {
+      epb = 256 / Np;
+      if (epb < 1) epb = 1;
+      while (epb > 1 && smem_of(epb) > 160 * 1024) --epb;
+    }
+    *smem = smem_of(epb);
+    *threads = epb * Np;
+  } else {
+    if (epb <= 0) {
+      epb = 256 / Np;
+      if (epb < 1) epb = 1;
+    }
+    *smem = common + sizeof(double) * ((size_t)epb * m->dim * Np * nv + (size_t)epb * Np * nv);
+    *threads = mma ? (epb * Np + 31) / 32 * 32 : epb * Np;
+  }
+  if (*threads > 1024 || *smem > 200 * 1024) {
+    eg_set_error("launch config: %d elements per CTA need %d threads and %zu B of shared memory",
+                 epb, *threads, *smem);
+    return EG_ERR_INVALID;
+  }
+  return EG_OK;
+}
+
+static int effective_epb(const eg_mesh* m) {
+  if (m->elem_epb > 0) return m->elem_epb;
   int e = 256 / m->Np;
   if (e < 1) e = 1;
-  *epb = e;
-  *threads = e * m->Np;
-  *smem = sizeof(double) * ((size_t)m->dim * m->Np * m->Np + (size_t)m->F * m->Nf * m->S +
-                            (size_t)(m->F * m->S + 1) / 2 + (size_t)e * m->dim * m->Np * nv +
-                            (size_t)e * m->Np * nv);
+  if (m->params.volume_integral_type == 2) {
+    int threads;
+    size_t smem;
+    while (e > 1 && (eg_element_shape(m, e, 0, &threads, &smem) != EG_OK || smem > 160 * 1024)) --e;
+  }
+  return e;
+}
+
+int eg_launch_element(eg_mesh* m, const double* q, double* res) {
+  if (m->params.volume_integral_type == 2) return eg_launch_split_element(m, q, res, effective_epb(m));
+  DevMesh md = dev_mesh(m);
+  const int epb = effective_epb(m);
+  const bool mma = m->vol_mma != 0;
+  int threads;
+  size_t smem;
+  int st = eg_element_shape(m, epb, mma, &threads, &smem);
+  if (st != EG_OK) return st;
+  const int blocks = (m->E + epb - 1) / epb;
+  // once per process (thread-safe static initialisation)
+  static const bool attr_set = [] {
+    cudaFuncSetAttribute(k_element<2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_element<3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_element<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_element<3, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    return true;
+  }();
+  (void)attr_set;
+  if (m->dim == 2) {
+    if (mma)
+      k_element<2, true><<<blocks, threads, smem, m->stream>>>(md, q, m->fflux, res, m->status, epb);
+    else
+      k_element<2, false><<<blocks, threads, smem, m->stream>>>(md, q, m->fflux, res, m->status, epb);
+  } else {
+    if (mma)
+      k_element<3, true><<<blocks, threads, smem, m->stream>>>(md, q, m->fflux, res, m->status, epb);
+    else
+      k_element<3, false><<<blocks, threads, smem, m->stream>>>(md, q, m->fflux, res, m->status, epb);
+  }
   return EG_OK;
 }
 
@@ -290,28 +422,9 @@ int eg_launch_residual(eg_mesh* m, const double* q, double* res) {
     eg_phase_end(m, EG_PHASE_FACE, 1);
   }
   eg_phase_begin(m, EG_PHASE_ELEMENT);
-  if (m->params.volume_integral_type == 2) {
-    int st = eg_launch_split_element(m, q, res);
-    eg_phase_end(m, EG_PHASE_ELEMENT, 1);
-    return st;
-  }
-  int epb, threads;
-  size_t smem;
-  element_launch_shape(m, &epb, &threads, &smem);
-  const int blocks = (m->E + epb - 1) / epb;
-  // once per process (thread-safe static initialisation)
-  static const bool attr_set = [] {
-    cudaFuncSetAttribute(k_element<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(k_element<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    return true;
-  }();
-  (void)attr_set;
-  if (m->dim == 2)
-    k_element<2><<<blocks, threads, smem, m->stream>>>(md, q, m->fflux, res, m->status, epb);
-  else
-    k_element<3><<<blocks, threads, smem, m->stream>>>(md, q, m->fflux, res, m->status, epb);
+  const int st = eg_launch_element(m, q, res);
   eg_phase_end(m, EG_PHASE_ELEMENT, 1);
-  return EG_OK;
+  return st;
 }
 
 int eg_launch_norm(eg_mesh* m, const double* r, int strongres, double* out_dev) {

@@ -126,21 +126,12 @@ __global__ void k_split_element(DevMesh md, const double* __restrict__ q,
 
 }  // namespace
 
-int eg_launch_split_element(eg_mesh* m, const double* q, double* res) {
+int eg_launch_split_element(eg_mesh* m, const double* q, double* res, int epb) {
   DevMesh md = dev_mesh(m);
-  const int Np = m->Np, nv = m->nv;
-  const int P = Np * (Np - 1) / 2;
-  int epb = 256 / Np;
-  if (epb < 1) epb = 1;
-  auto smem_of = [&](int e) {
-    return sizeof(double) * ((size_t)m->dim * Np * Np + (size_t)m->F * m->Nf * m->S +
-                             (size_t)(m->F * m->S + 1) / 2 + (size_t)e * Np * nv +
-                             (size_t)e * P * nv + (size_t)e * Np * nv + (size_t)e * Np * 7) +
-           sizeof(short2) * (size_t)P;
-  };
-  while (epb > 1 && smem_of(epb) > 160 * 1024) --epb;
-  const size_t smem = smem_of(epb);
-  const int threads = epb * Np;
+  int threads;
+  size_t smem;
+  const int st = eg_element_shape(m, epb, 0, &threads, &smem);
+  if (st != EG_OK) return st;
   const int blocks = (m->E + epb - 1) / epb;
   // once per process (thread-safe static initialisation)
   static const bool attr_set = [] {

@@ -82,6 +82,12 @@ def _declare(lib):
                            C.POINTER(Rk4Stats)]
     lib.eg_rk4_static.argtypes = lib.eg_rk4.argtypes
     lib.eg_newton_release.argtypes = [vp]
+    lib.eg_mesh_set_params.argtypes = [vp, C.POINTER(abi.EgParams)]
+    lib.eg_estimate_mem.argtypes = [C.POINTER(abi.EgMemQuery), C.POINTER(abi.EgMemEstimate)]
+    lib.eg_set_launch_config.argtypes = [vp, C.POINTER(abi.EgLaunchConfig)]
+    lib.eg_get_launch_config.argtypes = [vp, C.POINTER(abi.EgLaunchConfig)]
+    lib.eg_autotune.argtypes = [vp, vp, C.c_int32, C.POINTER(abi.EgTuneEntry), C.c_int32,
+                                C.POINTER(C.c_int32)]
 
 
 class LsStats(C.Structure):
@@ -145,6 +151,25 @@ def params_from_opts(opts: dict) -> abi.EgParams:
         p_free=opts.get("p_free"))
 
 
+def mem_query(mesh, precision=None, restart=30, host_state=False, prolong_from=None):
+    """eg_mem_query of a host Mesh: precision None (mesh and state only),
+    0 (FP64 Newton) or 1 (mixed); prolong_from = the coarser level's operator."""
+    op = mesh.sbp
+    return abi.EgMemQuery(
+        mesh.dim, mesh.numEl, op.numnodes, op.numfacenodes, op.stencilsize, mesh.numInterfaces,
+        mesh.numBoundaryFaces, mesh.nbrperm.shape[0], -1 if precision is None else int(precision),
+        int(restart), int(bool(host_state)), 0 if prolong_from is None else prolong_from.numnodes)
+
+
+def estimate_mem(mesh, precision=None, restart=30, host_state=False, prolong_from=None):
+    """Device bytes the library takes for `mesh` (and, with a precision, its
+    Newton work objects) plus the caller's q and res (reference estimateMem.jl)."""
+    out = abi.EgMemEstimate()
+    qy = mem_query(mesh, precision, restart, host_state, prolong_from)
+    check(library().eg_estimate_mem(C.byref(qy), C.byref(out)))
+    return out
+
+
 class GPUMesh:
     """Owner of one eg_mesh (device copy of mesh + operator + parameters)."""
 
@@ -158,6 +183,35 @@ class GPUMesh:
         check(self.lib.eg_mesh_create(C.byref(self.desc.desc), C.byref(self.params), C.byref(h)))
         self.handle = h
         self.ndof = int(self.lib.eg_mesh_num_dof(h))
+
+    def set_params(self, opts: dict):
+        """new physics options (Mach numbers, fluxes) for this device mesh; the
+        boundary Dirichlet states are re-evaluated on the host and uploaded."""
+        params = params_from_opts(opts)
+        check(self.lib.eg_mesh_set_params(self.handle, C.byref(params)))
+        self.params = params
+        self.opts = dict(opts)
+
+    def set_launch_config(self, elements_per_cta=0, volume_mma=False):
+        """element-kernel launch shape: elements per CTA (0: built-in) and the
+        FP64 tensor-core volume contraction (weak form only)."""
+        c = abi.EgLaunchConfig(int(elements_per_cta), int(bool(volume_mma)))
+        check(self.lib.eg_set_launch_config(self.handle, C.byref(c)))
+
+    def launch_config(self):
+        c = abi.EgLaunchConfig()
+        check(self.lib.eg_get_launch_config(self.handle, C.byref(c)))
+        return {"elements_per_cta": c.elements_per_cta, "volume_mma": bool(c.volume_mma)}
+
+    def autotune(self, q_dev, reps=20):
+        """time every admissible element-kernel configuration on the device
+        state q_dev and keep the fastest; returns [(config dict, ms)]."""
+        table = (abi.EgTuneEntry * 64)()
+        n = C.c_int32(0)
+        check(self.lib.eg_autotune(self.handle, self._dev(q_dev, self.ndof, "torch.float64"),
+                                   int(reps), table, 64, C.byref(n)))
+        return [({"elements_per_cta": t.config.elements_per_cta,
+                  "volume_mma": bool(t.config.volume_mma)}, t.ms) for t in table[:n.value]]
 
     def close(self):
         if getattr(self, "handle", None):

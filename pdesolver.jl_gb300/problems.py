@@ -115,3 +115,85 @@ def config4_problem(spec):
         if q0 is None:
             q0 = q
     return levels, q0
+
+
+def cube_problem(spec, warp=0.05, warp_seed=3):
+    """A 3-D steady solve: the warped unit cube of n^3 hexes -> 6 n^3 tets,
+    SBP diagonal-E tets of degree p (levels p = 1, then p when p > 1), Roe
+    faces, weak-form volume terms, free-stream Dirichlet data at Mach M_in,
+    started from that free stream times (1 + U(-0.01, 0.01)) with the spec's
+    seed.  Returns ([(mesh, opts)] per level, initial state of level 0)."""
+    ps = (1,) if spec["p"] == 1 else (1, spec["p"])
+    levels, q0 = [], None
+    M = spec["M_in"]
+    for p in ps:
+        op = _sbp.get_operator(3, "diage", p)
+        ms = _mesh.cube(op, spec["n"], warp=warp, seed=warp_seed, bc=_mesh.BC_FREESTREAM)
+        opts = {"gamma": 1.4, "Ma": M, "aoa": 0.0, "Flux_name": "RoeFlux",
+                "volume_integral_type": 1}
+        levels.append((ms, opts))
+        if q0 is None:
+            rng = np.random.default_rng(spec["seed"])
+            q = free_stream(3, ms.coords.shape[:2], Ma=M)
+            q0 = np.ascontiguousarray(q * (1.0 + rng.uniform(-0.01, 0.01, size=q.shape)))
+    return levels, q0
+
+
+def config5_specs(count=2000, seed=6, frac_3d=0.2):
+    """Serving stream: `count` requests, a fraction `frac_3d` of them 3-D
+    warped cubes (n ~ U{8..24}, p ~ U{1, 2}, Mach ~ U(0.3, 0.7)), the rest
+    drawn from the batched 2-D distribution (config4_specs).  Each spec has
+    "dim" and the unit-rate exponential inter-arrival gap "gap" (the stream's
+    arrival times are cumsum(gap) / rate for the chosen rate)."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for _ in range(count):
+        if rng.uniform() < frac_3d:
+            sp = {"dim": 3, "n": int(rng.integers(8, 25)), "p": int(rng.integers(1, 3)),
+                  "M_in": float(rng.uniform(0.3, 0.7))}
+        else:
+            n = int(round(np.exp(rng.uniform(np.log(8.0), np.log(96.0)))))
+            sp = {"dim": 2, "n": n, "p": int(rng.integers(1, 5)), "M_in": float(rng.uniform(0.3, 0.7))}
+        sp["seed"] = int(rng.integers(0, 2**31 - 1))
+        sp["gap"] = float(rng.exponential(1.0))
+        specs.append(sp)
+    return specs
+
+
+def request_meshes(key):
+    """Host meshes of the continuation levels of a geometry key (dim, n, p):
+    the annulus n x n with SBP-Gamma (2-D, vortex data) or the warped cube
+    n^3 x 6 with diagonal-E tets (3-D, free-stream data), degrees 1 and p."""
+    dim, n, p = key
+    out = []
+    for pl in ((1,) if p == 1 else (1, p)):
+        if dim == 2:
+            out.append(_mesh.annulus(_sbp.get_operator(2, "gamma", pl), n, n, bc=_mesh.BC_VORTEX))
+        else:
+            out.append(_mesh.cube(_sbp.get_operator(3, "diage", pl), n, warp=0.05, seed=3,
+                                  bc=_mesh.BC_FREESTREAM))
+    return out
+
+
+def request_problem(spec, meshes=None):
+    """([(mesh, opts)] per continuation level, initial state) of a 2-D
+    (as config4_problem) or 3-D (as cube_problem) serving request; `meshes`
+    (from request_meshes) skips building the geometry."""
+    dim = spec.get("dim", 2)
+    if meshes is None:
+        meshes = request_meshes(geometry_key(spec))
+    M = spec["M_in"]
+    opts = {"gamma": 1.4, "Ma": M, "aoa": 0.0, "Flux_name": "RoeFlux", "volume_integral_type": 1}
+    if dim == 2:
+        opts["vortex_M_in"] = M
+    ms0 = meshes[0]
+    rng = np.random.default_rng(spec["seed"])
+    q = free_stream(dim, ms0.coords.shape[:2], Ma=M)
+    q0 = np.ascontiguousarray(q * (1.0 + rng.uniform(-0.01, 0.01, size=q.shape)))
+    return [(ms, dict(opts)) for ms in meshes], q0
+
+
+def geometry_key(spec):
+    """Requests with equal keys share meshes (the same elements, operators
+    and boundary tags); they differ only in Mach number and initial state."""
+    return (spec.get("dim", 2), spec["n"], spec["p"])

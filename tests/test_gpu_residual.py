@@ -114,3 +114,46 @@ def test_norm_matches_oracle(gpu_lib, oracle):
     for strong in (0, 1):
         ref = oracle.oracle_calc_norm(C.byref(g.desc.desc), abi.dptr(r), strong)
         assert abs(g.calc_norm(r, strong) - ref) <= 1e-13 * ref
+
+
+@pytest.mark.parametrize("fam,p", [("omega", 2), ("gamma", 3), ("gamma", 4)])
+def test_residual_every_launch_config(gpu_lib, oracle, fam, p):
+    """every elements-per-CTA choice, with the CUDA-core and the FP64
+    tensor-core (mma.sync m8n8k4) volume contraction, meets the residual bar."""
+    ms, opts, q = problems.config1(n=7, p=p, family=fam, seed=300 + p)
+    g = eulergpu.GPUMesh(ms, opts)
+    ref = oracle_residual(oracle, g.desc, g.params, q)
+    np_ = ms.sbp.numnodes
+    for mma in (False, True):
+        epb = 1
+        while (epb - 1) * np_ < 1024 and epb <= 128:
+            g.set_launch_config(epb, mma)
+            res = g.eval_residual(q, np.zeros_like(q))
+            assert rel_err(res, ref) <= TOL, (epb, mma, rel_err(res, ref))
+            epb *= 2
+
+
+def test_split_form_launch_configs(gpu_lib, oracle):
+    ms, opts, q = problems.config3(n=3, p=2, seed=41)
+    g = eulergpu.GPUMesh(ms, opts)
+    ref = oracle_residual(oracle, g.desc, g.params, q)
+    for epb in (1, 2, 4, 8):
+        g.set_launch_config(epb, False)
+        res = g.eval_residual(q, np.zeros_like(q))
+        assert rel_err(res, ref) <= TOL, epb
+    with pytest.raises(eulergpu.EulerGPUError):
+        g.set_launch_config(2, True)       # no tensor-core split form
+    with pytest.raises(eulergpu.EulerGPUError):
+        g.set_launch_config(512, False)    # more threads than a CTA holds
+
+
+def test_autotune_keeps_the_fastest_and_stays_exact(gpu_lib, oracle):
+    import torch
+    ms, opts, q = problems.config2(n=32, p=3)
+    g = eulergpu.GPUMesh(ms, opts)
+    table = g.autotune(torch.from_numpy(q).cuda(), reps=5)
+    assert len(table) >= 4 and any(c["volume_mma"] for c, _ in table)
+    best = min(table, key=lambda t: t[1])[0]
+    assert g.launch_config() == best
+    ref = oracle_residual(oracle, g.desc, g.params, q)
+    assert rel_err(g.eval_residual(q, np.zeros_like(q)), ref) <= TOL

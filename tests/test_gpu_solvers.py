@@ -159,3 +159,16 @@ def test_functional_matches_oracle(gpu_lib, oracle):
     for grp in range(len(ms.bc_types)):
         fo = oracle.oracle_functional_pressure(C.byref(g.desc.desc), C.byref(g.params), abi.dptr(q), grp)
         assert abs(g.functional_pressure(q, grp) - fo) <= 1e-13 * abs(fo)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_newton_single_block_gmres_with_large_chunk(gpu_lib, precision):
+    """a small p=1 system (16x16 annulus, 512 elements) runs its GMRES as one
+    persistent block whose element chunk takes 40 KB of dynamic shared memory
+    next to the kernel's static shared memory (FP64: above the default 48 KB
+    per-block limit unless the kernel opts in)."""
+    ms, opts, q0 = problems.config2(n=16, p=1)
+    g = eulergpu.GPUMesh(ms, opts)
+    q = q0.copy()
+    st = g.newton(q, NEWTON_OPTS, precision=precision)
+    assert st.converged == 1 and st.res_norm < 1e-10
