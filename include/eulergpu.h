@@ -337,6 +337,10 @@ typedef struct {
   int32_t host_state;         /* 1: Newton is given host q (a staging vector) */
   int32_t prolong_from_nodes; /* Np of the coarser level this mesh is
                                  prolonged from (eg_prolong), 0: none         */
+  int32_t face_diagonal;      /* 1: the face interpolation is the identity
+                                 (face nodes are volume nodes, as for the
+                                 diagonal-E operators); the coupling blocks
+                                 then keep one nv x nv block per stencil node */
 } eg_mem_query;
 
 typedef struct {

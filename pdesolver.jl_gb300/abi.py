@@ -74,7 +74,7 @@ class EgMemQuery(C.Structure):
     _fields_ = [(k, C.c_int32) for k in (
         "dim", "num_el", "nodes_per_el", "nodes_per_face", "stencil_size", "num_interfaces",
         "num_bndry", "num_orient", "newton_precision", "gmres_restart", "host_state",
-        "prolong_from_nodes")]
+        "prolong_from_nodes", "face_diagonal")]
 
 
 class EgMemEstimate(C.Structure):

@@ -59,7 +59,8 @@ struct CoopArgs {
   DevMesh md;
   const T* inv;      // [E][n][n] block inverses (column-major)
   const T* diag;     // [E][n][n] element blocks of J (column-major)
-  const T* cpl;      // [I][2][nb][nb] coupling blocks (row-major)
+  const T* cpl;      // [I][2][nb][nb] coupling blocks (row-major), or
+                     // [I][2][S][NV][NV] when md.sparse_face (face-diagonal)
   const int* spos;   // [F][Np]
   const int* fside;  // [E][F] coupling block of each element face, or -1
   T* cfs;            // [I][2][nb] coupling products of each face side
@@ -109,6 +110,24 @@ __device__ void face_push(const CoopArgs<T>& a, const T* __restrict__ sZ, const 
     const int tgt = fs ^ 1;
     const T* zs = sZ + (size_t)le * n;
     const int* pf = sPerm + f * S;
+    if (a.md.sparse_face) {
+      // face-diagonal coupling [I][2][S][NV][NV]: row (s, r) of the
+      // neighbour's side couples to this element's node facing s only
+      const int o = a.md.ifaces[5 * (tgt >> 1) + 4];
+      const int* facing = (tgt & 1) ? a.md.nbrinv + o * a.md.Nf : a.md.nbrperm + o * a.md.Nf;
+      for (int i = gl; i < nb; i += G) {
+        const int s = i / NV;
+        const T* Cr = a.cpl + (size_t)tgt * nb * NV + (size_t)i * NV;
+        const T* zz = zs + pf[facing[s]] * NV;
+        T c[NV];
+        load_row_piece<NV, T>(Cr, c);
+        T acc = T(0);
+#pragma unroll
+        for (int b = 0; b < NV; ++b) acc += c[b] * zz[b];
+        cfs[(size_t)tgt * nb + i] = acc;
+      }
+      continue;
+    }
     for (int i = gl; i < nb; i += G) {
       const T* Cr = a.cpl + ((size_t)tgt * nb + i) * nb;
       T acc0 = T(0), acc1 = T(0);
@@ -550,6 +569,7 @@ int launch_T(eg_ls* ls) {
 #define EG_CASE(NBV) \
   case NBV: fn = m->dim == 2 ? (void*)k_gmres_coop<2, NBV, T> : (void*)k_gmres_coop<3, NBV, T>; break;
     EG_CASE(12) EG_CASE(24) EG_CASE(28) EG_CASE(40) EG_CASE(48) EG_CASE(60) EG_CASE(72) EG_CASE(30)
+    EG_CASE(115)
 #undef EG_CASE
     default: fn = m->dim == 2 ? (void*)k_gmres_coop<2, 0, T> : (void*)k_gmres_coop<3, 0, T>;
   }

@@ -115,7 +115,9 @@ __global__ void k_elem_jac(DevMesh md, const double* __restrict__ q, const T* __
   const int n = Np * NV;
   T* sA = reinterpret_cast<T*>(smraw);               // [DIM][Np][NV][NV]
   T* sB = sA + (size_t)DIM * Np * NV * NV;            // [n][n] col-major
+  T* sQ = sB + (size_t)n * n;                         // [DIM][Np][Np] = Q
   const int e = blockIdx.x;
+  for (int t = threadIdx.x; t < DIM * Np * Np; t += blockDim.x) sQ[t] = T(md.Q[t]);
   const Gas g{md.gamma, md.gamma_1};
   // flux Jacobians A_k(q_m) = dF_k/dq at node m, direction dxidx[.][k]
   for (int t = threadIdx.x; t < Np * DIM; t += blockDim.x) {
@@ -147,7 +149,7 @@ __global__ void k_elem_jac(DevMesh md, const double* __restrict__ q, const T* __
     T acc = T(0);
 #pragma unroll
     for (int k = 0; k < DIM; ++k)
-      acc += T(md.Q[((size_t)k * Np + j) * Np + m]) * sA[(((size_t)k * Np + m) * NV + a) * NV + b];
+      acc += sQ[((size_t)k * Np + j) * Np + m] * sA[(((size_t)k * Np + m) * NV + a) * NV + b];
     sB[t] = acc;
   }
   __syncthreads();
@@ -158,6 +160,20 @@ __global__ void k_elem_jac(DevMesh md, const double* __restrict__ q, const T* __
     const int sideoff = ef.side ? NV * NV : 0;  // dF/dq of this element's state
     const T sgn = ef.side ? T(1) : T(-1);
     const int* nb = md.nbrperm + ef.orient * Nf;
+    if (md.sparse_face) {
+      // interp = identity: only stencil node s with itself, through the face
+      // node i that sees it, acc = wface[s] dF_i (the dense sum's one term)
+      for (int t = threadIdx.x; t < S * NV * NV; t += blockDim.x) {
+        const int ab = t % (NV * NV), s = t / (NV * NV);
+        const int a = ab / NV, b = ab - a * NV;
+        const int i = ef.side ? md.nbrinv[ef.orient * Nf + s] : s;
+        const T acc = T(md.wface[s]) * dFs[(size_t)i * 2 * NV * NV + sideoff + a * NV + b];
+        const int node = md.perm[f * S + s] * NV;
+        sB[(size_t)(node + b) * n + node + a] += sgn * acc;
+      }
+      __syncthreads();
+      continue;
+    }
     for (int t = threadIdx.x; t < S * S * NV * NV; t += blockDim.x) {
       const int ab = t % (NV * NV), ss = t / (NV * NV);
       const int s = ss / S, sp = ss - s * S;        // row stencil s, column stencil s'
@@ -183,6 +199,34 @@ __global__ void k_elem_jac(DevMesh md, const double* __restrict__ q, const T* __
 // contiguous read: cpl[nI][side][row = s*NV+a][col = s'*NV+b]:
 //   side 0: rows elementL stencil, cols elementR stencil, from dF/dqR, sign -
 //   side 1: rows elementR stencil, cols elementL stencil, from dF/dqL, sign +
+// Face-diagonal operators (face nodes are volume nodes) keep only the
+// nonzero NV x NV block of each row stencil node: cpl[nI][side][s][a][b];
+// row node s of side 0 couples to elementR's node nbrperm[o][s], row node s
+// of side 1 to elementL's node nbrinv[o][s] (the one face node joining them).
+template <int DIM, typename T>
+__global__ void k_couple_jac_diag(DevMesh md, const T* __restrict__ dF, T* __restrict__ cpl) {
+  constexpr int NV = DIM + 2;
+  const int Nf = md.Nf, S = md.S;
+  const int64_t per = 2LL * S * NV * NV;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= per * md.I) return;
+  const int nI = (int)(t / per);
+  const int rem = (int)(t - (int64_t)nI * per);
+  const int side = rem / (S * NV * NV);
+  const int sab = rem - side * S * NV * NV;
+  const int s = sab / (NV * NV), ab = sab - s * NV * NV;
+  const int o = md.ifaces[5 * nI + 4];
+  const T* dFs = dF + (size_t)nI * Nf * 2 * NV * NV;
+  // the dense sum over face nodes has one nonzero term: wface[s] dF at the
+  // face node i that sees row node s (side 0: i = s; side 1: i = nbrinv[s])
+  if (side == 0) {
+    cpl[t] = -(T(md.wface[s]) * dFs[(size_t)s * 2 * NV * NV + NV * NV + ab]);
+  } else {
+    const int i = md.nbrinv[o * Nf + s];
+    cpl[t] = T(md.wface[s]) * dFs[(size_t)i * 2 * NV * NV + ab];
+  }
+}
+
 template <int DIM, typename T>
 __global__ void k_couple_jac(DevMesh md, const T* __restrict__ dF, T* __restrict__ cpl) {
   constexpr int NV = DIM + 2;
@@ -230,7 +274,8 @@ int launch_jac(eg_lo* lo, const double* q) {
   T* cpl = reinterpret_cast<T*>(lo->cpl);
   const int nslot = (m->I + m->B) * m->Nf;
   const int n = m->Np * m->nv;
-  const size_t smem = sizeof(T) * ((size_t)m->dim * m->Np * m->nv * m->nv + (size_t)n * n);
+  const size_t smem = sizeof(T) * ((size_t)m->dim * m->Np * m->nv * m->nv + (size_t)n * n +
+                                   (size_t)m->dim * m->Np * m->Np);
   eg_phase_begin(m, EG_PHASE_OTHER);
   if (m->dim == 2) {
     k_face_jac<2, T><<<(nslot + 127) / 128, 128, 0, m->stream>>>(md, q, dF);
@@ -241,13 +286,19 @@ int launch_jac(eg_lo* lo, const double* q) {
     cudaFuncSetAttribute(k_elem_jac<3, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     k_elem_jac<3, T><<<m->E, 256, smem, m->stream>>>(md, q, dF, diag);
   }
-  const int64_t ncpl = 2LL * (m->S * m->nv) * (m->S * m->nv) * m->I;
+  const int64_t ncpl = (int64_t)eg_lo_coupling_size(lo);
   if (ncpl > 0) {
     const int blocks = (int)((ncpl + 255) / 256);
-    if (m->dim == 2)
+    if (lo->cpl_sparse) {
+      if (m->dim == 2)
+        k_couple_jac_diag<2, T><<<blocks, 256, 0, m->stream>>>(md, dF, cpl);
+      else
+        k_couple_jac_diag<3, T><<<blocks, 256, 0, m->stream>>>(md, dF, cpl);
+    } else if (m->dim == 2) {
       k_couple_jac<2, T><<<blocks, 256, 0, m->stream>>>(md, dF, cpl);
-    else
+    } else {
       k_couple_jac<3, T><<<blocks, 256, 0, m->stream>>>(md, dF, cpl);
+    }
   }
   eg_phase_end(m, EG_PHASE_OTHER, ncpl > 0 ? 3 : 2);
   return EG_OK;
@@ -258,6 +309,7 @@ int launch_jac(eg_lo* lo, const double* q) {
 int eg_jacobian_launch(eg_lo* lo, const double* q) {
   const size_t smem_needed = (lo->prec == EG_F64 ? 8 : 4) *
                              ((size_t)lo->mesh->dim * lo->mesh->Np * lo->mesh->nv * lo->mesh->nv +
+                              (size_t)lo->mesh->dim * lo->mesh->Np * lo->mesh->Np +
                               (size_t)lo->n * lo->n);
   if (smem_needed > 200 * 1024) {
     eg_set_error("evalJacobian: element block of %d unknowns exceeds shared memory", lo->n);

@@ -6,6 +6,10 @@
 // Face-coupling part of row r of element e: sum over the element's interface
 // faces whose stencil holds row r's node of C (coupling block) x (neighbour's
 // stencil values).
+// With a face-diagonal operator (md.sparse_face) the coupling storage is
+// [I][2][S][NV][NV]: row stencil node s of a side couples only to the
+// neighbour's stencil node facing it, nbrperm[o][s] from side 0 (elementL)
+// and nbrinv[o][s] from side 1.
 template <int DIM, typename T>
 __device__ __forceinline__ T coupling_row(const DevMesh& md, const T* __restrict__ cpl,
                                           const int* __restrict__ spos, const T* __restrict__ x,
@@ -24,9 +28,18 @@ __device__ __forceinline__ T coupling_row(const DevMesh& md, const T* __restrict
     const int* itf = md.ifaces + 5 * ef.slot;
     const int en = ef.side ? itf[0] : itf[1];
     const int fn = ef.side ? itf[2] : itf[3];
+    const T* xn = x + (size_t)en * n;
+    if (md.sparse_face) {
+      const int o = itf[4];
+      const int sp = ef.side ? md.nbrinv[o * md.Nf + s] : md.nbrperm[o * md.Nf + s];
+      const T* C = cpl + ((((size_t)ef.slot * 2 + ef.side) * S + s) * NV + a) * NV;
+      const T* xs = xn + md.perm[fn * S + sp] * NV;
+#pragma unroll
+      for (int b = 0; b < NV; ++b) acc += C[b] * xs[b];
+      continue;
+    }
     // row (s, a) of the row-major coupling block: nb contiguous values
     const T* C = cpl + (((size_t)ef.slot * 2 + ef.side) * nb + s * NV + a) * nb;
-    const T* xn = x + (size_t)en * n;
     for (int sp = 0; sp < S; ++sp) {
       const T* xs = xn + md.perm[fn * S + sp] * NV;
 #pragma unroll

@@ -9,7 +9,11 @@ struct eg_lo {
   int n;           // Np * nv: element block size
   int nb;          // S * nv: coupling block size
   void* diag;      // [E][n][n] column-major element blocks
-  void* cpl;       // [I][2][nb][nb] column-major coupling blocks
+  void* cpl;       // [I][2][nb][nb] row-major coupling blocks; face-diagonal
+                   // (cpl_sparse): [I][2][S][nv][nv], see eg_lo_coupling_size
+  int cpl_sparse;  // the face operator is the identity on the stencil (face
+                   // nodes are volume nodes): row stencil node s couples only
+                   // to the neighbour's node facing it
   void* dF;        // [(I+B)][Nf][2][nv][nv] point flux Jacobians
   int32_t* spos;   // [F][Np]: stencil position of node j on face f, or -1
   int32_t* fside;  // [E][F]: coupling block (slot * 2 + side) of face f of e, or -1
@@ -70,6 +74,8 @@ int eg_jacobian_launch(eg_lo* lo, const double* q);
 int eg_lo_apply_T(eg_lo* lo, const void* x, void* y, const int* done = nullptr);
 // w = v + C z: the preconditioned operator J M^-1 v with z = M^-1 v, using the
 // coupling blocks only (the element blocks times their inverses are I)
+// values of the coupling storage: I*2*nb*nb, or I*2*S*nv*nv when face-diagonal
+size_t eg_lo_coupling_size(const eg_lo* lo);
 int eg_cpl_apply_T(eg_lo* lo, const void* v, const void* z, void* w, const int* done = nullptr);
 // y = M^-1 x in the operator precision
 int eg_pc_apply_T(eg_pc* pc, const void* x, void* y, const int* done = nullptr);

@@ -11,6 +11,7 @@
 // path, FP32 accumulation).
 #include <cmath>
 #include <cstring>
+#include <algorithm>
 #include <vector>
 
 #include "eg_internal.h"
@@ -334,20 +335,188 @@ int pcapply_T(eg_pc* pc, const T* x, T* y, const int* done = nullptr) {
   return EG_OK;
 }
 
+// Register-tiled Gauss-Jordan inversion for blocks of 33..128 unknowns, one
+// CTA of 256 threads (8 warps) per element block.  Thread (lane, warp) keeps
+// rows lane + 32 r (r < MR) and columns warp + 8 c (c < MC) in registers.
+// Partial pivoting is implicit: the pivot of column k is the unused row p of
+// largest |A[p][k]| (ties: lowest row), found by one warp with shuffles; row p
+// is scaled in place and eliminated from the others, so no rows move.  Row p
+// is read by every warp from its own lane p % 32 (shuffles), column k goes
+// through a double-buffered shared array, so one barrier per column suffices.
+// With S the in-place result and perm[k] the pivot row of column k,
+// A^-1[r][c] = S[perm[r]][q] where perm[q] = c.
+// register row r (warp-uniform) of a thread's tile, through branches on the
+// uniform index so that only one copy executes (no per-element selects)
+template <typename T, int MR, int MC>
+__device__ __forceinline__ void tile_row_shfl(const T (&a)[MR][MC], int r, int src_lane, T scale,
+                                              T (&out)[MC]) {
+#pragma unroll
+  for (int rr = 0; rr < MR; ++rr)
+    if (rr == r) {
+#pragma unroll
+      for (int c = 0; c < MC; ++c) out[c] = __shfl_sync(0xffffffffu, a[rr][c], src_lane) * scale;
+    }
+}
+
+template <typename T, int MR, int MC>
+__global__ void __launch_bounds__(256) k_block_inverse_reg(const T* __restrict__ blocks,
+                                                           T* __restrict__ inv, int n,
+                                                           unsigned int* __restrict__ status) {
+  extern __shared__ unsigned char smraw[];
+  T* S = reinterpret_cast<T*>(smraw);                      // [n][n] column-major, at the end
+  T* colk = S + (size_t)n * n;                             // [2][32 MR] column k
+  int* sp = reinterpret_cast<int*>(colk + 2 * 32 * MR);    // [2] pivot row
+  int* perm = sp + 2;                                      // [n]
+  int* iperm = perm + n;                                   // [n]
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const T* src = blocks + (size_t)blockIdx.x * n * n;
+  T a[MR][MC];
+  unsigned used = 0;  // bit r: row lane + 32 r is a pivot row already (or beyond n)
+#pragma unroll
+  for (int r = 0; r < MR; ++r) {
+    const int i = lane + 32 * r;
+    if (i >= n) used |= 1u << r;
+#pragma unroll
+    for (int c = 0; c < MC; ++c) {
+      const int col = warp + 8 * c;
+      a[r][c] = (i < n && col < n) ? src[(size_t)col * n + i] : T(0);
+    }
+  }
+  bool bad = false;
+  for (int k = 0; k < n; ++k) {
+    const int buf = k & 1;
+    T* ck = colk + buf * 32 * MR;
+    const bool kwarp = warp == (k & 7);  // this warp holds column k, as its column kc
+    const int kc = k >> 3;
+    if (kwarp) {
+      T best = T(-1);
+      int bi = n;
+#pragma unroll
+      for (int c = 0; c < MC; ++c)
+        if (c == kc) {
+#pragma unroll
+          for (int r = 0; r < MR; ++r) {
+            const T v = a[r][c];
+            ck[lane + 32 * r] = v;
+            // NaN ranks above every number, so some unused row (there are
+            // n - k) is always chosen and the pivot check below flags it
+            const T av = isnan(v) ? T(INFINITY) : fabs(v);
+            if (!((used >> r) & 1u) && av > best) {
+              best = av;
+              bi = lane + 32 * r;
+            }
+          }
+        }
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        const T ob = __shfl_xor_sync(0xffffffffu, best, off);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+        if (ob > best || (ob == best && oi < bi)) {
+          best = ob;
+          bi = oi;
+        }
+      }
+      if (lane == 0) sp[buf] = bi;
+    }
+    __syncthreads();
+    const int p = sp[buf];
+    const T pv = ck[p];
+    bad = bad || !(fabs(pv) > T(0));
+    const T d = bad ? T(0) : T(1) / pv;
+    T rc[MC];  // scaled pivot row, this thread's columns
+    tile_row_shfl<T, MR, MC>(a, p >> 5, p & 31, d, rc);
+    // rows: r_i -= f_i r_p (every column; column k is set below)
+#pragma unroll
+    for (int r = 0; r < MR; ++r) {
+      const T f = ck[lane + 32 * r];
+#pragma unroll
+      for (int c = 0; c < MC; ++c) a[r][c] = fma(-f, rc[c], a[r][c]);
+    }
+    // the pivot row becomes the scaled row, column k becomes -f d (d in the
+    // pivot row): the in-place inverse's new column
+    if (lane == (p & 31)) {
+#pragma unroll
+      for (int r = 0; r < MR; ++r)
+        if (r == (p >> 5)) {
+#pragma unroll
+          for (int c = 0; c < MC; ++c) a[r][c] = rc[c];
+          used |= 1u << r;
+        }
+    }
+    if (kwarp) {
+#pragma unroll
+      for (int c = 0; c < MC; ++c)
+        if (c == kc) {
+#pragma unroll
+          for (int r = 0; r < MR; ++r)
+            a[r][c] = (lane + 32 * r == p) ? d : -ck[lane + 32 * r] * d;
+        }
+    }
+    if (threadIdx.x == 0) perm[k] = p;
+  }
+  // gather through shared memory into column-major A^-1
+#pragma unroll
+  for (int r = 0; r < MR; ++r)
+#pragma unroll
+    for (int c = 0; c < MC; ++c) {
+      const int i = lane + 32 * r, col = warp + 8 * c;
+      if (i < n && col < n) S[(size_t)col * n + i] = a[r][c];
+    }
+  __syncthreads();
+  for (int k = threadIdx.x; k < n; k += blockDim.x) iperm[perm[k]] = k;
+  __syncthreads();
+  T* dst = inv + (size_t)blockIdx.x * n * n;
+  for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+    const int c = t / n, r = t - c * n;
+    dst[t] = S[(size_t)iperm[c] * n + perm[r]];
+  }
+  if (bad && threadIdx.x == 0) atomicOr(status, EG_DEV_LU_PIVOT);
+}
+
+// dynamic shared memory of k_block_inverse_reg
+template <typename T, int MR>
+size_t block_inverse_reg_smem(int n) {
+  return sizeof(T) * ((size_t)n * n + 2 * 32 * MR) + sizeof(int) * (2 + 2 * (size_t)n);
+}
+
 template <typename T>
 int pccalc_T(eg_pc* pc) {
   eg_lo* lo = pc->lo;
   eg_mesh* m = lo->mesh;
   const int n = lo->n;
-  const size_t smem = sizeof(T) * (size_t)n * n + sizeof(int) * n;
-  cudaFuncSetAttribute(k_block_inverse<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
   eg_phase_begin(m, EG_PHASE_OTHER);
-  k_block_inverse<T><<<m->E, 256, smem, m->stream>>>((const T*)lo->diag, (T*)pc->inv, n, m->status);
+  const T* A = (const T*)lo->diag;
+  T* X = (T*)pc->inv;
+#define EG_INV_REG(MR)                                                                          \
+  {                                                                                           \
+    const size_t smem = block_inverse_reg_smem<T, MR>(n);                                     \
+    cudaFuncSetAttribute(k_block_inverse_reg<T, MR, 4 * MR>,                                  \
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);            \
+    k_block_inverse_reg<T, MR, 4 * MR><<<m->E, 256, smem, m->stream>>>(A, X, n, m->status);   \
+  }
+  if (n <= 32) {
+    const size_t smem = sizeof(T) * (size_t)n * n + sizeof(int) * n;
+    cudaFuncSetAttribute(k_block_inverse<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    k_block_inverse<T><<<m->E, 256, smem, m->stream>>>(A, X, n, m->status);
+  } else if (n <= 64) {
+    EG_INV_REG(2)
+  } else if (n <= 96) {
+    EG_INV_REG(3)
+  } else {
+    EG_INV_REG(4)
+  }
+#undef EG_INV_REG
   eg_phase_end(m, EG_PHASE_OTHER, 1);
   return EG_OK;
 }
 
 }  // namespace
+
+size_t eg_lo_coupling_size(const eg_lo* lo) {
+  const eg_mesh* m = lo->mesh;
+  return lo->cpl_sparse ? (size_t)m->I * 2 * m->S * m->nv * m->nv
+                        : (size_t)m->I * 2 * lo->nb * lo->nb;
+}
 
 // ====================================================================== C ABI
 int eg_convert(eg_mesh* m, const double* src, void* dst, int prec, int64_t n, double scale) {
@@ -404,8 +573,9 @@ extern "C" int eg_lo_create(eg_mesh* m, int32_t precision, eg_lo** out) {
   lo->prec = precision;
   lo->n = m->Np * m->nv;
   lo->nb = m->S * m->nv;
+  lo->cpl_sparse = m->sparse_face;
   const size_t es = precision == EG_F64 ? 8 : 4;
-  const size_t nd = (size_t)m->E * lo->n * lo->n, nc = (size_t)m->I * 2 * lo->nb * lo->nb;
+  const size_t nd = (size_t)m->E * lo->n * lo->n, nc = eg_lo_coupling_size(lo);
   const size_t nf = (size_t)(m->I + m->B) * m->Nf * 2 * m->nv * m->nv;
   cudaError_t e = cudaMalloc(&lo->diag, es * nd);
   if (e == cudaSuccess && nc) e = cudaMalloc(&lo->cpl, es * nc);
@@ -499,7 +669,7 @@ extern "C" int eg_lo_get_blocks(eg_lo* lo, double* diag, double* coupling) {
     return EG_ERR_INVALID;
   }
   eg_mesh* m = lo->mesh;
-  const size_t nd = (size_t)m->E * lo->n * lo->n, nc = (size_t)m->I * 2 * lo->nb * lo->nb;
+  const size_t nd = (size_t)m->E * lo->n * lo->n, nc = eg_lo_coupling_size(lo);
   EG_CUDA(cudaStreamSynchronize(m->stream));
   auto copy = [&](const void* src, double* dst, size_t n) -> int {
     if (!dst || n == 0) return EG_OK;
@@ -518,10 +688,31 @@ extern "C" int eg_lo_get_blocks(eg_lo* lo, double* diag, double* coupling) {
     std::vector<double> tmp(nc);
     st = copy(lo->cpl, tmp.data(), nc);
     const int nb = lo->nb;
-    for (size_t blk = 0; blk < (size_t)m->I * 2; ++blk)
-      for (int r = 0; r < nb; ++r)
-        for (int c = 0; c < nb; ++c)
-          coupling[blk * nb * nb + (size_t)c * nb + r] = tmp[blk * nb * nb + (size_t)r * nb + c];
+    if (st == EG_OK && lo->cpl_sparse) {
+      // face-diagonal storage [I][2][S][nv][nv] -> dense blocks
+      const int S = m->S, nv = m->nv, Nf = m->Nf;
+      std::vector<int32_t> itf((size_t)m->I * 5), nbp((size_t)m->norient * Nf),
+          nbi((size_t)m->norient * Nf);
+      EG_CUDA(cudaMemcpy(itf.data(), m->ifaces, sizeof(int32_t) * itf.size(), cudaMemcpyDeviceToHost));
+      EG_CUDA(cudaMemcpy(nbp.data(), m->nbrperm, sizeof(int32_t) * nbp.size(), cudaMemcpyDeviceToHost));
+      EG_CUDA(cudaMemcpy(nbi.data(), m->nbrinv, sizeof(int32_t) * nbi.size(), cudaMemcpyDeviceToHost));
+      std::fill(coupling, coupling + (size_t)m->I * 2 * nb * nb, 0.0);
+      for (size_t blk = 0; blk < (size_t)m->I * 2; ++blk) {
+        const int o = itf[(blk / 2) * 5 + 4], side = (int)(blk & 1);
+        for (int s = 0; s < S; ++s) {
+          const int sp = side ? nbi[(size_t)o * Nf + s] : nbp[(size_t)o * Nf + s];
+          for (int a = 0; a < nv; ++a)
+            for (int b = 0; b < nv; ++b)
+              coupling[blk * nb * nb + (size_t)(sp * nv + b) * nb + s * nv + a] =
+                  tmp[((blk * S + s) * nv + a) * nv + b];
+        }
+      }
+    } else if (st == EG_OK) {
+      for (size_t blk = 0; blk < (size_t)m->I * 2; ++blk)
+        for (int r = 0; r < nb; ++r)
+          for (int c = 0; c < nb; ++c)
+            coupling[blk * nb * nb + (size_t)c * nb + r] = tmp[blk * nb * nb + (size_t)r * nb + c];
+    }
   }
   return st;
 }
@@ -558,8 +749,8 @@ extern "C" int eg_pc_calc(eg_pc* pc) {
     return EG_ERR_INVALID;
   }
   const int n = pc->lo->n;
-  const size_t smem = (pc->lo->prec == EG_F64 ? 8 : 4) * (size_t)n * n + sizeof(int) * n;
-  if (smem > 200 * 1024) {
+  const size_t smem = (pc->lo->prec == EG_F64 ? 8 : 4) * ((size_t)n * n + 256) + sizeof(int) * (2 + 2 * (size_t)n);
+  if (n > 128 || smem > 200 * 1024) {
     eg_set_error("eg_pc_calc: element block of %d unknowns exceeds shared memory", n);
     return EG_ERR_UNSUPPORTED;
   }

@@ -36,6 +36,7 @@ extern "C" int eg_estimate_mem(const eg_mem_query* qy, eg_mem_estimate* out) {
   if ((dim != 2 && dim != 3) || qy->num_el <= 0 || qy->nodes_per_el <= 0 ||
       qy->nodes_per_face <= 0 || qy->stencil_size <= 0 || qy->num_interfaces < 0 ||
       qy->num_bndry < 0 || qy->num_orient <= 0 || qy->prolong_from_nodes < 0 ||
+      (qy->face_diagonal != 0 && qy->face_diagonal != 1) ||
       (qy->newton_precision != -1 && qy->newton_precision != EG_F64 &&
        qy->newton_precision != EG_F32) ||
       (qy->newton_precision != -1 && (qy->gmres_restart < 1 || qy->gmres_restart > 31))) {
@@ -85,7 +86,8 @@ extern "C" int eg_estimate_mem(const eg_mem_query* qy, eg_mem_estimate* out) {
     const uint64_t n = Np * nv, nb = S * nv, m = qy->gmres_restart;
     // explicit Jacobian (eg_lo_create)
     jac.add(es * E * n * n);                    // element blocks
-    jac.add(es * I * 2 * nb * nb);              // coupling blocks
+    jac.add(qy->face_diagonal ? es * I * 2 * S * nv * nv   // coupling blocks
+                              : es * I * 2 * nb * nb);
     jac.add(es * (I + B) * Nf * 2 * nv * nv);   // point-flux Jacobians
     jac.add(4 * F * Np);                        // stencil positions
     jac.add(es * N);                            // x, y in the operator precision

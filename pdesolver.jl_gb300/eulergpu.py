@@ -155,10 +155,13 @@ def mem_query(mesh, precision=None, restart=30, host_state=False, prolong_from=N
     """eg_mem_query of a host Mesh: precision None (mesh and state only),
     0 (FP64 Newton) or 1 (mixed); prolong_from = the coarser level's operator."""
     op = mesh.sbp
+    ident = np.broadcast_to(np.eye(op.numfacenodes), op.interp.shape)
+    face_diag = op.stencilsize == op.numfacenodes and bool(np.array_equal(op.interp, ident))
     return abi.EgMemQuery(
         mesh.dim, mesh.numEl, op.numnodes, op.numfacenodes, op.stencilsize, mesh.numInterfaces,
         mesh.numBoundaryFaces, mesh.nbrperm.shape[0], -1 if precision is None else int(precision),
-        int(restart), int(bool(host_state)), 0 if prolong_from is None else prolong_from.numnodes)
+        int(restart), int(bool(host_state)), 0 if prolong_from is None else prolong_from.numnodes,
+        int(face_diag))
 
 
 def estimate_mem(mesh, precision=None, restart=30, host_state=False, prolong_from=None):

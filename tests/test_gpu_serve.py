@@ -66,9 +66,11 @@ def test_set_params_equals_fresh_mesh(gpu_lib):
     assert not np.array_equal(r1, r0)
 
 
-def test_estimate_mem_bounds_what_the_library_takes(gpu_lib):
+@pytest.mark.parametrize("case", ["annulus48_p3", "cube10_p2"])
+def test_estimate_mem_bounds_what_the_library_takes(gpu_lib, case):
     """eg_estimate_mem against the device memory a mesh and its mixed-
-    precision Newton work objects take (cudaMemGetInfo before and after)."""
+    precision Newton work objects take (cudaMemGetInfo before and after);
+    the cube's diagonal-E operator stores face-diagonal coupling blocks."""
     import torch
     torch.cuda.init()
     # load the kernels once (lazy module loading takes device memory too)
@@ -76,7 +78,13 @@ def test_estimate_mem_bounds_what_the_library_takes(gpu_lib):
     gs = eulergpu.GPUMesh(ms_s, opts_s)
     gs.newton(q_s.copy(), dict(NEWTON_OPTS, itermax=200), precision=1)
     gs.close()
-    ms, opts, q = problems.config2(n=48, p=3)
+    if case == "annulus48_p3":
+        ms, opts, q = problems.config2(n=48, p=3)
+    else:
+        ms = problems.request_meshes((3, 10, 2))[-1]
+        levels, q = problems.request_problem({"dim": 3, "n": 10, "p": 2, "M_in": 0.5, "seed": 2},
+                                             [ms])
+        opts = levels[0][1]
     torch.cuda.synchronize()
     free0 = torch.cuda.mem_get_info()[0]
     g = eulergpu.GPUMesh(ms, opts)

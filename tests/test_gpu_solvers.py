@@ -36,6 +36,30 @@ def test_jacobian_blocks_fp64(gpu_lib, oracle, fam, p, flux):
     assert np.abs(c - rc).max() <= 1e-10 * scale
 
 
+@pytest.mark.parametrize("p,flux", [(1, "RoeFlux"), (2, "RoeFlux"), (2, "IRFlux")])
+def test_jacobian_blocks_tet(gpu_lib, oracle, p, flux):
+    """warped cube (2^3 x 6 tets), diagonal-E tets (face nodes are volume
+    nodes: the element face terms and coupling blocks take the one-term path),
+    weak-form volume, at a perturbed free stream: FP64 blocks 1e-10, FP32
+    1e-5 relative to the largest entry."""
+    ms, opts, q = problems.config3(n=2, p=p, seed=71)
+    opts = dict(opts, Flux_name=flux, volume_integral_type=1)
+    g = eulergpu.GPUMesh(ms, opts)
+    rd, rc = oracle_jacobian(oracle, g.desc, g.params, ms, q)
+    scale = max(np.abs(rd).max(), np.abs(rc).max())
+    v = np.random.default_rng(8).normal(size=q.shape)
+    jv = oracle_jvp(oracle, g.desc, g.params, q, v)
+    for prec, tol in ((0, 1e-10), (1, 1e-5)):
+        lo = eulergpu.LinearOperator(g, precision=prec)
+        lo.calc(q)
+        d, c = lo.blocks()
+        assert np.abs(d - rd).max() <= tol * scale
+        assert np.abs(c - rc).max() <= tol * scale
+        # operator apply (face-diagonal coupling rows) == J v
+        y = lo.apply(np.ascontiguousarray(v), np.zeros_like(v))
+        assert np.abs(y - jv).max() <= tol * np.abs(jv).max()
+
+
 def test_jacobian_fp32_and_apply(gpu_lib, oracle):
     ms, opts, q, g = setup()
     rd, rc = oracle_jacobian(oracle, g.desc, g.params, ms, q)
@@ -70,6 +94,33 @@ def test_block_jacobi_inverse(gpu_lib, oracle):
     b = np.einsum("ecr,ec->er", d, x.reshape(d.shape[0], -1)).reshape(q.shape)
     y = pc.apply(np.ascontiguousarray(b), np.zeros_like(b))
     assert np.abs(y - x).max() <= 1e-12 * np.abs(x).max() * 10
+
+
+@pytest.mark.parametrize("case", ["gamma1", "gamma2", "gamma4", "omega4", "tet1", "tet2"])
+@pytest.mark.parametrize("precision", [0, 1])
+def test_block_inverse_every_block_size(gpu_lib, case, precision):
+    """block inverses of 12 .. 115 unknowns (shared-memory Gauss-Jordan up to
+    32 unknowns, register-tiled above): M^-1 (D x) = x for the element blocks
+    D at a perturbed state; FP64 1e-12, FP32 1e-4 relative (times 10)."""
+    if case.startswith("tet"):
+        levels, q = problems.cube_problem({"n": 2, "p": int(case[-1]), "M_in": 0.5, "seed": 9})
+        ms, opts = levels[-1]
+        if len(levels) > 1:
+            q = problems.free_stream(3, ms.coords.shape[:2], Ma=0.5)
+            q = np.ascontiguousarray(q * (1 + np.random.default_rng(9).uniform(-0.01, 0.01, q.shape)))
+    else:
+        ms, opts, q = problems.config1(n=4, p=int(case[-1]), family=case[:-1], seed=61)
+    g = eulergpu.GPUMesh(ms, opts)
+    lo = eulergpu.LinearOperator(g, precision=precision)
+    lo.calc(q)
+    pc = eulergpu.BlockJacobiPC(lo)
+    pc.calc()
+    d, _ = lo.blocks()
+    x = np.random.default_rng(4).normal(size=q.shape)
+    b = np.einsum("ecr,ec->er", d, x.reshape(d.shape[0], -1)).reshape(q.shape)
+    y = pc.apply(np.ascontiguousarray(b), np.zeros_like(b))
+    tol = 1e-12 if precision == 0 else 1e-4
+    assert np.abs(y - x).max() <= tol * np.abs(x).max() * 10
 
 
 @pytest.mark.parametrize("precision,tol", [(0, 1e-8), (1, 1e-4)])
