@@ -920,6 +920,57 @@ def run_tune(args):
     print(json.dumps({"autotune": out}), flush=True)
 
 
+def run_gmres_grid(args):
+    """Microseconds per Arnoldi iteration of the persistent GMRES kernel
+    against its grid size (eg_ls_set_grid; 0 = automatic), FP32 operator and
+    block-Jacobi inverses at a perturbed free stream, GMRES(30), 120
+    iterations, L2 flushed, best of 3.  One JSON line per operator."""
+    import torch
+    from pdesolver_gb300 import eulergpu
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    cases = [("c2 p1", (2, 64, 1)), ("c2 p3", (2, 64, 3)), ("n32 p3", (2, 32, 3)),
+             ("n16 p2", (2, 16, 2)), ("n96 p4", (2, 96, 4)), ("cube16 p2", (3, 16, 2)),
+             ("cube24 p2", (3, 24, 2))]
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    for name, key in cases:
+        ms = problems.request_meshes(key)[-1]
+        lv, q = problems.request_problem({"dim": key[0], "n": key[1], "p": key[2], "M_in": 0.5,
+                                          "seed": 1}, [ms])
+        gm = eulergpu.GPUMesh(ms, lv[0][1])
+        gm.set_stream(stream.cuda_stream)
+        lo = eulergpu.LinearOperator(gm, precision=1)
+        lo.calc(q)
+        pc = eulergpu.BlockJacobiPC(lo)
+        pc.calc()
+        ls = eulergpu.LinearSolver(pc, lo, restart=30)
+        ls.set_tolerances(reltol=1e-30, abstol=0.0, itermax=120)
+        b = torch.randn(ms.numDof, dtype=torch.float64, device="cuda")
+        x = torch.zeros_like(b)
+        row = {"case": name, "E": ms.numEl, "n": ms.sbp.numnodes * ms.numDofPerNode}
+        for nb in [0, 1, 4, 8, 16, 32, 64, 96, 152]:
+            if nb == 1 and ms.numEl > 20000:
+                continue
+            ls.set_grid(nb)
+            x.zero_()
+            ls.solve(b, x)
+            ts = []
+            for _ in range(3):
+                x.zero_()
+                flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                st = ls.solve(b, x)
+                e1.record()
+                torch.cuda.synchronize()
+                ts.append(e0.elapsed_time(e1) / max(st.iters, 1) * 1e3)
+            row[str(nb)] = round(min(ts), 2)
+        print(json.dumps(row), flush=True)
+        for o in (ls, pc, lo, gm):
+            o.close()
+
+
 def run_kernels_only(args, which):
     """Short run of the isolated kernels for profiling captures: the FP32
     operator / block-Jacobi applies of the C2 problem (p=3, initial state), or
@@ -992,7 +1043,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5", "tune"],
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5", "tune", "gmres-grid"],
                     help="c2: steady Newton solves (headline); c3: 3-D entropy-stable RK4; "
                          "c4: batch of 96 steady solves; c5: served stream of steady solves")
     ap.add_argument("--workers", type=int, default=8,
@@ -1012,6 +1063,9 @@ def main():
         return
     if args.workload == "c4" and args.impl == "ours":
         run_c4(args, rank, world)
+        return
+    if args.workload == "gmres-grid" and args.impl == "ours":
+        run_gmres_grid(args)
         return
     if args.workload == "tune" and args.impl == "ours":
         run_tune(args)

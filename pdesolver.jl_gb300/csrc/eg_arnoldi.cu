@@ -582,6 +582,7 @@ int launch_T(eg_ls* ls) {
   const size_t elem_bytes = (size_t)a.n * sizeof(T);
   const size_t op_bytes = (size_t)m->E * a.n * a.n * sizeof(T);
   int nblk = op_bytes <= kSmallOperatorBytes ? 1 : std::max(2, std::min(sms, (m->E + 31) / 32));
+  if (ls->coop_grid > 0) nblk = std::min(ls->coop_grid, sms);
   if (nblk > m->E) nblk = m->E;
   if (nblk > EG_COOP_MAX_BLOCKS) nblk = EG_COOP_MAX_BLOCKS;
   const int epb = (m->E + nblk - 1) / nblk;

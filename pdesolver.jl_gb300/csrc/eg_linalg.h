@@ -49,6 +49,7 @@ struct eg_ls {
   double* xd;      // [ndof] FP64 staging
   double* bd;      // [ndof]
   int nblk;
+  int coop_grid;   // blocks of the persistent GMRES grid (0: automatic)
   // device-side GMRES state (eg_gmres.cu)
   double* dH;      // H | cs | sn | g | y  (FP64)
   int* dflags;     // done, jdone, its, converged, itermax

@@ -848,6 +848,15 @@ extern "C" int eg_ls_create(eg_lo* lo, eg_pc* pc, int32_t restart, eg_ls** out) 
   return EG_OK;
 }
 
+extern "C" int eg_ls_set_grid(eg_ls* ls, int32_t blocks) {
+  if (!ls || blocks < 0) {
+    eg_set_error("eg_ls_set_grid: invalid argument");
+    return EG_ERR_INVALID;
+  }
+  ls->coop_grid = blocks;
+  return EG_OK;
+}
+
 extern "C" int eg_ls_destroy(eg_ls* ls) {
   if (!ls) return EG_OK;
   cudaStreamSynchronize(ls->lo->mesh->stream);

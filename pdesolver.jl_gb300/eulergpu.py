@@ -77,6 +77,7 @@ def _declare(lib):
     lib.eg_ls_destroy.argtypes = [vp]
     lib.eg_ls_set_tolerances.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_int32]
     lib.eg_ls_solve.argtypes = [vp, vp, vp, C.c_int32, C.POINTER(LsStats)]
+    lib.eg_ls_set_grid.argtypes = [vp, C.c_int32]
     lib.eg_newton_solve.argtypes = [vp, vp, C.c_int32, C.POINTER(NewtonOpts), C.POINTER(NewtonStats)]
     lib.eg_rk4.argtypes = [vp, vp, C.c_double, C.c_double, C.c_int32, C.c_double, C.c_int32,
                            C.POINTER(Rk4Stats)]
@@ -471,6 +472,10 @@ class LinearSolver:
 
     def set_tolerances(self, reltol=-1.0, abstol=-1.0, dtol=-1.0, itermax=-1):
         check(self.lib.eg_ls_set_tolerances(self.handle, reltol, abstol, dtol, itermax))
+
+    def set_grid(self, blocks=0):
+        """blocks of the persistent GMRES kernel (0: automatic)."""
+        check(self.lib.eg_ls_set_grid(self.handle, int(blocks)))
 
     def solve(self, b, x):
         pb, mb = GPUMesh._ptr(b, self.lo.g.ndof)
