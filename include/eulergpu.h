@@ -288,7 +288,7 @@ typedef struct {
   int32_t iters;            /* Newton iterations taken                      */
   int32_t krylov_iters;     /* total GMRES iterations                       */
   int32_t converged;
-  int32_t reserved;
+  int32_t graph_iters;      /* iterations run as CUDA graphs (0: eager path) */
   double res_norm0;         /* calcNorm(R(q0), strongres) (physicsRhs)       */
   double res_norm;          /* final                                        */
   double step_norm;         /* last ||dq||_2                                */
@@ -340,7 +340,6 @@ typedef struct {
   int32_t num_interfaces, num_bndry, num_orient;
   int32_t newton_precision;   /* EG_F64, EG_F32, or -1: mesh and state only   */
   int32_t gmres_restart;      /* restart length of the Newton GMRES (1..31)   */
-  int32_t host_state;         /* 1: Newton is given host q (a staging vector) */
   int32_t prolong_from_nodes; /* Np of the coarser level this mesh is
                                  prolonged from (eg_prolong), 0: none         */
   int32_t face_diagonal;      /* 1: the face interpolation is the identity

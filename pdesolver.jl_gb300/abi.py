@@ -73,8 +73,8 @@ class EgMemQuery(C.Structure):
     """eg_mem_query: the mesh counts eg_estimate_mem reads."""
     _fields_ = [(k, C.c_int32) for k in (
         "dim", "num_el", "nodes_per_el", "nodes_per_face", "stencil_size", "num_interfaces",
-        "num_bndry", "num_orient", "newton_precision", "gmres_restart", "host_state",
-        "prolong_from_nodes", "face_diagonal")]
+        "num_bndry", "num_orient", "newton_precision", "gmres_restart", "prolong_from_nodes",
+        "face_diagonal")]
 
 
 class EgMemEstimate(C.Structure):

@@ -39,8 +39,6 @@ namespace cg = cooperative_groups;
 
 namespace {
 
-enum { F_DONE = 0, F_JDONE = 1, F_ITS = 2, F_CONV = 3, F_ITERMAX = 4, F_REORTH = 5, F_CYCLES = 6 };
-enum { S_TOL = 0, S_RESID = 1, S_BETA = 2, S_BNORM = 3, S_RELTOL = 4, S_ABSTOL = 5, S_BETA0 = 6 };
 constexpr int NT = 1024;  // one block per SM
 constexpr int NB_MAX = 64;  // coupling-block rows handled by the face-side pass
 // systems whose element blocks take at most this many bytes run on one block

@@ -23,14 +23,12 @@
 
 namespace {
 
-enum { F_DONE = 0, F_JDONE = 1, F_ITS = 2, F_CONV = 3, F_ITERMAX = 4, F_REORTH = 5, F_CYCLES = 6 };
 
 // a cycle kernel runs unless the cycle is done, or its optional condition
 // flag (need >= 0) is zero
 __device__ __forceinline__ bool gm_skip(const int* flags, int need) {
   return flags && (flags[F_DONE] || (need >= 0 && !flags[need]));
 }
-enum { S_TOL = 0, S_RESID = 1, S_BETA = 2, S_BNORM = 3, S_RELTOL = 4, S_ABSTOL = 5, S_BETA0 = 6 };
 
 // per-block partial sums of V[k] . w for k < cnt (skips when *done)
 template <typename T, int NT>

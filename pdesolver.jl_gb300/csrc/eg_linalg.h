@@ -60,6 +60,9 @@ struct eg_ls {
   bool graphs_ok;  // capture succeeded (else the same launches run eagerly)
 };
 void eg_gmres_release(eg_ls* ls);
+// slots of the device GMRES state: dflags[] and dscal[]
+enum { F_DONE = 0, F_JDONE = 1, F_ITS = 2, F_CONV = 3, F_ITERMAX = 4, F_REORTH = 5, F_CYCLES = 6 };
+enum { S_TOL = 0, S_RESID = 1, S_BETA = 2, S_BNORM = 3, S_RELTOL = 4, S_ABSTOL = 5, S_BETA0 = 6 };
 // the whole GMRES solve as one persistent cooperative kernel (eg_arnoldi.cu)
 #define EG_COOP_MAX_BLOCKS 1024
 int eg_gmres_coop(eg_ls* ls);
@@ -73,10 +76,10 @@ int eg_jacobian_launch(eg_lo* lo, const double* q);
 // y = J x in the operator precision (device pointers of that precision);
 // with `done` non-null the launch does nothing while *done != 0
 int eg_lo_apply_T(eg_lo* lo, const void* x, void* y, const int* done = nullptr);
-// w = v + C z: the preconditioned operator J M^-1 v with z = M^-1 v, using the
-// coupling blocks only (the element blocks times their inverses are I)
 // values of the coupling storage: I*2*nb*nb, or I*2*S*nv*nv when face-diagonal
 size_t eg_lo_coupling_size(const eg_lo* lo);
+// w = v + C z: the preconditioned operator J M^-1 v with z = M^-1 v, using the
+// coupling blocks only (the element blocks times their inverses are I)
 int eg_cpl_apply_T(eg_lo* lo, const void* v, const void* z, void* w, const int* done = nullptr);
 // y = M^-1 x in the operator precision
 int eg_pc_apply_T(eg_pc* pc, const void* x, void* y, const int* done = nullptr);

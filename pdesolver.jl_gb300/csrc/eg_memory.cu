@@ -112,11 +112,12 @@ extern "C" int eg_estimate_mem(const eg_mem_query* qy, eg_mem_estimate* out) {
     kry.add(8 * 8);                             // scalars
     kry.add(8 * N);                             // x, b in FP64
     kry.add(8 * N);
-    // Newton vectors (eg_newton_solve): residual, step, saved state, host staging
+    // Newton vectors (eg_newton_solve): residual, step, saved state, the
+    // state the iteration graphs update
     newton.add(8 * N);
     newton.add(8 * N);
     newton.add(8 * N);
-    if (qy->host_state) newton.add(8 * N);
+    newton.add(8 * N);
   }
   out->mesh = mesh.bytes;
   out->eqn = eqn.bytes;

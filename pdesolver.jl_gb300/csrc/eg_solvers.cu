@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <vector>
 
 #include "eg_internal.h"
 #include "eg_kernels.cuh"
@@ -118,6 +119,15 @@ constexpr double PTC_STALL = 0.5;
 // Newton work objects of a mesh, kept between solves so that repeated solves
 // (continuation levels, batches, serving) allocate nothing after the first:
 // cudaFree synchronises the device and would serialise concurrent streams.
+// With the graph path, one Newton iteration runs as three CUDA graphs around
+// the persistent GMRES launch (see newton_graph_iteration); the graphs are
+// bound to the work objects' pointers and captured once per option set.
+struct GraphKey {
+  eg_params params;
+  int elem_epb, vol_mma, globalize, itermax;
+  double reltol;
+};
+
 struct eg_newton_ws {
   int prec = -1, restart = 0;
   eg_lo* lo = nullptr;
@@ -125,13 +135,26 @@ struct eg_newton_ws {
   eg_ls* ls = nullptr;
   double* res = nullptr;    // [N] residual
   double* dq = nullptr;     // [N] Newton step
-  double* qsave = nullptr;  // [N] state before the step (pseudo-time rejection)
-  double* qd = nullptr;     // [N] device state for host inputs (lazily)
+  double* qsave = nullptr;  // [N] state before the step (rejection, pivot failure)
+  double* qd = nullptr;     // [N] the state the graphs update (caller's q staged here)
+  // graph path
+  bool graph_tried = false, graph_ok = false;
+  GraphKey key;
+  cudaGraphExec_t gJ = nullptr, gP = nullptr, gU = nullptr;  // Jacobian, PC + rhs, update + residual
+  int64_t nJ = 0, nP = 0, nU = 0;                             // kernel nodes of each
+  double* h_tau = nullptr;  // pinned: pseudo-time step of the next iteration
+  cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
 };
 
 void eg_newton_ws_free(eg_mesh* m) {
   eg_newton_ws* w = m ? m->nws : nullptr;
   if (!w) return;
+  cudaGraphExec_t gs[] = {w->gJ, w->gP, w->gU};
+  for (cudaGraphExec_t g : gs)
+    if (g) cudaGraphExecDestroy(g);
+  for (cudaEvent_t e : w->ev)
+    if (e) cudaEventDestroy(e);
+  if (w->h_tau) cudaFreeHost(w->h_tau);
   if (w->ls) eg_ls_destroy(w->ls);
   if (w->pc) eg_pc_destroy(w->pc);
   if (w->lo) eg_lo_destroy(w->lo);
@@ -151,7 +174,7 @@ extern "C" int eg_newton_release(eg_mesh* m) {
 
 namespace {
 // the mesh's Newton work objects for (precision, restart), created on first use
-int newton_ws(eg_mesh* m, int prec, int restart, bool host, eg_newton_ws** out) {
+int newton_ws(eg_mesh* m, int prec, int restart, eg_newton_ws** out) {
   eg_newton_ws* w = m->nws;
   if (w && (w->prec != prec || w->restart != restart)) {
     EG_CUDA(cudaStreamSynchronize(m->stream));
@@ -167,6 +190,9 @@ int newton_ws(eg_mesh* m, int prec, int restart, bool host, eg_newton_ws** out) 
     cudaError_t ce = cudaMalloc((void**)&w->res, 8 * N);
     if (ce == cudaSuccess) ce = cudaMalloc((void**)&w->dq, 8 * N);
     if (ce == cudaSuccess) ce = cudaMalloc((void**)&w->qsave, 8 * N);
+    if (ce == cudaSuccess) ce = cudaMalloc((void**)&w->qd, 8 * N);
+    if (ce == cudaSuccess) ce = cudaMallocHost((void**)&w->h_tau, sizeof(double));
+    for (int k = 0; k < 5 && ce == cudaSuccess; ++k) ce = cudaEventCreate(&w->ev[k]);
     if (ce != cudaSuccess) {
       eg_newton_ws_free(m);
       return eg_cuda_fail(ce, "eg_newton_solve");
@@ -179,12 +205,285 @@ int newton_ws(eg_mesh* m, int prec, int restart, bool host, eg_newton_ws** out) 
       return st;
     }
   }
-  if (host && !w->qd) {
-    cudaError_t ce = cudaMalloc((void**)&w->qd, 8 * N);
-    if (ce != cudaSuccess) return eg_cuda_fail(ce, "eg_newton_solve");
-  }
   *out = w;
   return EG_OK;
+}
+
+// pseudo-time shift with tau_l read from device memory (graph path: the
+// host writes the step of each iteration into pinned memory, a captured copy
+// brings it to the device)
+template <typename T>
+__global__ void k_ptc_shift_dev(T* __restrict__ diag, const double* __restrict__ jac,
+                                const double* __restrict__ w, const double* __restrict__ tau, int E,
+                                int Np, int nv) {
+  const int n = Np * nv;
+  const double tau_l = *tau;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < (int64_t)E * n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int e = (int)(t / n), r = (int)(t - (int64_t)e * n);
+    const int j = r / nv;
+    const double jj = jac[(size_t)e * Np + j];
+    const double M = w[j] / jj;
+    const double tv = tau_l / (1.0 + sqrt(jj));
+    diag[(size_t)e * n * n + (size_t)r * n + r] -= T(M / tv);
+  }
+}
+
+// fresh GMRES state for one linear solve (the values linearSolve starts from)
+__global__ void k_gmres_reset(double* __restrict__ scal, int* __restrict__ flags, double reltol,
+                              double abstol, int itermax) {
+  if (threadIdx.x != 0) return;
+  for (int k = 0; k < 8; ++k) {
+    scal[k] = 0.0;
+    flags[k] = 0;
+  }
+  scal[S_RELTOL] = reltol;
+  scal[S_ABSTOL] = abstol;
+  flags[F_ITERMAX] = itermax;
+}
+
+// capture fn on the mesh stream into an executable graph; false (and no
+// graph) when the stream cannot be captured or the capture fails
+template <typename F>
+bool capture_graph(eg_mesh* m, F fn, cudaGraphExec_t* exec, int64_t* nodes) {
+  *exec = nullptr;
+  if (m->stream == 0 || m->stream == cudaStreamLegacy || m->stream == cudaStreamPerThread) return false;
+  cudaGraph_t graph = nullptr;
+  const int64_t l0 = m->launches;
+  m->capturing = true;
+  cudaError_t e = cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) {
+    m->capturing = false;
+    cudaGetLastError();
+    return false;
+  }
+  fn();
+  e = cudaStreamEndCapture(m->stream, &graph);
+  m->capturing = false;
+  m->launches = l0;
+  if (e != cudaSuccess || !graph) {
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    return false;
+  }
+  // kernel nodes (the launch count of one replay)
+  size_t n = 0;
+  cudaGraphGetNodes(graph, nullptr, &n);
+  std::vector<cudaGraphNode_t> nl(n);
+  int64_t kernels = 0;
+  if (n && cudaGraphGetNodes(graph, nl.data(), &n) == cudaSuccess)
+    for (size_t k = 0; k < n; ++k) {
+      cudaGraphNodeType t;
+      if (cudaGraphNodeGetType(nl[k], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++kernels;
+    }
+  e = cudaGraphInstantiate(exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    *exec = nullptr;
+    cudaGetLastError();
+    return false;
+  }
+  *nodes = kernels;
+  return true;
+}
+
+// the three graphs of one Newton iteration:
+//   gJ  status word cleared, pseudo-time step to the device, Jacobian blocks,
+//       pseudo-time diagonal shift
+//   gP  block-Jacobi inverses, dq = 0, b = -R and x = 0 in the operator
+//       precision, fresh GMRES state
+//   gU  dq from the Krylov solution, ||dq||, q saved, q += dq, R(q), ||R||_{M^-1},
+//       read-back of the norms, the status word and the GMRES state
+bool capture_newton_graphs(eg_mesh* m, eg_newton_ws* w, const GraphKey& key) {
+  eg_lo* lo = w->lo;
+  eg_pc* pc = w->pc;
+  eg_ls* ls = w->ls;
+  const int64_t N = m->ndof;
+  cudaStream_t s = m->stream;
+  double* d_tau = m->red + 2050;
+  bool ok = capture_graph(m, [&]() {
+    cudaMemsetAsync(m->status, 0, sizeof(unsigned int), s);
+    if (key.globalize) cudaMemcpyAsync(d_tau, w->h_tau, sizeof(double), cudaMemcpyHostToDevice, s);
+    eg_jacobian_launch(lo, w->qd);
+    if (key.globalize) {
+      const int blocks = grid64((int64_t)m->E * lo->n);
+      if (lo->prec == EG_F64)
+        k_ptc_shift_dev<double><<<blocks, 256, 0, s>>>((double*)lo->diag, m->jac, m->w, d_tau, m->E, m->Np, m->nv);
+      else
+        k_ptc_shift_dev<float><<<blocks, 256, 0, s>>>((float*)lo->diag, m->jac, m->w, d_tau, m->E, m->Np, m->nv);
+    }
+  }, &w->gJ, &w->nJ);
+  lo->valid = true;
+  ok = ok && capture_graph(m, [&]() {
+    eg_pc_calc(pc);
+    cudaMemsetAsync(w->dq, 0, 8 * N, s);
+    eg_convert(m, w->res, ls->bT, lo->prec, N, -1.0);
+    eg_convert(m, w->dq, ls->xT, lo->prec, N, 1.0);
+    k_gmres_reset<<<1, 32, 0, s>>>(ls->dscal, ls->dflags, key.reltol, 1e-30, key.itermax);
+  }, &w->gP, &w->nP);
+  ok = ok && capture_graph(m, [&]() {
+    eg_convert_back(m, ls->xT, w->dq, lo->prec, N);
+    eg_launch_norm(m, w->dq, 2, m->red + 2049);
+    cudaMemcpyAsync(w->qsave, w->qd, 8 * N, cudaMemcpyDeviceToDevice, s);
+    k_axpby64<<<grid64(N), 256, 0, s>>>(1.0, w->dq, 1.0, w->qd, N);
+    eg_launch_residual(m, w->qd, w->res);
+    eg_launch_norm(m, w->res, 1, m->red + 2048);
+    cudaMemcpyAsync(m->h_red, m->red + 2048, 2 * sizeof(double), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(m->h_status, m->status, sizeof(unsigned int), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(ls->hh, ls->dscal, 8 * sizeof(double), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(ls->hh + 8, ls->dflags, 8 * sizeof(int), cudaMemcpyDeviceToHost, s);
+  }, &w->gU, &w->nU);
+  if (!ok) {
+    cudaGraphExec_t gs[] = {w->gJ, w->gP, w->gU};
+    for (cudaGraphExec_t g : gs)
+      if (g) cudaGraphExecDestroy(g);
+    w->gJ = w->gP = w->gU = nullptr;
+  }
+  return ok;
+}
+
+// Result of one Newton iteration (either path).
+struct IterOut {
+  int st = EG_OK;
+  bool updated = false;    // q holds q + dq (else q is the iteration's start)
+  double norm = 0.0;       // ||R(q + dq)||_{M^-1}
+  double step = 0.0;       // ||dq||_2
+  int kits = 0, kconv = 0;
+  double tj = 0, tp = 0, tk = 0, tr = 0;  // ms: Jacobian, PC, Krylov, update + residual
+};
+
+// One iteration on the graph path: gJ, gP, the persistent GMRES launch, gU,
+// then one synchronisation.  A zero pivot restores q from its saved copy.
+IterOut newton_graph_iteration(eg_mesh* m, eg_newton_ws* w, double tau_l) {
+  IterOut r;
+  cudaStream_t s = m->stream;
+  eg_ls* ls = w->ls;
+  *w->h_tau = tau_l;
+  cudaError_t ce = cudaEventRecord(w->ev[0], s);
+  if (ce == cudaSuccess) ce = cudaGraphLaunch(w->gJ, s);
+  if (ce == cudaSuccess) ce = cudaEventRecord(w->ev[1], s);
+  if (ce == cudaSuccess) ce = cudaGraphLaunch(w->gP, s);
+  if (ce == cudaSuccess) ce = cudaEventRecord(w->ev[2], s);
+  if (ce != cudaSuccess) {
+    r.st = eg_cuda_fail(ce, "eg_newton_solve graph");
+    return r;
+  }
+  m->launches += w->nJ + w->nP;
+  r.st = eg_gmres_coop(ls);
+  if (r.st != EG_OK) return r;
+  ce = cudaEventRecord(w->ev[3], s);
+  if (ce == cudaSuccess) ce = cudaGraphLaunch(w->gU, s);
+  if (ce == cudaSuccess) ce = cudaEventRecord(w->ev[4], s);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+  if (ce != cudaSuccess) {
+    r.st = eg_cuda_fail(ce, "eg_newton_solve graph");
+    return r;
+  }
+  m->launches += w->nU;
+  r.updated = true;
+  float t[4] = {0, 0, 0, 0};
+  for (int k = 0; k < 4; ++k) cudaEventElapsedTime(&t[k], w->ev[k], w->ev[k + 1]);
+  r.tj = t[0];
+  r.tp = t[1];
+  r.tk = t[2];
+  r.tr = t[3];
+  double scal[8];
+  int flags[8];
+  std::memcpy(scal, ls->hh, sizeof(scal));
+  std::memcpy(flags, ls->hh + 8, sizeof(flags));
+  r.kits = flags[F_ITS];
+  r.kconv = flags[F_CONV];
+  r.step = m->h_red[1];
+  r.norm = m->h_red[0];
+  const unsigned int status = *m->h_status;
+  if (status & EG_DEV_LU_PIVOT) {
+    // the eager path stops before the update: put q back
+    cudaMemcpyAsync(w->qd, w->qsave, 8 * m->ndof, cudaMemcpyDeviceToDevice, s);
+    cudaStreamSynchronize(s);
+    eg_set_error("zero pivot in block LU");
+    r.st = EG_ERR_LU_PIVOT;
+    r.updated = false;
+    return r;
+  }
+  if (!std::isfinite(scal[S_BETA])) {
+    cudaMemcpyAsync(w->qd, w->qsave, 8 * m->ndof, cudaMemcpyDeviceToDevice, s);
+    cudaStreamSynchronize(s);
+    eg_set_error("GMRES: non-finite residual");
+    r.st = EG_ERR_NONFINITE;
+    r.updated = false;
+    return r;
+  }
+  r.st = eg_check_status(m);
+  if (r.st == EG_OK && !std::isfinite(r.norm)) {
+    eg_set_error("non-finite residual norm");
+    r.st = EG_ERR_NONFINITE;
+  }
+  return r;
+}
+
+// One iteration launched eagerly (timers on, a stream that cannot be
+// captured, or a system the persistent GMRES kernel does not take).
+IterOut newton_eager_iteration(eg_mesh* m, eg_newton_ws* w, double* qd, bool globalize, double tau_l) {
+  IterOut r;
+  eg_lo* lo = w->lo;
+  eg_pc* pc = w->pc;
+  eg_ls* ls = w->ls;
+  const int64_t N = m->ndof;
+  auto t0 = std::chrono::steady_clock::now();
+  int st = eg_lo_calc(lo, qd, EG_MEM_DEVICE);
+  if (st == EG_OK && globalize) {
+    const int blocks = grid64((int64_t)m->E * lo->n);
+    if (lo->prec == EG_F64)
+      k_ptc_shift<double><<<blocks, 256, 0, m->stream>>>((double*)lo->diag, m->jac, m->w, tau_l, m->E, m->Np, m->nv);
+    else
+      k_ptc_shift<float><<<blocks, 256, 0, m->stream>>>((float*)lo->diag, m->jac, m->w, tau_l, m->E, m->Np, m->nv);
+    m->launches += 1;
+  }
+  if (st == EG_OK) {
+    cudaError_t ce = cudaStreamSynchronize(m->stream);
+    if (ce != cudaSuccess) st = eg_cuda_fail(ce, "eg_newton_solve");
+  }
+  r.tj = ms_since(t0);
+  if ((r.st = st) != EG_OK) return r;
+  t0 = std::chrono::steady_clock::now();
+  st = eg_pc_calc(pc);
+  if (st == EG_OK) {
+    cudaError_t ce = cudaMemcpyAsync(m->h_status, m->status, sizeof(unsigned int), cudaMemcpyDeviceToHost, m->stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(m->stream);
+    st = ce != cudaSuccess ? eg_cuda_fail(ce, "eg_newton_solve") : eg_check_status(m);
+  }
+  r.tp = ms_since(t0);
+  if ((r.st = st) != EG_OK) return r;
+  // J dq = -R, dq0 = 0
+  t0 = std::chrono::steady_clock::now();
+  cudaMemsetAsync(w->dq, 0, 8 * N, m->stream);
+  eg_convert(m, w->res, ls->bT, lo->prec, N, -1.0);
+  eg_convert(m, w->dq, ls->xT, lo->prec, N, 1.0);
+  eg_ls_stats ks;
+  st = eg_gmres_T(ls, ls->bT, ls->xT, &ks);
+  if ((r.st = st) != EG_OK) return r;
+  eg_convert_back(m, ls->xT, w->dq, lo->prec, N);
+  r.kits = ks.iters;
+  r.kconv = ks.converged;
+  // step norm ||dq||_2 (reference newton.jl:238: norm(delta_q_vec))
+  eg_launch_norm(m, w->dq, 2, m->red + 2049);
+  cudaMemcpyAsync(w->qsave, qd, 8 * N, cudaMemcpyDeviceToDevice, m->stream);
+  k_axpby64<<<grid64(N), 256, 0, m->stream>>>(1.0, w->dq, 1.0, qd, N);
+  m->launches += 1;
+  r.updated = true;
+  cudaMemcpyAsync(m->h_red + 1, m->red + 2049, sizeof(double), cudaMemcpyDeviceToHost, m->stream);
+  cudaError_t ce = cudaStreamSynchronize(m->stream);
+  if (ce != cudaSuccess) {
+    r.st = eg_cuda_fail(ce, "eg_newton_solve");
+    return r;
+  }
+  r.step = m->h_red[1];
+  r.tk = ms_since(t0);
+  // residual at the new state
+  t0 = std::chrono::steady_clock::now();
+  r.st = residual_and_norm(m, qd, w->res, &r.norm);
+  r.tr = ms_since(t0);
+  return r;
 }
 }  // namespace
 
@@ -198,114 +497,101 @@ extern "C" int eg_newton_solve(eg_mesh* m, double* q, int32_t mem, const eg_newt
   eg_newton_stats s;
   std::memset(&s, 0, sizeof(s));
   eg_newton_ws* w = nullptr;
-  int st = newton_ws(m, o->precision, o->gmres_restart > 0 ? o->gmres_restart : 30, mem == EG_MEM_HOST, &w);
+  int st = newton_ws(m, o->precision, o->gmres_restart > 0 ? o->gmres_restart : 30, &w);
   if (st != EG_OK) return st;
-  eg_lo* lo = w->lo;
-  eg_pc* pc = w->pc;
   eg_ls* ls = w->ls;
-  double* res = w->res;
-  double* dq = w->dq;
-  double* qd = mem == EG_MEM_HOST ? w->qd : q;
+  const int kmax = o->krylov_itermax > 0 ? o->krylov_itermax : 1000;
+  st = eg_ls_set_tolerances(ls, o->krylov_reltol, 1e-30, -1, kmax);
+  if (st != EG_OK) return st;
+  const bool globalize = o->globalize_euler != 0;
+  // graph path: the state lives in the work objects' own vector
+  GraphKey key;
+  std::memset(&key, 0, sizeof(key));
+  key.params = m->params;
+  key.elem_epb = m->elem_epb;
+  key.vol_mma = m->vol_mma;
+  key.globalize = globalize;
+  key.itermax = kmax;
+  key.reltol = o->krylov_reltol;
+  bool graph = !eg_timing_on(m) && !m->capturing && eg_coop_usable(ls);
+  double* qd = (mem == EG_MEM_HOST || graph) ? w->qd : q;
   cudaError_t ce = cudaSuccess;
-  if (mem == EG_MEM_HOST) {
-    ce = cudaMemcpyAsync(qd, q, 8 * N, cudaMemcpyHostToDevice, m->stream);
+  if (qd != q) {
+    ce = cudaMemcpyAsync(qd, q, 8 * N, mem == EG_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice,
+                         m->stream);
     if (ce != cudaSuccess) return eg_cuda_fail(ce, "eg_newton_solve");
   }
-  st = eg_ls_set_tolerances(ls, o->krylov_reltol, 1e-30, -1, o->krylov_itermax > 0 ? o->krylov_itermax : 1000);
-  if (st != EG_OK) return st;
   auto t0 = std::chrono::steady_clock::now();
   double norm = 0;
-  st = residual_and_norm(m, qd, res, &norm);
+  st = residual_and_norm(m, qd, w->res, &norm);
   s.t_residual += ms_since(t0);
   if (st != EG_OK) return st;
+  if (graph && (!w->graph_tried || std::memcmp(&key, &w->key, sizeof(key)) != 0)) {
+    cudaGraphExec_t gs[] = {w->gJ, w->gP, w->gU};
+    for (cudaGraphExec_t g : gs)
+      if (g) cudaGraphExecDestroy(g);
+    w->gJ = w->gP = w->gU = nullptr;
+    w->key = key;
+    w->graph_tried = true;
+    w->graph_ok = capture_newton_graphs(m, w, key);
+  }
+  // no graphs: a device caller's state is iterated in place (it still holds q0)
+  if (graph && !w->graph_ok && mem == EG_MEM_DEVICE) qd = q;
+  graph = graph && w->graph_ok;
   s.res_norm0 = norm;
   s.res_norm = norm;
   const double norm_rel = norm;
-  bool conv = norm < o->res_abstol || (norm_rel > 0 && norm / norm_rel < o->res_reltol && false);
-  const int g = grid64(N);
-  double* qsave = o->globalize_euler ? w->qsave : nullptr;
+  bool conv = norm < o->res_abstol;
   double tau_l = o->euler_tau, norm_prev = 0.0;
   // per-iteration trace on stderr (the reference's newton_verbosity output)
   const bool verbose = std::getenv("EG_NEWTON_VERBOSE") != nullptr;
   for (int it = 1; !conv && it <= o->itermax; ++it) {
-    // Jacobian (+ pseudo-time diagonal) and preconditioner at the current state
-    t0 = std::chrono::steady_clock::now();
-    st = eg_lo_calc(lo, qd, EG_MEM_DEVICE);
-    if (st == EG_OK && o->globalize_euler) {
+    if (globalize) {
       if (norm_prev != 0.0) tau_l *= fmin(norm_prev / norm, PTC_MAX_GROWTH);
       norm_prev = norm;
-      const int blocks = grid64((int64_t)m->E * lo->n);
-      if (lo->prec == EG_F64)
-        k_ptc_shift<double><<<blocks, 256, 0, m->stream>>>((double*)lo->diag, m->jac, m->w, tau_l, m->E, m->Np, m->nv);
-      else
-        k_ptc_shift<float><<<blocks, 256, 0, m->stream>>>((float*)lo->diag, m->jac, m->w, tau_l, m->E, m->Np, m->nv);
-      m->launches += 1;
     }
-    if (st == EG_OK) EG_CUDA(cudaStreamSynchronize(m->stream));
-    s.t_jacobian += ms_since(t0);
-    if (st != EG_OK) break;
-    t0 = std::chrono::steady_clock::now();
-    st = eg_pc_calc(pc);
-    if (st == EG_OK) {
-      EG_CUDA(cudaMemcpyAsync(m->h_status, m->status, sizeof(unsigned int), cudaMemcpyDeviceToHost, m->stream));
-      EG_CUDA(cudaStreamSynchronize(m->stream));
-      st = eg_check_status(m);
-    }
-    s.t_pc += ms_since(t0);
-    if (st != EG_OK) break;
-    // J dq = -R, dq0 = 0
-    t0 = std::chrono::steady_clock::now();
-    EG_CUDA(cudaMemsetAsync(dq, 0, 8 * N, m->stream));
-    eg_convert(m, res, ls->bT, lo->prec, N, -1.0);
-    eg_convert(m, dq, ls->xT, lo->prec, N, 1.0);
-    eg_ls_stats ks;
-    st = eg_gmres_T(ls, ls->bT, ls->xT, &ks);
-    if (st != EG_OK) break;
-    eg_convert_back(m, ls->xT, dq, lo->prec, N);
-    s.krylov_iters += ks.iters;
-    // step norm ||dq||_2 (reference newton.jl:238: norm(delta_q_vec))
-    eg_launch_norm(m, dq, 2, m->red + 2049);
-    if (qsave) EG_CUDA(cudaMemcpyAsync(qsave, qd, 8 * N, cudaMemcpyDeviceToDevice, m->stream));
-    k_axpby64<<<g, 256, 0, m->stream>>>(1.0, dq, 1.0, qd, N);
-    m->launches += 1;
-    EG_CUDA(cudaMemcpyAsync(m->h_red + 1, m->red + 2049, sizeof(double), cudaMemcpyDeviceToHost, m->stream));
-    EG_CUDA(cudaStreamSynchronize(m->stream));
-    s.step_norm = m->h_red[1];
-    s.t_krylov += ms_since(t0);
-    // residual at the new state
-    t0 = std::chrono::steady_clock::now();
-    double nn = 0.0;
-    st = residual_and_norm(m, qd, res, &nn);
-    s.t_residual += ms_since(t0);
+    const IterOut r = graph ? newton_graph_iteration(m, w, tau_l)
+                            : newton_eager_iteration(m, w, qd, globalize, tau_l);
+    s.t_jacobian += r.tj;
+    s.t_pc += r.tp;
+    s.t_krylov += r.tk;
+    s.t_residual += r.tr;
+    s.krylov_iters += r.kits;
+    if (graph) s.graph_iters += 1;
+    st = r.st;
+    if (st != EG_OK && !r.updated) break;  // failed before the update: q unchanged
+    s.step_norm = r.step;
+    const double nn = r.norm;
     s.iters = it;
     if (verbose)
       std::fprintf(stderr, "eg_newton %3d |R| %.3e -> %.3e tau %.3e krylov %d st %d\n", it, norm, nn,
-                   tau_l, ks.iters, st);
+                   tau_l, r.kits, st);
     const bool bad = st == EG_ERR_NEG_DENSITY || st == EG_ERR_NEG_PRESSURE || st == EG_ERR_NONFINITE ||
                      (st == EG_OK && nn > PTC_MAX_INCREASE * norm);
-    if (bad && o->globalize_euler) {
+    if (bad && globalize) {
       // reject the pseudo-time step: restore q, shrink tau
-      EG_CUDA(cudaMemcpyAsync(qd, qsave, 8 * N, cudaMemcpyDeviceToDevice, m->stream));
-      st = residual_and_norm(m, qd, res, &nn);
+      EG_CUDA(cudaMemcpyAsync(qd, w->qsave, 8 * N, cudaMemcpyDeviceToDevice, m->stream));
+      double nr = 0.0;
+      st = residual_and_norm(m, qd, w->res, &nr);
       if (st != EG_OK) break;
       tau_l *= 0.25;
       norm_prev = 0.0;
       continue;
     }
     if (st != EG_OK) break;
-    const bool stalled = o->globalize_euler && !ks.converged && nn > PTC_STALL * norm;
+    const bool stalled = globalize && !r.kconv && nn > PTC_STALL * norm;
     norm = nn;
     s.res_norm = norm;
-    conv = norm < o->res_abstol || (norm / norm_rel < o->res_reltol) ||
-           (s.step_norm <= o->step_tol);
+    conv = norm < o->res_abstol || (norm / norm_rel < o->res_reltol) || (s.step_norm <= o->step_tol);
     if (stalled && !conv) {
       tau_l *= 0.25;
       norm_prev = 0.0;  // no SER growth right after
     }
   }
   s.converged = conv ? 1 : 0;
-  if (st == EG_OK && mem == EG_MEM_HOST) {
-    ce = cudaMemcpyAsync(q, qd, 8 * N, cudaMemcpyDeviceToHost, m->stream);
+  if (st == EG_OK && qd != q) {
+    ce = cudaMemcpyAsync(q, qd, 8 * N, mem == EG_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice,
+                         m->stream);
     if (ce == cudaSuccess) ce = cudaStreamSynchronize(m->stream);
     if (ce != cudaSuccess) st = eg_cuda_fail(ce, "eg_newton_solve copy-out");
   }

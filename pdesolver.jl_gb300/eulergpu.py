@@ -114,7 +114,7 @@ class NewtonOpts(C.Structure):
 
 class NewtonStats(C.Structure):
     _fields_ = [("iters", C.c_int32), ("krylov_iters", C.c_int32), ("converged", C.c_int32),
-                ("reserved", C.c_int32), ("res_norm0", C.c_double), ("res_norm", C.c_double),
+                ("graph_iters", C.c_int32), ("res_norm0", C.c_double), ("res_norm", C.c_double),
                 ("step_norm", C.c_double), ("t_residual", C.c_double), ("t_jacobian", C.c_double),
                 ("t_pc", C.c_double), ("t_krylov", C.c_double)]
 
@@ -152,7 +152,7 @@ def params_from_opts(opts: dict) -> abi.EgParams:
         p_free=opts.get("p_free"))
 
 
-def mem_query(mesh, precision=None, restart=30, host_state=False, prolong_from=None):
+def mem_query(mesh, precision=None, restart=30, prolong_from=None):
     """eg_mem_query of a host Mesh: precision None (mesh and state only),
     0 (FP64 Newton) or 1 (mixed); prolong_from = the coarser level's operator."""
     op = mesh.sbp
@@ -161,15 +161,14 @@ def mem_query(mesh, precision=None, restart=30, host_state=False, prolong_from=N
     return abi.EgMemQuery(
         mesh.dim, mesh.numEl, op.numnodes, op.numfacenodes, op.stencilsize, mesh.numInterfaces,
         mesh.numBoundaryFaces, mesh.nbrperm.shape[0], -1 if precision is None else int(precision),
-        int(restart), int(bool(host_state)), 0 if prolong_from is None else prolong_from.numnodes,
-        int(face_diag))
+        int(restart), 0 if prolong_from is None else prolong_from.numnodes, int(face_diag))
 
 
-def estimate_mem(mesh, precision=None, restart=30, host_state=False, prolong_from=None):
+def estimate_mem(mesh, precision=None, restart=30, prolong_from=None):
     """Device bytes the library takes for `mesh` (and, with a precision, its
     Newton work objects) plus the caller's q and res (reference estimateMem.jl)."""
     out = abi.EgMemEstimate()
-    qy = mem_query(mesh, precision, restart, host_state, prolong_from)
+    qy = mem_query(mesh, precision, restart, prolong_from)
     check(library().eg_estimate_mem(C.byref(qy), C.byref(out)))
     return out
 

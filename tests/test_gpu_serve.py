@@ -94,7 +94,7 @@ def test_estimate_mem_bounds_what_the_library_takes(gpu_lib, case):
         pass   # one iteration does not converge; the work objects exist
     torch.cuda.synchronize()
     taken = free0 - torch.cuda.mem_get_info()[0]
-    est = eulergpu.estimate_mem(ms, precision=1, host_state=True)
+    est = eulergpu.estimate_mem(ms, precision=1)
     lib_bytes = est.total - est.eqn     # q and res are the caller's (host here)
     slack = est.allocations * (2 << 20)
     assert 0.9 * lib_bytes - slack <= taken <= 1.1 * lib_bytes + slack, (taken, lib_bytes)

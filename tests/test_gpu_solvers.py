@@ -223,3 +223,28 @@ def test_newton_single_block_gmres_with_large_chunk(gpu_lib, precision):
     q = q0.copy()
     st = g.newton(q, NEWTON_OPTS, precision=precision)
     assert st.converged == 1 and st.res_norm < 1e-10
+
+
+@pytest.mark.parametrize("device_state", [False, True])
+def test_newton_graph_path_equals_eager_path(gpu_lib, device_state):
+    """one Newton iteration as three CUDA graphs around the persistent GMRES
+    launch gives the eagerly launched iteration's result bit for bit (phase
+    timers force the eager path)."""
+    import torch
+    ms, opts, q0 = problems.config2(n=8, p=2)
+    g = eulergpu.GPUMesh(ms, opts)
+    qa = torch.from_numpy(q0).cuda() if device_state else q0.copy()
+    st = g.newton(qa, NEWTON_OPTS, precision=1)
+    assert st.converged == 1 and st.graph_iters == st.iters > 0
+    g.set_timing(True)
+    qb = torch.from_numpy(q0).cuda() if device_state else q0.copy()
+    st2 = g.newton(qb, NEWTON_OPTS, precision=1)
+    g.set_timing(False)
+    assert st2.converged == 1 and st2.graph_iters == 0 and st2.iters == st.iters
+    a = qa.cpu().numpy() if device_state else qa
+    b = qb.cpu().numpy() if device_state else qb
+    assert np.array_equal(a, b)
+    # a second graph solve reuses the captured graphs
+    qc = q0.copy()
+    st3 = g.newton(qc, NEWTON_OPTS, precision=1)
+    assert st3.graph_iters == st3.iters and np.array_equal(qc, a)
