@@ -997,6 +997,25 @@ def run_kernels_only(args, which):
         out["launches_each"] = args.steps
         print(json.dumps(out), flush=True)
         return
+    if which == "blockinv":
+        # block-Jacobi inverses: the C2 p=3 operator (48 unknowns per block) and
+        # the warped 8^3 x 6 cube with diagonal-E p=2 tets (115 unknowns)
+        for key in ((2, 64, 3), (3, 8, 2)):
+            msk = problems.request_meshes(key)[-1]
+            lvk, qk = problems.request_problem({"dim": key[0], "n": key[1], "p": key[2],
+                                                "M_in": 0.5, "seed": 1}, [msk])
+            gk = eulergpu.GPUMesh(msk, lvk[0][1])
+            gk.set_stream(stream.cuda_stream)
+            lo = eulergpu.LinearOperator(gk, precision=1)
+            lo.calc(qk)
+            pc = eulergpu.BlockJacobiPC(lo)
+            for _ in range(args.steps):
+                pc.calc()
+            torch.cuda.synchronize()
+        out["kernels"] = ["k_block_inverse_reg<float,2,8>", "k_block_inverse_reg<float,4,16>"]
+        out["launches_each"] = args.steps
+        print(json.dumps(out), flush=True)
+        return
     if which == "gmres":
         # one Newton linear system: FP32 Jacobian + block-Jacobi at the initial
         # state, GMRES(30) for `steps` iterations (one restart cycle per 30)
@@ -1050,7 +1069,7 @@ def main():
                     help="host threads of the c4 batch / serving slots of c5")
     ap.add_argument("--requests", type=int, default=2000, help="c5: requests of the stream served")
     ap.add_argument("--probe", type=int, default=32, help="c5: requests of the capacity probe")
-    ap.add_argument("--only", default=None, choices=["krylov", "residual", "gmres", "split"],
+    ap.add_argument("--only", default=None, choices=["krylov", "residual", "gmres", "split", "blockinv"],
                     help="run only the isolated kernels (for profiler captures)")
     args = ap.parse_args()
     if args.only:

@@ -261,6 +261,15 @@ int eg_ls_set_tolerances(eg_ls* ls, double reltol, double abstol, double dtol, i
    reference counterpart; the result does not depend on it beyond the order of
    the FP reductions. */
 int eg_ls_set_grid(eg_ls* ls, int32_t blocks);
+/* Batched persistent GMRES (process-wide switch; no reference counterpart).
+   When enabled, the Krylov solves that threads reach within window_us of each
+   other (or as soon as every thread inside eg_newton_solve on the device has
+   reached one) run as one cooperative launch: each solve gets its own range of
+   blocks (at most one block per SM in total) and barriers over those blocks
+   only.  Meant for many meshes solved at once on different threads/streams
+   (batches, serving).  A solve's result does not depend on the batch it runs
+   in.  Off by default. */
+int eg_set_gmres_batching(int32_t enable, double window_us);
 /* linearSolve: x <- A^-1 b (x is also the initial guess) */
 int eg_ls_solve(eg_ls* ls, const double* b, double* x, int32_t mem, eg_ls_stats* stats);
 

@@ -1,6 +1,8 @@
 // eg_linalg.h -- Jacobian operator, block-Jacobi preconditioner and GMRES
 // objects behind the eg_lo / eg_pc / eg_ls handles of the C ABI.
 #pragma once
+#include <mutex>
+
 #include "eg_internal.h"
 
 struct eg_lo {
@@ -58,6 +60,11 @@ struct eg_ls {
   void* g_cycle;   // cudaGraphExec_t: one restart cycle + update + re-initialisation
   int64_t g_init_nodes, g_cycle_nodes;
   bool graphs_ok;  // capture succeeded (else the same launches run eagerly)
+  // batched persistent GMRES: the solve's kernel arguments (device copy and
+  // pinned staging) and the event marking them ready on the mesh stream
+  void* dargs;
+  void* hargs;
+  cudaEvent_t ev_in;
 };
 void eg_gmres_release(eg_ls* ls);
 // slots of the device GMRES state: dflags[] and dscal[]
@@ -66,6 +73,17 @@ enum { S_TOL = 0, S_RESID = 1, S_BETA = 2, S_BNORM = 3, S_RELTOL = 4, S_ABSTOL =
 // the whole GMRES solve as one persistent cooperative kernel (eg_arnoldi.cu)
 #define EG_COOP_MAX_BLOCKS 1024
 int eg_gmres_coop(eg_ls* ls);
+// one cooperative GMRES grid at a time per device (held across launch and
+// completion of multi-block grids, single or batched)
+std::mutex& eg_coop_mutex(int dev);
+// batched persistent GMRES (eg_arnoldi_batch.cu): on when enabled by
+// eg_set_gmres_batching; eg_gmres_coop then hands the solve to the batcher
+bool eg_gmres_batching();
+int eg_gmres_coop_batched(eg_ls* ls);
+// threads inside eg_newton_solve on a device while batching is on (the
+// batcher waits for their solves before launching)
+void eg_batch_enter(int dev);
+void eg_batch_leave(int dev);
 bool eg_coop_supported();
 // the persistent kernel handles this system (device support, coupling blocks
 // of at most 64 rows, small face tables)

@@ -789,10 +789,12 @@ static void ls_free(eg_ls* ls) {
   if (!ls) return;
   eg_gmres_release(ls);
   void* bufs[] = {ls->V, ls->w, ls->z, ls->xT, ls->bT, ls->part, ls->h, ls->y, ls->xd, ls->bd,
-                  ls->dH, ls->dflags, ls->dscal, ls->cfs};
+                  ls->dH, ls->dflags, ls->dscal, ls->cfs, ls->dargs};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (ls->hh) cudaFreeHost(ls->hh);
+  if (ls->hargs) cudaFreeHost(ls->hargs);
+  if (ls->ev_in) cudaEventDestroy(ls->ev_in);
   delete ls;
 }
 

@@ -496,6 +496,17 @@ extern "C" int eg_newton_solve(eg_mesh* m, double* q, int32_t mem, const eg_newt
   const int64_t N = m->ndof;
   eg_newton_stats s;
   std::memset(&s, 0, sizeof(s));
+  // with batched GMRES, the batcher waits for the solves of the threads in here
+  struct BatchGuard {
+    int dev = -1;
+    BatchGuard() {
+      if (eg_gmres_batching() && cudaGetDevice(&dev) == cudaSuccess) eg_batch_enter(dev);
+      else dev = -1;
+    }
+    ~BatchGuard() {
+      if (dev >= 0) eg_batch_leave(dev);
+    }
+  } batch_guard;
   eg_newton_ws* w = nullptr;
   int st = newton_ws(m, o->precision, o->gmres_restart > 0 ? o->gmres_restart : 30, &w);
   if (st != EG_OK) return st;

@@ -78,6 +78,7 @@ def _declare(lib):
     lib.eg_ls_set_tolerances.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_int32]
     lib.eg_ls_solve.argtypes = [vp, vp, vp, C.c_int32, C.POINTER(LsStats)]
     lib.eg_ls_set_grid.argtypes = [vp, C.c_int32]
+    lib.eg_set_gmres_batching.argtypes = [C.c_int32, C.c_double]
     lib.eg_newton_solve.argtypes = [vp, vp, C.c_int32, C.POINTER(NewtonOpts), C.POINTER(NewtonStats)]
     lib.eg_rk4.argtypes = [vp, vp, C.c_double, C.c_double, C.c_int32, C.c_double, C.c_int32,
                            C.POINTER(Rk4Stats)]
@@ -171,6 +172,12 @@ def estimate_mem(mesh, precision=None, restart=30, prolong_from=None):
     qy = mem_query(mesh, precision, restart, prolong_from)
     check(library().eg_estimate_mem(C.byref(qy), C.byref(out)))
     return out
+
+
+def set_gmres_batching(enable=True, window_us=200.0):
+    """run the Krylov solves of concurrent Newton solves (one thread per mesh)
+    in shared cooperative launches (process-wide switch)."""
+    check(library().eg_set_gmres_batching(int(bool(enable)), float(window_us)))
 
 
 class GPUMesh:
