@@ -662,8 +662,9 @@ def run_c4(args, rank, world):
     torch.cuda.synchronize()
     t_setup = time.perf_counter() - t0
     workers = args.workers
+    batched = args.gmres_batching == "on"
     for _ in range(max(1, args.warmup)):
-        batch.solve_batch(probs, workers=workers)
+        batch.solve_batch(probs, workers=workers, batch_gmres=batched)
     torch.cuda.synchronize()
     l0 = sum(g.timings().launches for pr in probs for g in pr.levels)
     # several streams driven by host threads: the host clock between two
@@ -672,7 +673,7 @@ def run_c4(args, rank, world):
         torch.cuda.synchronize()
         t1 = time.perf_counter()
         for _ in range(args.steps):
-            results = batch.solve_batch(probs, workers=workers)
+            results = batch.solve_batch(probs, workers=workers, batch_gmres=batched)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t1
     n_launch = sum(g.timings().launches for pr in probs for g in pr.levels) - l0
@@ -694,8 +695,14 @@ def run_c4(args, rank, world):
     hprobs = [batch.SteadyProblem(levels=pr.levels, q0=pr.q0.cpu().numpy(), opts=pr.opts,
                                   level_tol=pr.level_tol, tag=pr.tag, work=pr.work) for pr in probs]
     t2 = time.perf_counter()
-    batch.solve_batch(hprobs, workers=workers)
+    batch.solve_batch(hprobs, workers=workers, batch_gmres=batched)
     e2e = world * len(probs) / (time.perf_counter() - t2)
+    # the same batch with the other Krylov launch mode, for comparison
+    torch.cuda.synchronize()
+    t3 = time.perf_counter()
+    batch.solve_batch(probs, workers=workers, batch_gmres=not batched)
+    torch.cuda.synchronize()
+    other_rate = len(probs) / (time.perf_counter() - t3)
     h2d = sum(pr.q0.numel() * 8 + sum(g.ndof * 8 for g in pr.levels[1:]) for pr in probs)
     d2h = sum(sum(g.ndof * 8 for g in pr.levels) + sum(g.ndof * 8 for g in pr.levels[1:])
               for pr in probs)
@@ -719,8 +726,11 @@ def run_c4(args, rank, world):
                    "timing": "host clock between device synchronisations (threads x streams)",
                    "setup_s": t_setup, "l2": "per-problem working sets up to 1.2 GB; the batch "
                                              "exceeds the 129 MB L2",
-                   "parallelism": f"{workers} host threads x 1 stream each, replicas x{world}"},
+                   "parallelism": f"{workers} host threads x 1 stream each, replicas x{world}",
+                   "gmres_batching": args.gmres_batching},
         "batch": {"failed": failed, "retried": retried,
+                  ("solves_per_s_gmres_batching_off" if batched else "solves_per_s_gmres_batching_on"):
+                      other_rate,
                   "krylov_its": sum(l[3] for lv in counts for l in lv),
                   "newton_its": sum(l[2] for lv in counts for l in lv),
                   "solve_s_p50": statistics.median(r.seconds for r in results),
@@ -819,7 +829,8 @@ def run_c5(args, rank, world):
     summaries, results, servers = {}, {}, {}
     # capacity: the probe requests all queued at once (closed loop), mixed precision
     probe = _c5_requests(probe_specs, meshes, 1.0, arrivals=False)
-    srv = serve.SteadySolveServer(budget, slots=args.workers, precision=1)
+    srv = serve.SteadySolveServer(budget, slots=args.workers, precision=1,
+                                  batch_gmres=args.gmres_batching == "on")
     pres = srv.serve(probe)
     srv.close()
     capacity = serve.latency_summary(pres)["solves_per_s"]
@@ -827,7 +838,8 @@ def run_c5(args, rank, world):
     with ClockSampler(dev) as clk:
         for name, prec in (("mixed", 1), ("fp64", 0)):
             reqs = _c5_requests(specs, meshes, rate)
-            srv = serve.SteadySolveServer(budget, slots=args.workers, precision=prec)
+            srv = serve.SteadySolveServer(budget, slots=args.workers, precision=prec,
+                                          batch_gmres=args.gmres_batching == "on")
             torch.cuda.synchronize()
             res = srv.serve(reqs)
             torch.cuda.synchronize()
@@ -872,7 +884,8 @@ def run_c5(args, rank, world):
                    "timing": "host clock: completion minus arrival per request; solves/s = "
                              "completed / (last completion - first arrival)",
                    "l2": "per-request working sets up to 14 GB; inputs exceed the 129 MB L2",
-                   "parallelism": f"{args.workers} slots (host threads x streams), replicas x{world}"},
+                   "parallelism": f"{args.workers} slots (host threads x streams), replicas x{world}",
+                   "gmres_batching": args.gmres_batching},
         "serving": {"mixed": mixed, "fp64": summaries["fp64"],
                     "functional_rel_diff_mixed_vs_fp64_max": max(fdiff) if fdiff else None},
         "cpu_baseline": {"value": n_ok / cpu_t if cpu_t else None, "unit": "solves/s", "cores": used,
@@ -1068,6 +1081,8 @@ def main():
     ap.add_argument("--workers", type=int, default=8,
                     help="host threads of the c4 batch / serving slots of c5")
     ap.add_argument("--requests", type=int, default=2000, help="c5: requests of the stream served")
+    ap.add_argument("--gmres-batching", default="off", choices=["on", "off"],
+                    help="c4/c5: Krylov solves of concurrent problems in shared cooperative launches")
     ap.add_argument("--probe", type=int, default=32, help="c5: requests of the capacity probe")
     ap.add_argument("--only", default=None, choices=["krylov", "residual", "gmres", "split", "blockinv"],
                     help="run only the isolated kernels (for profiler captures)")

@@ -262,11 +262,12 @@ int eg_ls_set_tolerances(eg_ls* ls, double reltol, double abstol, double dtol, i
    the FP reductions. */
 int eg_ls_set_grid(eg_ls* ls, int32_t blocks);
 /* Batched persistent GMRES (process-wide switch; no reference counterpart).
-   When enabled, the Krylov solves that threads reach within window_us of each
-   other (or as soon as every thread inside eg_newton_solve on the device has
-   reached one) run as one cooperative launch: each solve gets its own range of
-   blocks (at most one block per SM in total) and barriers over those blocks
-   only.  Meant for many meshes solved at once on different threads/streams
+   When enabled, the multi-block Krylov solves that threads reach within
+   window_us of each other (or as soon as every thread inside eg_newton_solve
+   with such a solve has reached one) run as one cooperative launch: each
+   solve keeps the blocks it gets alone, solves are packed while their blocks
+   fit on the SMs, and barriers cover a solve's own blocks only.  One-block
+   solves launch at once (they share the GPU without batching).  Meant for many meshes solved at once on different threads/streams
    (batches, serving).  A solve's result does not depend on the batch it runs
    in.  Off by default. */
 int eg_set_gmres_batching(int32_t enable, double window_us);

@@ -12,7 +12,8 @@ GB300 the problems share the device through concurrent CUDA streams:
   stay allocated between solves (`eg_newton_solve`), so a warm batch
   allocates nothing and no `cudaFree` serialises the streams;
 * small Krylov solves run as one-block persistent kernels side by side;
-  larger ones take the whole GPU one at a time (eg_arnoldi.cu).
+  larger ones take the GPU one grid at a time (eg_arnoldi.cu), or, with
+  batch_gmres, share cooperative launches (eg_arnoldi_batch.cu).
 
 A problem that does not converge, or whose pseudo-time steps keep hitting a
 non-physical state, is retried from its initial state with the initial
@@ -77,9 +78,25 @@ def solve_one(pr: SteadyProblem, precision=1, retries=2, stream=None) -> SteadyR
     return res
 
 
-def solve_batch(problems, workers=8, precision=1, retries=2):
+def solve_batch(problems, workers=8, precision=1, retries=2, batch_gmres=False):
     """Solve every problem; returns one SteadyResult per problem (in input
-    order).  Each worker thread owns one CUDA stream."""
+    order).  Each worker thread owns one CUDA stream.  With batch_gmres the
+    workers' multi-block Krylov solves that meet in time run in shared
+    cooperative launches (eg_set_gmres_batching); each result is the same bits
+    as alone.  Off by default: on the batched workload a shared launch lasts as
+    long as its longest solve, and the waiting of the shorter ones outweighs
+    the sharing (2.96 against 3.10 solves/s)."""
+    import torch
+
+    from .eulergpu import set_gmres_batching
+    set_gmres_batching(bool(batch_gmres))
+    try:
+        return _solve_batch(problems, workers, precision, retries)
+    finally:
+        set_gmres_batching(False)
+
+
+def _solve_batch(problems, workers, precision, retries):
     import torch
     order = sorted(range(len(problems)), key=lambda i: -problems[i].work)
     lock = threading.Lock()

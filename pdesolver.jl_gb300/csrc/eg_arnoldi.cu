@@ -98,7 +98,7 @@ int launch_T(eg_ls* ls) {
 // partial sums need 4 * grid * 33 values of ls->part (eg_ls_create sizes
 // them for EG_COOP_MAX_BLOCKS blocks)
 int eg_gmres_coop(eg_ls* ls) {
-  if (eg_gmres_batching()) return eg_gmres_coop_batched(ls);
+  if (eg_gmres_batching() && eg_gmres_wanted_blocks(ls) > 1) return eg_gmres_coop_batched(ls);
   return ls->lo->prec == EG_F64 ? launch_T<double>(ls) : launch_T<float>(ls);
 }
 

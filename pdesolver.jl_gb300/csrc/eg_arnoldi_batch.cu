@@ -3,7 +3,9 @@
 //
 // When batching is on (eg_set_gmres_batching), a thread that reaches the
 // Krylov solve of its Newton iteration hands the solve to a per-device
-// batcher instead of launching it.  The solves handed in within a short
+// batcher instead of launching it, if the solve runs on several blocks (a
+// one-block solve is launched at once: one-block grids of several threads
+// already share the GPU without waiting for each other).  The solves handed in within a short
 // window (or as soon as every thread inside eg_newton_solve has handed one in)
 // go out as one cooperative grid walking a work list: each problem gets a
 // contiguous range of blocks (at most one block per SM in total, more blocks
@@ -85,22 +87,26 @@ struct BatchList {
   BatchEntry e[kMaxBatch];
 };
 
-// (dimension, element-block size) cases with a compiled body; others run the
-// generic body of their dimension
+// (dimension, element-block size) cases with a compiled body, the same set
+// as the single-problem launcher compiles for these dimensions (the block
+// size changes the order of the block-row sums); others run the generic body
 int kind_of(int dim, int n) {
   if (dim == 2) {
     switch (n) {
       case 12: return 0;
-      case 28: return 1;
-      case 48: return 2;
-      case 72: return 3;
-      default: return 4;
+      case 24: return 1;
+      case 28: return 2;
+      case 40: return 3;
+      case 48: return 4;
+      case 60: return 5;
+      case 72: return 6;
+      default: return 7;
     }
   }
   switch (n) {
-    case 30: return 5;
-    case 115: return 6;
-    default: return 7;
+    case 30: return 8;
+    case 115: return 9;
+    default: return 10;
   }
 }
 
@@ -125,12 +131,15 @@ __global__ void __launch_bounds__(NT, 1) k_gmres_batch(BatchList list, unsigned 
   SubBarrier bar{bars + 2 * k, bars + 2 * k + 1, err, nblk, &s_ok};
   switch (s_kind) {
     case 0: gmres_body<2, 12, T>(sa, b, nblk, bar, sm); break;
-    case 1: gmres_body<2, 28, T>(sa, b, nblk, bar, sm); break;
-    case 2: gmres_body<2, 48, T>(sa, b, nblk, bar, sm); break;
-    case 3: gmres_body<2, 72, T>(sa, b, nblk, bar, sm); break;
-    case 4: gmres_body<2, 0, T>(sa, b, nblk, bar, sm); break;
-    case 5: gmres_body<3, 30, T>(sa, b, nblk, bar, sm); break;
-    case 6: gmres_body<3, 115, T>(sa, b, nblk, bar, sm); break;
+    case 1: gmres_body<2, 24, T>(sa, b, nblk, bar, sm); break;
+    case 2: gmres_body<2, 28, T>(sa, b, nblk, bar, sm); break;
+    case 3: gmres_body<2, 40, T>(sa, b, nblk, bar, sm); break;
+    case 4: gmres_body<2, 48, T>(sa, b, nblk, bar, sm); break;
+    case 5: gmres_body<2, 60, T>(sa, b, nblk, bar, sm); break;
+    case 6: gmres_body<2, 72, T>(sa, b, nblk, bar, sm); break;
+    case 7: gmres_body<2, 0, T>(sa, b, nblk, bar, sm); break;
+    case 8: gmres_body<3, 30, T>(sa, b, nblk, bar, sm); break;
+    case 9: gmres_body<3, 115, T>(sa, b, nblk, bar, sm); break;
     default: gmres_body<3, 0, T>(sa, b, nblk, bar, sm); break;
   }
 }
@@ -152,7 +161,8 @@ struct Batcher {
   unsigned int* bars = nullptr;   // [kMaxBatch][2] barrier counters (device)
   int* err = nullptr;             // device error flag
   int* h_err = nullptr;           // pinned copy
-  std::atomic<int> active{0};     // threads inside eg_newton_solve
+  std::atomic<int> active{0};     // threads inside eg_newton_solve with a
+                                  // multi-block Krylov solve
 };
 
 Batcher& batcher(int dev) {
@@ -161,7 +171,7 @@ Batcher& batcher(int dev) {
 }
 
 std::atomic<int> g_batching{0};
-std::atomic<long long> g_window_ns{200000};
+std::atomic<long long> g_window_ns{50000};
 
 int ensure_batcher(Batcher& B) {
   if (B.stream) return EG_OK;
@@ -173,42 +183,26 @@ int ensure_batcher(Batcher& B) {
   return EG_OK;
 }
 
-// blocks per problem: each gets what the single-problem launcher would give
-// it when they all fit on the SMs, else one each plus a share of the rest in
-// proportion to its operator bytes
-std::vector<int> allocate_blocks(const std::vector<Submission*>& batch, int sms) {
-  const size_t np = batch.size();
-  std::vector<int> want(np), got(np, 1);
-  std::vector<double> work(np);
-  long long total = 0;
-  for (size_t i = 0; i < np; ++i) {
-    const eg_ls* ls = batch[i]->ls;
-    const eg_mesh* m = ls->lo->mesh;
-    const size_t es = ls->lo->prec == EG_F64 ? 8 : 4;
-    const double op = (double)m->E * ls->lo->n * ls->lo->n * es;
-    work[i] = op;
-    want[i] = op <= double(size_t(2) << 20) ? 1 : std::max(2, std::min(sms, (m->E + 31) / 32));
-    want[i] = std::min(want[i], m->E);
-    total += want[i];
-  }
-  if (total <= sms) return want;
-  double wsum = 0.0;
-  for (double w : work) wsum += w;
-  int left = sms - (int)np;
-  for (size_t i = 0; i < np && left > 0; ++i) {
-    int extra = (int)((double)(sms - (int)np) * work[i] / wsum);
-    extra = std::min(extra, std::min(left, want[i] - 1));
-    got[i] += std::max(0, extra);
-    left -= std::max(0, extra);
-  }
-  return got;
+// blocks of one problem: what the single-problem launcher gives it (one block
+// for operators of at most 2 MB, else up to one block per SM with at least 32
+// elements each).  A batch never shrinks a problem's share: the block
+// partition fixes the order of the dot-product reductions, so a solve gives
+// the same bits in any batch and alone.
+int wanted_blocks_sms(const eg_ls* ls, int sms) {
+  const eg_mesh* m = ls->lo->mesh;
+  const size_t es = ls->lo->prec == EG_F64 ? 8 : 4;
+  const size_t op = (size_t)m->E * ls->lo->n * ls->lo->n * es;
+  int nb = op <= (size_t(2) << 20) ? 1 : std::max(2, std::min(sms, (m->E + 31) / 32));
+  nb = std::min(nb, m->E);
+  return std::min(nb, EG_COOP_MAX_BLOCKS);
 }
 
 template <typename T>
 int launch_batch(Batcher& B, const std::vector<Submission*>& batch, int dev) {
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const std::vector<int> nb = allocate_blocks(batch, sms);
+  std::vector<int> nb(batch.size());
+  for (size_t i = 0; i < batch.size(); ++i) nb[i] = wanted_blocks_sms(batch[i]->ls, sms);
   BatchList list;
   list.n = (int)batch.size();
   int b0 = 0;
@@ -270,6 +264,13 @@ int stage_args(eg_ls* ls) {
 
 bool eg_gmres_batching() { return g_batching.load() != 0; }
 
+int eg_gmres_wanted_blocks(const eg_ls* ls) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return wanted_blocks_sms(ls, sms);
+}
+
 void eg_batch_enter(int dev) { batcher(dev).active.fetch_add(1); }
 void eg_batch_leave(int dev) { batcher(dev).active.fetch_sub(1); }
 
@@ -295,12 +296,24 @@ int eg_gmres_coop_batched(eg_ls* ls) {
     const bool late = std::chrono::duration_cast<std::chrono::nanoseconds>(now - B.first).count() >=
                       g_window_ns.load();
     if (!B.launching && !B.pending.empty() && (full || late)) {
-      // lead: take the pending solves of the first one's precision
+      // lead: pack pending solves of the first one's precision, in arrival
+      // order, while their blocks fit on the SMs (first fit; the others wait
+      // for the next launch)
       B.launching = true;
+      int sms = 0;
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
       const int prec = B.pending[0]->ls->lo->prec;
       std::vector<Submission*> batch, rest;
-      for (Submission* s : B.pending)
-        (s->ls->lo->prec == prec && (int)batch.size() < kMaxBatch ? batch : rest).push_back(s);
+      int used = 0;
+      for (Submission* s : B.pending) {
+        const int w = wanted_blocks_sms(s->ls, sms);
+        if (s->ls->lo->prec == prec && (int)batch.size() < kMaxBatch && used + w <= sms) {
+          batch.push_back(s);
+          used += w;
+        } else {
+          rest.push_back(s);
+        }
+      }
       B.pending.swap(rest);
       if (!B.pending.empty()) B.first = now;
       lk.unlock();

@@ -80,8 +80,11 @@ std::mutex& eg_coop_mutex(int dev);
 // eg_set_gmres_batching; eg_gmres_coop then hands the solve to the batcher
 bool eg_gmres_batching();
 int eg_gmres_coop_batched(eg_ls* ls);
-// threads inside eg_newton_solve on a device while batching is on (the
-// batcher waits for their solves before launching)
+// blocks the persistent GMRES kernel gives this solver's system (alone or in
+// a batch)
+int eg_gmres_wanted_blocks(const eg_ls* ls);
+// threads inside eg_newton_solve on a device with a multi-block Krylov solve
+// while batching is on (the batcher waits for their solves before launching)
 void eg_batch_enter(int dev);
 void eg_batch_leave(int dev);
 bool eg_coop_supported();

@@ -496,21 +496,25 @@ extern "C" int eg_newton_solve(eg_mesh* m, double* q, int32_t mem, const eg_newt
   const int64_t N = m->ndof;
   eg_newton_stats s;
   std::memset(&s, 0, sizeof(s));
-  // with batched GMRES, the batcher waits for the solves of the threads in here
-  struct BatchGuard {
-    int dev = -1;
-    BatchGuard() {
-      if (eg_gmres_batching() && cudaGetDevice(&dev) == cudaSuccess) eg_batch_enter(dev);
-      else dev = -1;
-    }
-    ~BatchGuard() {
-      if (dev >= 0) eg_batch_leave(dev);
-    }
-  } batch_guard;
   eg_newton_ws* w = nullptr;
   int st = newton_ws(m, o->precision, o->gmres_restart > 0 ? o->gmres_restart : 30, &w);
   if (st != EG_OK) return st;
   eg_ls* ls = w->ls;
+  // with batched GMRES, the batcher waits for the multi-block solves of the
+  // threads in here
+  struct BatchGuard {
+    int dev = -1;
+    explicit BatchGuard(const eg_ls* ls) {
+      if (eg_gmres_batching() && eg_coop_usable(ls) && eg_gmres_wanted_blocks(ls) > 1 &&
+          cudaGetDevice(&dev) == cudaSuccess)
+        eg_batch_enter(dev);
+      else
+        dev = -1;
+    }
+    ~BatchGuard() {
+      if (dev >= 0) eg_batch_leave(dev);
+    }
+  } batch_guard(ls);
   const int kmax = o->krylov_itermax > 0 ? o->krylov_itermax : 1000;
   st = eg_ls_set_tolerances(ls, o->krylov_reltol, 1e-30, -1, kmax);
   if (st != EG_OK) return st;

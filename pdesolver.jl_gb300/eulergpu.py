@@ -174,7 +174,7 @@ def estimate_mem(mesh, precision=None, restart=30, prolong_from=None):
     return out
 
 
-def set_gmres_batching(enable=True, window_us=200.0):
+def set_gmres_batching(enable=True, window_us=50.0):
     """run the Krylov solves of concurrent Newton solves (one thread per mesh)
     in shared cooperative launches (process-wide switch)."""
     check(library().eg_set_gmres_batching(int(bool(enable)), float(window_us)))

@@ -14,9 +14,11 @@ state) as they arrive and keeps up to `slots` of them on the device at once:
   times, after which nothing passes it until it is admitted;
 * overlap: each slot is a host thread with its own CUDA stream; the library
   calls release the GIL, so the admitted requests' Newton iterations
-  (residual, Jacobian, block inverse, GMRES) run on the device side by side,
-  and a request that arrives while others run starts as soon as a slot and
-  memory free up, not when the batch ends;
+  (residual, Jacobian, block inverse, one-block Krylov solves) run on the
+  device side by side, multi-block Krylov solves take the GPU in turn (or,
+  with batch_gmres, share cooperative launches, each on its own SMs); a
+  request that arrives while others run starts as soon as a slot and memory
+  free up, not when a batch ends;
 * residency: a request's meshes, state, Jacobian and preconditioner stay on
   the device for its whole solve; afterwards its meshes (with the Newton work
   objects they keep) go to an idle pool keyed by geometry, so a later request
@@ -150,13 +152,14 @@ class SteadySolveServer:
 
     def __init__(self, hbm_budget, slots=8, precision=1, retries=2, max_bypass=8,
                  run_request=None, make_meshes=None, close_meshes=None, make_stream=None,
-                 clock=time.perf_counter):
+                 clock=time.perf_counter, batch_gmres=False):
         self.budget = int(hbm_budget)
         self.slots = int(slots)
         self.precision = int(precision)
         self.retries = int(retries)
         self.max_bypass = int(max_bypass)
         self.clock = clock
+        self.batch_gmres = bool(batch_gmres) and run_request is None
         self._run_request = run_request or self._gpu_run_request
         self._make_meshes = make_meshes or self._gpu_make_meshes
         self._close_meshes = close_meshes or self._gpu_close_meshes
@@ -289,6 +292,9 @@ class SteadySolveServer:
                 self._close_meshes(meshes)
 
     def start(self):
+        if self.batch_gmres:
+            from .eulergpu import set_gmres_batching
+            set_gmres_batching(True)
         self._closed = False
         self._threads = [threading.Thread(target=self._worker, daemon=True)
                          for _ in range(self.slots)]
@@ -319,6 +325,9 @@ class SteadySolveServer:
         for t in self._threads:
             t.join()
         self._threads = []
+        if self.batch_gmres:
+            from .eulergpu import set_gmres_batching
+            set_gmres_batching(False)
 
     def close(self):
         """destroy the idle device meshes."""

@@ -124,7 +124,7 @@ def test_served_results_equal_alone(gpu_lib):
     """continuous batching: six requests arriving 20 ms apart, up to four on
     the device at once, give the results of the same requests solved one at
     a time on a fresh server."""
-    mix = serve.SteadySolveServer(8 << 30, slots=4, precision=1)
+    mix = serve.SteadySolveServer(8 << 30, slots=4, precision=1, batch_gmres=True)
     out = mix.serve(_requests())
     mix.close()
     assert all(r.error is None for r in out), [r.error for r in out]
@@ -139,3 +139,29 @@ def test_served_results_equal_alone(gpu_lib):
         assert all(s["converged"] == 1 and s["res_norm"] < 1e-10 for s in m.stats[-1:])
         assert np.abs(m.q - a.q).max() <= 1e-10 * np.abs(a.q).max()
         assert abs(m.functional - a.functional) <= 1e-8 * abs(a.functional)
+
+
+def test_batched_gmres_gives_the_same_bits_as_alone(gpu_lib):
+    """eight steady solves of mixed sizes (one- and multi-block Krylov solves,
+    2-D and 3-D) on eight threads with batched GMRES (several solves per
+    cooperative launch, barriers over each solve's own blocks) give the
+    states and iteration counts of the same solves run one at a time without
+    batching."""
+    import torch
+    from pdesolver_gb300 import batch
+    specs = [{"dim": 2, "n": 6, "p": 3}, {"dim": 2, "n": 10, "p": 2}, {"dim": 2, "n": 12, "p": 1},
+             {"dim": 2, "n": 20, "p": 4}, {"dim": 3, "n": 3, "p": 2}, {"dim": 3, "n": 2, "p": 1},
+             {"dim": 2, "n": 16, "p": 3}, {"dim": 2, "n": 24, "p": 2}]
+    probs = []
+    for k, sp in enumerate(specs):
+        sp.update(M_in=0.35 + 0.04 * k, seed=200 + k)
+        levels, q0 = problems.request_problem(sp)
+        gl = [eulergpu.GPUMesh(ms, o) for ms, o in levels]
+        probs.append(batch.SteadyProblem(levels=gl, q0=torch.from_numpy(q0).cuda(), opts=NEWTON_OPTS,
+                                         level_tol=1e-4, tag=k, work=float(q0.size)))
+    alone = [batch.solve_one(pr, precision=1) for pr in probs]
+    mixed = batch.solve_batch(probs, workers=8, precision=1, batch_gmres=True)
+    for a, b in zip(alone, mixed):
+        assert a.error is None and b.error is None, (a.error, b.error)
+        assert [s.krylov_iters for s in a.stats] == [s.krylov_iters for s in b.stats]
+        assert torch.equal(a.q, b.q)
