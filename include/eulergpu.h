@@ -223,6 +223,9 @@ int eg_lo_apply(eg_lo* lo, const double* x, double* y, int32_t mem);
 /* y = J x with x, y device arrays in the operator's own precision (double
    for EG_F64, float for EG_F32), no conversion; enqueued, no synchronisation */
 int eg_lo_apply_native(eg_lo* lo, const void* x, void* y);
+/* applyLinearOperatorTranspose (reference LinearSolvers.jl:533,
+   lo_petscmat.jl:143-160): y = J^T x; x, y FP64 in host or device memory */
+int eg_lo_apply_transpose(eg_lo* lo, const double* x, double* y, int32_t mem);
 /* copy the blocks to host FP64 arrays: diag [E][Np nv][Np nv],
    coupling [I][2][S nv][S nv] (either may be NULL) */
 int eg_lo_get_blocks(eg_lo* lo, double* diag, double* coupling);
@@ -237,6 +240,8 @@ int eg_pc_calc(eg_pc* pc);
 int eg_pc_apply(eg_pc* pc, const double* x, double* y, int32_t mem);
 /* y = M^-1 x in the operator's own precision on device arrays, enqueued */
 int eg_pc_apply_native(eg_pc* pc, const void* x, void* y);
+/* applyPCTranspose (reference LinearSolvers.jl:277): y = M^-T x */
+int eg_pc_apply_transpose(eg_pc* pc, const double* x, double* y, int32_t mem);
 
 typedef struct {
   int32_t iters;        /* total Krylov iterations                          */

@@ -330,9 +330,53 @@ int eval_jacobian(const eg_mesh_desc* d, const eg_params* ep, const double* q, d
   const int Np = v.Np, Nf = v.Nf, S = v.S, n = Np * NV, nb = S * NV;
   std::memset(diag, 0, sizeof(double) * (size_t)v.E * n * n);
   if (cpl) std::memset(cpl, 0, sizeof(double) * (size_t)d->num_interfaces * 2 * nb * nb);
-  // volume
+  if (ep->volume_integral_type == 2) {
+    // split form: the pair terms of calcVolumeIntegralsSplitFormCurvilinear
+    // (euler_funcs.jl:295-362) differentiated pair by pair, as
+    // calcVolumeIntegralsSplitFormCurvilinear_diff does (euler_funcs_diff.jl:
+    // 330-430): res_j -= 2 S_x[j,k,:] F_IR(q_j, q_k), res_k += the same
+    double nrmD[9] = {0};
+    for (int dd = 0; dd < DIM; ++dd) nrmD[dd * DIM + dd] = 1.0;
+#pragma omp parallel for schedule(static)
+    for (int e = 0; e < v.E; ++e) {
+      std::vector<double> Sx((size_t)DIM * Np * Np, 0.0);
+      for (int d1 = 0; d1 < DIM; ++d1)
+        for (int d2 = 0; d2 < DIM; ++d2)
+          for (int i = 0; i < Np; ++i)
+            for (int j = 0; j < i; ++j) {
+              double& sji = Sx[((size_t)d1 * Np + j) * Np + i];
+              sji += 0.5 * v.dxidx(e, j, d1, d2) * v.Q(d2, j, i) - 0.5 * v.dxidx(e, i, d1, d2) * v.Q(d2, i, j);
+              Sx[((size_t)d1 * Np + i) * Np + j] = -sji;
+            }
+      double* D = diag + (size_t)e * n * n;
+      for (int j = 0; j < Np; ++j)
+        for (int k = 0; k < j; ++k) {
+          Dual<2 * NV> qj[NV], qk[NV], Fd[3 * NV];
+          for (int c = 0; c < NV; ++c) {
+            qj[c] = Dual<2 * NV>(q[((size_t)e * Np + j) * NV + c]);
+            qk[c] = Dual<2 * NV>(q[((size_t)e * Np + k) * NV + c]);
+            qj[c].d[c] = 1.0;
+            qk[c].d[NV + c] = 1.0;
+          }
+          ir_flux<DIM>(p, qj, qk, nrmD, DIM, Fd);
+          for (int dd = 0; dd < DIM; ++dd) {
+            const double s2 = 2 * Sx[((size_t)dd * Np + j) * Np + k];
+            for (int a = 0; a < NV; ++a)
+              for (int b = 0; b < NV; ++b) {
+                const double gj = s2 * Fd[dd * NV + a].d[b], gk = s2 * Fd[dd * NV + a].d[NV + b];
+                D[(size_t)(j * NV + b) * n + j * NV + a] -= gj;
+                D[(size_t)(k * NV + b) * n + j * NV + a] -= gk;
+                D[(size_t)(j * NV + b) * n + k * NV + a] += gj;
+                D[(size_t)(k * NV + b) * n + k * NV + a] += gk;
+              }
+          }
+        }
+    }
+  }
+  // volume (weak form)
 #pragma omp parallel for schedule(static)
   for (int e = 0; e < v.E; ++e) {
+    if (ep->volume_integral_type == 2) continue;
     std::vector<double> A((size_t)DIM * Np * NV * NV);
     for (int m = 0; m < Np; ++m)
       for (int k = 0; k < DIM; ++k) {
@@ -620,7 +664,6 @@ extern "C" {
 
 int oracle_eval_jacobian(const eg_mesh_desc* d, const eg_params* p, const double* q, double* diag,
                          double* cpl) {
-  if (p->volume_integral_type != 1) return EG_ERR_UNSUPPORTED;
   return d->dim == 2 ? eval_jacobian<2>(d, p, q, diag, cpl) : eval_jacobian<3>(d, p, q, diag, cpl);
 }
 

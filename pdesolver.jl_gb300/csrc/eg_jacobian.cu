@@ -14,6 +14,7 @@
 //   diag[E][Np*nv][Np*nv]          element blocks (volume + own face terms)
 //   cpl[I][2][S*nv][S*nv]          interface coupling blocks LR, RL (row-major)
 // Kernels (templated on the precision T of the Jacobian: double or float):
+//   k_elem_jac_split  the element block of the entropy-stable split form
 //   k_face_jac     one thread per (face slot, face node): dF/dqL, dF/dqR
 //   k_elem_jac     one CTA per element: sum_k Q_k(m,j) A_k(q_m) into a shared
 //                  block, then the element's own face terms, coalesced store
@@ -102,16 +103,62 @@ __global__ void k_face_jac(DevMesh md, const double* __restrict__ q, T* __restri
     }
 }
 
+// The element's own face terms (LL for elementL / boundary, RR for
+// elementR) added into the shared block sB of element e, then stored.
+template <int DIM, typename T>
+__device__ void elem_face_terms(const DevMesh& md, const T* __restrict__ dF, T* sB, int e) {
+  constexpr int NV = DIM + 2;
+  constexpr int F = DIM + 1;
+  const int Np = md.Np, Nf = md.Nf, S = md.S;
+  const int n = Np * NV;
+  for (int f = 0; f < F; ++f) {
+    const EFace ef = md.eface[(size_t)e * F + f];
+    const T* dFs = dF + (size_t)ef.slot * Nf * 2 * NV * NV;
+    const int sideoff = ef.side ? NV * NV : 0;  // dF/dq of this element's state
+    const T sgn = ef.side ? T(1) : T(-1);
+    const int* nb = md.nbrperm + ef.orient * Nf;
+    if (md.sparse_face) {
+      // interp = identity: only stencil node s with itself, through the face
+      // node i that sees it, acc = wface[s] dF_i (the dense sum's one term)
+      for (int t = threadIdx.x; t < S * NV * NV; t += blockDim.x) {
+        const int ab = t % (NV * NV), s = t / (NV * NV);
+        const int a = ab / NV, b = ab - a * NV;
+        const int i = ef.side ? md.nbrinv[ef.orient * Nf + s] : s;
+        const T acc = T(md.wface[s]) * dFs[(size_t)i * 2 * NV * NV + sideoff + a * NV + b];
+        const int node = md.perm[f * S + s] * NV;
+        sB[(size_t)(node + b) * n + node + a] += sgn * acc;
+      }
+      __syncthreads();
+      continue;
+    }
+    for (int t = threadIdx.x; t < S * S * NV * NV; t += blockDim.x) {
+      const int ab = t % (NV * NV), ss = t / (NV * NV);
+      const int s = ss / S, sp = ss - s * S;        // row stencil s, column stencil s'
+      const int a = ab / NV, b = ab - a * NV;
+      T acc = T(0);
+      for (int i = 0; i < Nf; ++i) {
+        const int ii = ef.side ? nb[i] : i;         // this element's face-node index
+        const T l = T(md.liftS[((size_t)f * Nf + ii) * S + s]);
+        const T r = T(md.interp[((size_t)f * Nf + ii) * S + sp]);
+        acc += l * r * dFs[(size_t)i * 2 * NV * NV + sideoff + a * NV + b];
+      }
+      const int row = md.perm[f * S + s] * NV + a;
+      const int col = md.perm[f * S + sp] * NV + b;
+      sB[(size_t)col * n + row] += sgn * acc;
+    }
+    __syncthreads();
+  }
+}
+
 // Element block: one CTA per element.  Shared: A[k][m][a][b] (flux
 // Jacobians at the nodes), the block blk[col][row] and face tables.
 template <int DIM, typename T>
 __global__ void k_elem_jac(DevMesh md, const double* __restrict__ q, const T* __restrict__ dF,
                            T* __restrict__ diag) {
   constexpr int NV = DIM + 2;
-  constexpr int F = DIM + 1;
   using D1 = Fwd<T, NV>;
   extern __shared__ unsigned char smraw[];
-  const int Np = md.Np, Nf = md.Nf, S = md.S;
+  const int Np = md.Np;
   const int n = Np * NV;
   T* sA = reinterpret_cast<T*>(smraw);               // [DIM][Np][NV][NV]
   T* sB = sA + (size_t)DIM * Np * NV * NV;            // [n][n] col-major
@@ -153,44 +200,99 @@ __global__ void k_elem_jac(DevMesh md, const double* __restrict__ q, const T* __
     sB[t] = acc;
   }
   __syncthreads();
-  // the element's own face terms (LL for elementL / boundary, RR for elementR)
-  for (int f = 0; f < F; ++f) {
-    const EFace ef = md.eface[(size_t)e * F + f];
-    const T* dFs = dF + (size_t)ef.slot * Nf * 2 * NV * NV;
-    const int sideoff = ef.side ? NV * NV : 0;  // dF/dq of this element's state
-    const T sgn = ef.side ? T(1) : T(-1);
-    const int* nb = md.nbrperm + ef.orient * Nf;
-    if (md.sparse_face) {
-      // interp = identity: only stencil node s with itself, through the face
-      // node i that sees it, acc = wface[s] dF_i (the dense sum's one term)
-      for (int t = threadIdx.x; t < S * NV * NV; t += blockDim.x) {
-        const int ab = t % (NV * NV), s = t / (NV * NV);
-        const int a = ab / NV, b = ab - a * NV;
-        const int i = ef.side ? md.nbrinv[ef.orient * Nf + s] : s;
-        const T acc = T(md.wface[s]) * dFs[(size_t)i * 2 * NV * NV + sideoff + a * NV + b];
-        const int node = md.perm[f * S + s] * NV;
-        sB[(size_t)(node + b) * n + node + a] += sgn * acc;
-      }
-      __syncthreads();
-      continue;
+  elem_face_terms<DIM, T>(md, dF, sB, e);
+  T* dst = diag + (size_t)e * n * n;
+  for (int t = threadIdx.x; t < n * n; t += blockDim.x) dst[t] = sB[t];
+}
+
+// d/dq of the pair term of the split form for the pair (first, second),
+// first > second (residual: res_first -= G, res_second += G with
+// G = F_IR(q_first, q_second; n), n = 2 S_x[first, second, :]), with respect
+// to q_first (wrt_first) or q_second, times sign, added into blk[a][b].
+template <int DIM, typename T>
+__device__ void split_pair_jac(const DevMesh& md, const Gas& g, const double* __restrict__ qe,
+                               const double* __restrict__ dxe, const T* sQ, int first, int second,
+                               bool wrt_first, T sign, T (&blk)[DIM + 2][DIM + 2]) {
+  constexpr int NV = DIM + 2;
+  using D1 = Fwd<T, NV>;
+  const int Np = md.Np;
+  const double* d1 = dxe + (size_t)first * DIM * DIM;
+  const double* d2 = dxe + (size_t)second * DIM * DIM;
+  T nrm[DIM];
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    T acc = T(0);
+#pragma unroll
+    for (int m = 0; m < DIM; ++m) {
+      // Q_m(first, second) = sQ[m][second][first]; Q_m(second, first) = sQ[m][first][second]
+      acc += T(d1[d * DIM + m]) * sQ[((size_t)m * Np + second) * Np + first];
+      acc -= T(d2[d * DIM + m]) * sQ[((size_t)m * Np + first) * Np + second];
     }
-    for (int t = threadIdx.x; t < S * S * NV * NV; t += blockDim.x) {
-      const int ab = t % (NV * NV), ss = t / (NV * NV);
-      const int s = ss / S, sp = ss - s * S;        // row stencil s, column stencil s'
-      const int a = ab / NV, b = ab - a * NV;
-      T acc = T(0);
-      for (int i = 0; i < Nf; ++i) {
-        const int ii = ef.side ? nb[i] : i;         // this element's face-node index
-        const T l = T(md.liftS[((size_t)f * Nf + ii) * S + s]);
-        const T r = T(md.interp[((size_t)f * Nf + ii) * S + sp]);
-        acc += l * r * dFs[(size_t)i * 2 * NV * NV + sideoff + a * NV + b];
-      }
-      const int row = md.perm[f * S + s] * NV + a;
-      const int col = md.perm[f * S + sp] * NV + b;
-      sB[(size_t)col * n + row] += sgn * acc;
-    }
-    __syncthreads();
+    nrm[d] = acc;
   }
+  D1 qa[NV], qb[NV], G[NV];
+#pragma unroll
+  for (int c = 0; c < NV; ++c) {
+    qa[c] = D1(T(qe[(size_t)first * NV + c]));
+    qb[c] = D1(T(qe[(size_t)second * NV + c]));
+    if (wrt_first)
+      qa[c].d[c] = T(1);
+    else
+      qb[c].d[c] = T(1);
+  }
+  auto av = eg::ir_average<DIM>(g, qa, qb);
+  eg::ir_dir<DIM>(av, nrm, G);
+#pragma unroll
+  for (int a = 0; a < NV; ++a)
+#pragma unroll
+    for (int b = 0; b < NV; ++b) blk[a][b] += sign * G[a].d[b];
+}
+
+// Element block of the entropy-stable split form (volume_integral_type 2):
+// the Hadamard pair terms differentiated pair by pair (reference
+// calcVolumeIntegralsSplitFormCurvilinear_diff, euler_funcs_diff.jl:330-430),
+// then the same face terms as the weak form.  One thread per (row node j,
+// column node m) block of the element: an off-diagonal block is the one pair
+// (j, m); a diagonal block sums the pairs of node j, in a fixed order.
+template <int DIM, typename T>
+__global__ void k_elem_jac_split(DevMesh md, const double* __restrict__ q, const T* __restrict__ dF,
+                                 T* __restrict__ diag) {
+  constexpr int NV = DIM + 2;
+  extern __shared__ unsigned char smraw[];
+  const int Np = md.Np;
+  const int n = Np * NV;
+  T* sB = reinterpret_cast<T*>(smraw);                // [n][n] col-major
+  T* sQ = sB + (size_t)n * n;                         // [DIM][Np][Np] = Q
+  const int e = blockIdx.x;
+  for (int t = threadIdx.x; t < DIM * Np * Np; t += blockDim.x) sQ[t] = T(md.Q[t]);
+  __syncthreads();
+  const Gas g{md.gamma, md.gamma_1};
+  const double* qe = q + (size_t)e * Np * NV;
+  const double* dxe = md.dxidx + (size_t)e * Np * DIM * DIM;
+  for (int t = threadIdx.x; t < Np * Np; t += blockDim.x) {
+    const int j = t / Np, m = t - j * Np;  // row node j, column node m
+    T blk[NV][NV];
+#pragma unroll
+    for (int a = 0; a < NV; ++a)
+#pragma unroll
+      for (int b = 0; b < NV; ++b) blk[a][b] = T(0);
+    if (m < j) {
+      split_pair_jac<DIM, T>(md, g, qe, dxe, sQ, j, m, false, T(-1), blk);  // res_j -= G(q_j, q_m)
+    } else if (m > j) {
+      split_pair_jac<DIM, T>(md, g, qe, dxe, sQ, m, j, true, T(1), blk);   // res_j += G(q_m, q_j)
+    } else {
+      for (int k = 0; k < Np; ++k) {
+        if (k < j) split_pair_jac<DIM, T>(md, g, qe, dxe, sQ, j, k, true, T(-1), blk);
+        else if (k > j) split_pair_jac<DIM, T>(md, g, qe, dxe, sQ, k, j, false, T(1), blk);
+      }
+    }
+#pragma unroll
+    for (int a = 0; a < NV; ++a)
+#pragma unroll
+      for (int b = 0; b < NV; ++b) sB[(size_t)(m * NV + b) * n + j * NV + a] = blk[a][b];
+  }
+  __syncthreads();
+  elem_face_terms<DIM, T>(md, dF, sB, e);
   T* dst = diag + (size_t)e * n * n;
   for (int t = threadIdx.x; t < n * n; t += blockDim.x) dst[t] = sB[t];
 }
@@ -277,14 +379,25 @@ int launch_jac(eg_lo* lo, const double* q) {
   const size_t smem = sizeof(T) * ((size_t)m->dim * m->Np * m->nv * m->nv + (size_t)n * n +
                                    (size_t)m->dim * m->Np * m->Np);
   eg_phase_begin(m, EG_PHASE_OTHER);
+  const bool split = m->params.volume_integral_type == 2;
   if (m->dim == 2) {
     k_face_jac<2, T><<<(nslot + 127) / 128, 128, 0, m->stream>>>(md, q, dF);
-    cudaFuncSetAttribute(k_elem_jac<2, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    k_elem_jac<2, T><<<m->E, 256, smem, m->stream>>>(md, q, dF, diag);
+    if (split) {
+      cudaFuncSetAttribute(k_elem_jac_split<2, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+      k_elem_jac_split<2, T><<<m->E, 256, smem, m->stream>>>(md, q, dF, diag);
+    } else {
+      cudaFuncSetAttribute(k_elem_jac<2, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+      k_elem_jac<2, T><<<m->E, 256, smem, m->stream>>>(md, q, dF, diag);
+    }
   } else {
     k_face_jac<3, T><<<(nslot + 127) / 128, 128, 0, m->stream>>>(md, q, dF);
-    cudaFuncSetAttribute(k_elem_jac<3, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    k_elem_jac<3, T><<<m->E, 256, smem, m->stream>>>(md, q, dF, diag);
+    if (split) {
+      cudaFuncSetAttribute(k_elem_jac_split<3, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+      k_elem_jac_split<3, T><<<m->E, 256, smem, m->stream>>>(md, q, dF, diag);
+    } else {
+      cudaFuncSetAttribute(k_elem_jac<3, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+      k_elem_jac<3, T><<<m->E, 256, smem, m->stream>>>(md, q, dF, diag);
+    }
   }
   const int64_t ncpl = (int64_t)eg_lo_coupling_size(lo);
   if (ncpl > 0) {
@@ -313,10 +426,6 @@ int eg_jacobian_launch(eg_lo* lo, const double* q) {
                               (size_t)lo->n * lo->n);
   if (smem_needed > 200 * 1024) {
     eg_set_error("evalJacobian: element block of %d unknowns exceeds shared memory", lo->n);
-    return EG_ERR_UNSUPPORTED;
-  }
-  if (lo->mesh->params.volume_integral_type != 1) {
-    eg_set_error("evalJacobian: only the weak-form volume integral (type 1) is differentiated");
     return EG_ERR_UNSUPPORTED;
   }
   return lo->prec == EG_F64 ? launch_jac<double>(lo, q) : launch_jac<float>(lo, q);

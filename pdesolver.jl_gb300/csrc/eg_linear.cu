@@ -335,6 +335,88 @@ int pcapply_T(eg_pc* pc, const T* x, T* y, const int* done = nullptr) {
   return EG_OK;
 }
 
+// ------------------------------------------------------------ transposes
+// y = J^T x (applyLinearOperatorTranspose, LinearSolvers.jl:533; the PETSc
+// operator runs MatMultTranspose, lo_petscmat.jl:143-160), one thread per row
+// of y.  Row (e, j, a) of J^T is column (e, j, a) of J: column r of e's element
+// block, plus, for each interface face of e whose stencil holds node j, column
+// (s, a) of the neighbour's coupling block (the block whose rows are the
+// neighbour's stencil and whose columns are e's).
+template <int DIM, typename T>
+__global__ void k_spmv_t(DevMesh md, const T* __restrict__ diag, const T* __restrict__ cpl,
+                         const int* __restrict__ spos, const T* __restrict__ x, T* __restrict__ y,
+                         int n) {
+  constexpr int NV = DIM + 2;
+  constexpr int F = DIM + 1;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= (int64_t)md.E * n) return;
+  const int e = (int)(t / n), r = (int)(t - (int64_t)e * n);
+  const T* col = diag + ((size_t)e * n + r) * n;  // column r of the element block
+  const T* xe = x + (size_t)e * n;
+  T acc = T(0);
+  for (int i = 0; i < n; ++i) acc += col[i] * xe[i];
+  const int Np = md.Np, S = md.S, nb = S * NV, Nf = md.Nf;
+  const int j = r / NV, a = r - j * NV;
+  for (int f = 0; f < F; ++f) {
+    const int s = spos[f * Np + j];
+    if (s < 0) continue;
+    const EFace ef = md.eface[(size_t)e * F + f];
+    if (ef.slot >= md.I) continue;
+    const int* itf = md.ifaces + 5 * ef.slot;
+    const int en = ef.side ? itf[0] : itf[1];
+    const int fn = ef.side ? itf[2] : itf[3];
+    const int o = itf[4];
+    const int blk = ef.slot * 2 + (1 - ef.side);  // rows: the neighbour's stencil
+    const T* xn = x + (size_t)en * n;
+    if (md.sparse_face) {
+      // the neighbour's row node facing e's node s
+      const int sp = (1 - ef.side) == 0 ? md.nbrinv[o * Nf + s] : md.nbrperm[o * Nf + s];
+      const T* C = cpl + ((size_t)blk * S + sp) * NV * NV;
+      const T* xs = xn + md.perm[fn * S + sp] * NV;
+      for (int b = 0; b < NV; ++b) acc += C[b * NV + a] * xs[b];
+    } else {
+      const T* C = cpl + (size_t)blk * nb * nb;  // row-major [row][col]
+      for (int sp = 0; sp < S; ++sp) {
+        const T* xs = xn + md.perm[fn * S + sp] * NV;
+        for (int b = 0; b < NV; ++b) acc += C[(size_t)(sp * NV + b) * nb + s * NV + a] * xs[b];
+      }
+    }
+  }
+  y[t] = acc;
+}
+
+// y = M^-T x (applyPCTranspose, LinearSolvers.jl:277): the transposed element
+// inverses, one thread per row
+template <typename T>
+__global__ void k_block_apply_t(const T* __restrict__ inv, const T* __restrict__ x, T* __restrict__ y,
+                                int E, int n) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= (int64_t)E * n) return;
+  const int e = (int)(t / n), r = (int)(t - (int64_t)e * n);
+  const T* col = inv + ((size_t)e * n + r) * n;
+  const T* xe = x + (size_t)e * n;
+  T acc = T(0);
+  for (int i = 0; i < n; ++i) acc += col[i] * xe[i];
+  y[t] = acc;
+}
+
+template <typename T>
+void launch_transpose(eg_lo* lo, const T* inv, const T* x, T* y) {
+  eg_mesh* m = lo->mesh;
+  const int64_t rows = (int64_t)m->E * lo->n;
+  const int blocks = (int)((rows + 255) / 256);
+  eg_phase_begin(m, EG_PHASE_OTHER);
+  if (inv)
+    k_block_apply_t<T><<<blocks, 256, 0, m->stream>>>(inv, x, y, m->E, lo->n);
+  else if (m->dim == 2)
+    k_spmv_t<2, T><<<blocks, 256, 0, m->stream>>>(dev_mesh(m), (const T*)lo->diag, (const T*)lo->cpl,
+                                                  lo->spos, x, y, lo->n);
+  else
+    k_spmv_t<3, T><<<blocks, 256, 0, m->stream>>>(dev_mesh(m), (const T*)lo->diag, (const T*)lo->cpl,
+                                                  lo->spos, x, y, lo->n);
+  eg_phase_end(m, EG_PHASE_OTHER, 1);
+}
+
 // Register-tiled Gauss-Jordan inversion for blocks of 33..128 unknowns, one
 // CTA of 256 threads (8 warps) per element block.  Thread (lane, warp) keeps
 // rows lane + 32 r (r < MR) and columns warp + 8 c (c < MC) in registers.
@@ -661,6 +743,44 @@ extern "C" int eg_lo_apply(eg_lo* lo, const double* x, double* y, int32_t mem) {
     EG_CUDA(cudaStreamSynchronize(m->stream));
   }
   return EG_OK;
+}
+
+// FP64 interface of the transposed applies: x -> operator precision, apply,
+// back to FP64 (host or device arrays per mem)
+static int apply_transpose(eg_lo* lo, const void* inv, const double* x, double* y, int32_t mem) {
+  eg_mesh* m = lo->mesh;
+  const double* xd = x;
+  if (mem == EG_MEM_HOST) {
+    EG_CUDA(cudaMemcpyAsync(lo->xd, x, 8 * m->ndof, cudaMemcpyHostToDevice, m->stream));
+    xd = lo->xd;
+  }
+  eg_convert(m, xd, lo->xT, lo->prec, m->ndof, 1.0);
+  if (lo->prec == EG_F64)
+    launch_transpose<double>(lo, (const double*)inv, (const double*)lo->xT, (double*)lo->yT);
+  else
+    launch_transpose<float>(lo, (const float*)inv, (const float*)lo->xT, (float*)lo->yT);
+  double* yd = mem == EG_MEM_HOST ? lo->yd : y;
+  eg_convert_back(m, lo->yT, yd, lo->prec, m->ndof);
+  EG_CUDA(cudaGetLastError());
+  if (mem == EG_MEM_HOST) EG_CUDA(cudaMemcpyAsync(y, yd, 8 * m->ndof, cudaMemcpyDeviceToHost, m->stream));
+  EG_CUDA(cudaStreamSynchronize(m->stream));
+  return EG_OK;
+}
+
+extern "C" int eg_lo_apply_transpose(eg_lo* lo, const double* x, double* y, int32_t mem) {
+  if (!lo || !x || !y || !lo->valid) {
+    eg_set_error("eg_lo_apply_transpose: invalid argument or operator not computed");
+    return EG_ERR_INVALID;
+  }
+  return apply_transpose(lo, nullptr, x, y, mem);
+}
+
+extern "C" int eg_pc_apply_transpose(eg_pc* pc, const double* x, double* y, int32_t mem) {
+  if (!pc || !x || !y || !pc->valid) {
+    eg_set_error("eg_pc_apply_transpose: invalid argument or preconditioner not computed");
+    return EG_ERR_INVALID;
+  }
+  return apply_transpose(pc->lo, pc->inv, x, y, mem);
 }
 
 extern "C" int eg_lo_get_blocks(eg_lo* lo, double* diag, double* coupling) {

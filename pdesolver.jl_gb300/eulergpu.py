@@ -73,6 +73,8 @@ def _declare(lib):
     lib.eg_pc_destroy.argtypes = [vp]
     lib.eg_pc_calc.argtypes = [vp]
     lib.eg_pc_apply.argtypes = [vp, vp, vp, C.c_int32]
+    lib.eg_lo_apply_transpose.argtypes = [vp, vp, vp, C.c_int32]
+    lib.eg_pc_apply_transpose.argtypes = [vp, vp, vp, C.c_int32]
     lib.eg_ls_create.argtypes = [vp, vp, C.c_int32, C.POINTER(vp)]
     lib.eg_ls_destroy.argtypes = [vp]
     lib.eg_ls_set_tolerances.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_int32]
@@ -397,6 +399,15 @@ class LinearOperator:
         check(self.lib.eg_lo_apply(self.handle, px, py, mx))
         return y
 
+    def apply_transpose(self, x, y):
+        """y = J^T x (reference applyLinearOperatorTranspose)."""
+        px, mx = GPUMesh._ptr(x, self.g.ndof)
+        py, my = GPUMesh._ptr(y, self.g.ndof)
+        if mx != my:
+            raise ValueError("x and y must both be host or both be device arrays")
+        check(self.lib.eg_lo_apply_transpose(self.handle, px, py, mx))
+        return y
+
     @property
     def native_dtype(self):
         return "torch.float32" if self.precision == 1 else "torch.float64"
@@ -446,6 +457,15 @@ class BlockJacobiPC:
         if mx != my:
             raise ValueError("x and y must both be host or both be device arrays")
         check(self.lib.eg_pc_apply(self.handle, px, py, mx))
+        return y
+
+    def apply_transpose(self, x, y):
+        """y = M^-T x (reference applyPCTranspose)."""
+        px, mx = GPUMesh._ptr(x, self.lo.g.ndof)
+        py, my = GPUMesh._ptr(y, self.lo.g.ndof)
+        if mx != my:
+            raise ValueError("x and y must both be host or both be device arrays")
+        check(self.lib.eg_pc_apply_transpose(self.handle, px, py, mx))
         return y
 
     def apply_native(self, x_dev, y_dev):

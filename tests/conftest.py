@@ -91,3 +91,18 @@ def block_apply(ms, diag, cpl, x):
         y[eL, iL] += cpl[k, 0].T @ xe[eR, iR]
         y[eR, iR] += cpl[k, 1].T @ xe[eL, iL]
     return y.reshape(x.shape)
+
+
+def block_apply_t(ms, diag, cpl, x):
+    """y = J^T x for the element-block storage (host, numpy)."""
+    E, n = diag.shape[0], diag.shape[1]
+    op = ms.sbp
+    nv = ms.numDofPerNode
+    xe = x.reshape(E, n)
+    y = np.einsum("ecr,er->ec", diag, xe)
+    for k, (eL, eR, fL, fR, o) in enumerate(ms.interfaces):
+        iL = (op.perm[fL][:, None] * nv + np.arange(nv)[None]).ravel()
+        iR = (op.perm[fR][:, None] * nv + np.arange(nv)[None]).ravel()
+        y[eR, iR] += cpl[k, 0] @ xe[eL, iL]
+        y[eL, iL] += cpl[k, 1] @ xe[eR, iR]
+    return y.reshape(x.shape)

@@ -256,6 +256,25 @@ def test_explicit_jacobian_vs_dual_jvp(oracle, fam, p, flux):
         assert np.abs(b1 - b2).max() < 1e-11 * max(1.0, np.abs(b2).max())
 
 
+@pytest.mark.parametrize("p", [1, 2])
+def test_split_form_jacobian_vs_dual_jvp(oracle, p):
+    """the entropy-stable split-form volume Jacobian (pair by pair, as
+    calcVolumeIntegralsSplitFormCurvilinear_diff, euler_funcs_diff.jl:330-430)
+    with IR faces on the warped cube equals the residual's directional
+    derivative at 1e-11."""
+    from conftest import block_apply, oracle_jacobian, oracle_jvp
+    ms, opts, q = problems.config3(n=2, p=p, seed=33)
+    desc = abi.MeshDesc(ms)
+    P = eulergpu_params(opts)
+    diag, cpl = oracle_jacobian(oracle, desc, P, ms, q)
+    rng = np.random.default_rng(5)
+    for _ in range(2):
+        v = rng.normal(size=q.shape)
+        b1 = block_apply(ms, diag, cpl, v)
+        b2 = oracle_jvp(oracle, desc, P, q, v)
+        assert np.abs(b1 - b2).max() < 1e-11 * max(1.0, np.abs(b2).max())
+
+
 def eulergpu_params(opts):
     from pdesolver_gb300 import eulergpu
     return eulergpu.params_from_opts(opts)
