@@ -157,6 +157,11 @@ int eg_calc_norm(eg_mesh* mesh, const double* r, int32_t strongres, int32_t mem,
  */
 int eg_calc_functional(eg_mesh* mesh, const double* q, int32_t bc_group, int32_t mem, double* out);
 
+/* calcMaxWaveSpeed (reference src/solver/euler/euler_funcs.jl:1810-1834):
+   max over the nodes of a + |u|, the wave speed of the CFL time step
+   delta_t = CFL * min_el_size / wave_speed (startup_func.jl:241-247). */
+int eg_calc_max_wave_speed(eg_mesh* mesh, const double* q, int32_t mem, double* out);
+
 /* ---- streams, asynchronous launch and phase timers ---------------------- */
 
 /* Run this mesh's work on `stream` (a cudaStream_t; NULL is CUDA's default

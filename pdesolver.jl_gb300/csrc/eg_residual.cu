@@ -292,6 +292,49 @@ __global__ void k_functional_pressure(DevMesh md, const double* __restrict__ q, 
   if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
 }
 
+// calcMaxWaveSpeed (reference euler_funcs.jl:1810-1834): max over the nodes
+// of a + |u|, a = sqrt(gamma p / rho); per-block maxima, then one block
+template <int DIM, int NT>
+__global__ void k_wave_speed_partial(const double* __restrict__ q, int64_t nnode, double gamma,
+                                     double gamma_1, double* __restrict__ part) {
+  constexpr int NV = DIM + 2;
+  __shared__ double sh[NT];
+  const Gas g{gamma, gamma_1};
+  double mx = 0.0;
+  for (int64_t k = blockIdx.x * (int64_t)NT + threadIdx.x; k < nnode; k += (int64_t)gridDim.x * NT) {
+    const double* qk = q + k * NV;
+    const double p = eg::pressure<DIM>(g, qk);
+    double u2 = 0.0;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      const double u = qk[d + 1] / qk[0];
+      u2 = fma(u, u, u2);
+    }
+    mx = fmax(mx, sqrt(gamma * p / qk[0]) + sqrt(u2));
+  }
+  sh[threadIdx.x] = mx;
+  __syncthreads();
+  for (int w = NT / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sh[threadIdx.x] = fmax(sh[threadIdx.x], sh[threadIdx.x + w]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+template <int NT>
+__global__ void k_max_final(const double* __restrict__ part, int n, double* __restrict__ out) {
+  __shared__ double sh[NT];
+  double mx = 0.0;
+  for (int k = threadIdx.x; k < n; k += NT) mx = fmax(mx, part[k]);
+  sh[threadIdx.x] = mx;
+  __syncthreads();
+  for (int w = NT / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sh[threadIdx.x] = fmax(sh[threadIdx.x], sh[threadIdx.x + w]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[0] = sh[0];
+}
+
 template <int NT>
 __global__ void k_sum_final(const double* __restrict__ part, int n, double* __restrict__ out) {
   __shared__ double sh[NT];
@@ -497,6 +540,32 @@ extern "C" int eg_calc_norm(eg_mesh* m, const double* r, int32_t strongres, int3
   eg_launch_norm(m, rd, strongres, m->red + 2048);
   EG_CUDA(cudaGetLastError());
   EG_CUDA(cudaMemcpyAsync(m->h_red, m->red + 2048, sizeof(double), cudaMemcpyDeviceToHost, m->stream));
+  EG_CUDA(cudaStreamSynchronize(m->stream));
+  *out = m->h_red[0];
+  return EG_OK;
+}
+
+extern "C" int eg_calc_max_wave_speed(eg_mesh* m, const double* q, int32_t mem, double* out) {
+  if (!m || !q || !out) {
+    eg_set_error("eg_calc_max_wave_speed: NULL argument");
+    return EG_ERR_INVALID;
+  }
+  const double* qd = q;
+  if (mem == EG_MEM_HOST) {
+    EG_CUDA(cudaMemcpyAsync(m->q_dev, q, sizeof(double) * (size_t)m->ndof, cudaMemcpyHostToDevice, m->stream));
+    qd = m->q_dev;
+  }
+  const int64_t nnode = (int64_t)m->E * m->Np;
+  int blocks = (int)((nnode + 255) / 256);
+  if (blocks > 1024) blocks = 1024;
+  if (m->dim == 2)
+    k_wave_speed_partial<2, 256><<<blocks, 256, 0, m->stream>>>(qd, nnode, m->dp.gamma, m->dp.gamma_1, m->red);
+  else
+    k_wave_speed_partial<3, 256><<<blocks, 256, 0, m->stream>>>(qd, nnode, m->dp.gamma, m->dp.gamma_1, m->red);
+  k_max_final<256><<<1, 256, 0, m->stream>>>(m->red, blocks, m->red + 2051);
+  m->launches += 2;
+  EG_CUDA(cudaGetLastError());
+  EG_CUDA(cudaMemcpyAsync(m->h_red, m->red + 2051, sizeof(double), cudaMemcpyDeviceToHost, m->stream));
   EG_CUDA(cudaStreamSynchronize(m->stream));
   *out = m->h_red[0];
   return EG_OK;

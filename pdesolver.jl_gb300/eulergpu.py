@@ -61,6 +61,7 @@ def _declare(lib):
     lib.eg_get_timings.argtypes = [vp, C.POINTER(Timings)]
     lib.eg_reset_timings.argtypes = [vp]
     lib.eg_calc_functional.argtypes = [vp, vp, C.c_int32, C.c_int32, dp]
+    lib.eg_calc_max_wave_speed.argtypes = [vp, vp, C.c_int32, dp]
     lib.eg_prolong.argtypes = [vp, vp, vp, vp, vp, C.c_int32]
     lib.eg_lo_create.argtypes = [vp, C.c_int32, C.POINTER(vp)]
     lib.eg_lo_destroy.argtypes = [vp]
@@ -307,6 +308,18 @@ class GPUMesh:
         out = C.c_double()
         check(self.lib.eg_calc_functional(self.handle, pq, bc_group, mq, C.byref(out)))
         return out.value
+
+    def max_wave_speed(self, q):
+        """calcMaxWaveSpeed: max over the nodes of a + |u| (euler_funcs.jl:1810)."""
+        pq, mq = self._ptr(q, self.ndof)
+        out = C.c_double()
+        check(self.lib.eg_calc_max_wave_speed(self.handle, pq, mq, C.byref(out)))
+        return out.value
+
+    def cfl_time_step(self, q, cfl):
+        """delta_t = CFL * min_el_size / wave_speed (startup_func.jl:241-247);
+        min_el_size is the shortest element edge of the mesh."""
+        return cfl * self.mesh.min_el_size / self.max_wave_speed(q)
 
     def newton(self, q, opts=None, precision=0):
         """steady Newton solve in place (reference newton.jl:54); returns stats.

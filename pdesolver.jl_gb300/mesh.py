@@ -49,6 +49,7 @@ class Mesh:
     nrm_bndry: np.ndarray
     bndry_tag: np.ndarray         # geometric boundary id of each boundary face
     name: str = ""
+    min_el_size: float = 0.0      # shortest element edge (the CFL length scale)
 
     @property
     def numEl(self):
@@ -224,7 +225,15 @@ def annulus(sbp: SBPOperator, nr: int, ntheta: int, r_in=1.0, r_out=3.0,
     nrm_b = _face_normals(sbp, dxf, bfaces)
     crd_b = fpts[bfaces[:, 0], bfaces[:, 1]]
     return Mesh(2, sbp, coords, dxidx, jac, iface, nbrperm, nrm_f, crd_f, bfaces, offs,
-                bct, crd_b, nrm_b, tags, name=f"annulus{nr}x{ntheta}")
+                bct, crd_b, nrm_b, tags, name=f"annulus{nr}x{ntheta}",
+                min_el_size=_min_edge(X, ((0, 1), (1, 2), (0, 2))))
+
+
+def _min_edge(X, edges):
+    """shortest straight edge over the elements' vertices X [E, nvert, d]
+    (the reference takes mesh.min_el_size from PUMI; the edge length is
+    this build's definition of it)."""
+    return float(min(np.linalg.norm(X[:, a] - X[:, b], axis=1).min() for a, b in edges))
 
 
 def _bary_tri(xi):
@@ -346,4 +355,46 @@ def cube(sbp: SBPOperator, n: int, warp=0.05, seed=3, bc=BC_FREESTREAM) -> Mesh:
     nrm_b = _face_normals(sbp, fdx, bfaces)
     crd_b = fpts[bfaces[:, 0], bfaces[:, 1]]
     return Mesh(3, sbp, coords, dxidx, jac, iface, nbrperm, nrm_f, crd_f, bfaces, offs,
-                bct, crd_b, nrm_b, tags, name=f"cube{n}")
+                bct, crd_b, nrm_b, tags, name=f"cube{n}",
+                min_el_size=_min_edge(G[:, :4], _TET_EDGES))
+
+
+# ---------------------------------------------------------------- on-disk form
+# A neutral description of a Mesh: every array the hot path reads (the fields
+# of the reference's AbstractMesh that evalResidual / evalJacobian touch,
+# docs/src/interfaces.md), the boundary tags and the operator's identity
+# (dimension, family, degree; the operator is rebuilt, not stored).  The
+# reference reads PUMI .smb files, which need PUMI; this is the stand-in for
+# bringing a mesh from another tool.
+_MESH_ARRAYS = ("coords", "dxidx", "jac", "interfaces", "nbrperm", "nrm_face", "coords_face",
+                "bndryfaces", "bndry_offsets", "bc_types", "coords_bndry", "nrm_bndry", "bndry_tag")
+
+
+def save_mesh(path, mesh: Mesh):
+    """write `mesh` to an .npz file (see load_mesh)."""
+    np.savez_compressed(path, **{k: getattr(mesh, k) for k in _MESH_ARRAYS},
+                        dim=mesh.dim, sbp_family=mesh.sbp.family, sbp_p=mesh.sbp.p,
+                        name=mesh.name, min_el_size=mesh.min_el_size)
+
+
+def load_mesh(path) -> Mesh:
+    """read a mesh written by save_mesh; the SBP operator is rebuilt from its
+    family and degree, and the arrays are checked against its node counts."""
+    from . import sbp as _sbp
+    with np.load(path, allow_pickle=False) as z:
+        dim = int(z["dim"])
+        op = _sbp.get_operator(dim, str(z["sbp_family"]), int(z["sbp_p"]))
+        arrs = {k: np.array(z[k]) for k in _MESH_ARRAYS}
+        name, h = str(z["name"]), float(z["min_el_size"])
+    E, Np = arrs["coords"].shape[:2]
+    if Np != op.numnodes or arrs["coords"].shape[2] != dim:
+        raise ValueError(f"coords {arrs['coords'].shape} do not match the {op.family} p={op.p} operator")
+    if arrs["dxidx"].shape != (E, Np, dim, dim) or arrs["jac"].shape != (E, Np):
+        raise ValueError("metric arrays do not match the element and node counts")
+    I = arrs["interfaces"].shape[0]
+    if arrs["nrm_face"].shape != (I, op.numfacenodes, dim):
+        raise ValueError("interface normals do not match the interfaces and face nodes")
+    return Mesh(dim, op, arrs["coords"], arrs["dxidx"], arrs["jac"], arrs["interfaces"],
+                arrs["nbrperm"], arrs["nrm_face"], arrs["coords_face"], arrs["bndryfaces"],
+                arrs["bndry_offsets"], arrs["bc_types"], arrs["coords_bndry"], arrs["nrm_bndry"],
+                arrs["bndry_tag"], name=name, min_el_size=h)

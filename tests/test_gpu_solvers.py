@@ -325,3 +325,28 @@ def test_newton_entropy_stable_3d_matches_oracle(gpu_lib, oracle):
     st = g.newton(q32, NEWTON_OPTS, precision=1)
     assert st.converged == 1 and st.res_norm < 1e-10
     assert abs(g.functional_pressure(q32, 0) - fo) <= 1e-8 * abs(fo)
+
+
+def test_config1_rk4_at_cfl(gpu_lib, oracle):
+    """Config 1 (b): 100 RK4 steps of the 512-triangle vortex annulus at CFL
+    0.4, delta_t = CFL min_el_size / max wave speed (startup_func.jl:241-247,
+    calcMaxWaveSpeed euler_funcs.jl:1810-1834), against the oracle's RK4 at
+    1e-11; the wave speed against numpy at 1e-14."""
+    ms, opts, q0 = problems.config1()
+    g = eulergpu.GPUMesh(ms, opts)
+    rho = q0[..., 0]
+    u = q0[..., 1:3] / rho[..., None]
+    p = 0.4 * (q0[..., 3] - 0.5 * rho * (u ** 2).sum(-1))
+    ref = (np.sqrt(1.4 * p / rho) + np.sqrt((u ** 2).sum(-1))).max()
+    assert abs(g.max_wave_speed(q0) - ref) <= 1e-14 * ref
+    h = g.cfl_time_step(q0, 0.4)
+    assert h == pytest.approx(0.4 * ms.min_el_size / ref, rel=1e-14)
+    qg = q0.copy()
+    st = g.rk4(qg, h, 100 * h)
+    assert st.steps == 100
+    qo = q0.copy()
+    sto = eulergpu.Rk4Stats()
+    assert oracle.oracle_rk4(C.byref(g.desc.desc), C.byref(g.params), abi.dptr(qo), C.c_double(h),
+                             C.c_double(100 * h), 0, C.c_double(-1.0), C.byref(sto)) == 0
+    assert sto.steps == 100
+    assert np.abs(qg - qo).max() <= 1e-11 * np.abs(qo).max()
