@@ -318,7 +318,7 @@ class GPUMesh:
 
     def cfl_time_step(self, q, cfl):
         """delta_t = CFL * min_el_size / wave_speed (startup_func.jl:241-247);
-        min_el_size is the shortest element edge of the mesh."""
+        min_el_size is the smallest node spacing of an element (mesh.py)."""
         return cfl * self.mesh.min_el_size / self.max_wave_speed(q)
 
     def newton(self, q, opts=None, precision=0):
