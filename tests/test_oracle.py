@@ -156,6 +156,38 @@ def test_ir_flux_properties(oracle):
         np.testing.assert_allclose(Fm[d], ir(oracle, qL, qR, dirs[d]), rtol=1e-14)
 
 
+def _entropy_vars(q, gamma=1.4):
+    """v = dU/dq of U = -rho s / (gamma - 1), s = log p - gamma log rho."""
+    dim = len(q) - 2
+    rho, m, E = q[0], q[1:dim + 1], q[dim + 1]
+    p = (gamma - 1) * (E - 0.5 * (m @ m) / rho)
+    s = math.log(p) - gamma * math.log(rho)
+    u = m / rho
+    return np.concatenate([[(gamma - s) / (gamma - 1) - 0.5 * rho * (u @ u) / p], m / p, [-rho / p]])
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_ir_flux_is_entropy_conservative(oracle, dim):
+    """The property behind the entropy-conservation lemmas of
+    test/euler/test_ESS.jl:447-580 (face integrals) and the split-form volume
+    terms: Tadmor's condition (v_L - v_R) . F_IR(q_L, q_R; n) = (psi_L -
+    psi_R) . n with psi = rho u (test_ESS.jl:89-97), at 1e-12."""
+    rng = np.random.default_rng(40 + dim)
+    for _ in range(20):
+        qs = []
+        for _ in range(2):
+            rho = rng.uniform(0.5, 2.0)
+            u = rng.uniform(-0.8, 0.8, size=dim)
+            p = rng.uniform(0.3, 1.5)
+            qs.append(np.concatenate([[rho], rho * u, [p / 0.4 + 0.5 * rho * (u @ u)]]))
+        qL, qR = qs
+        n = rng.normal(size=dim)
+        F = ir(oracle, qL, qR, n)
+        lhs = (_entropy_vars(qL) - _entropy_vars(qR)) @ F
+        rhs = (qL[1:dim + 1] - qR[1:dim + 1]) @ n
+        assert abs(lhs - rhs) <= 1e-12 * max(1.0, abs(rhs))
+
+
 def test_logavg(oracle):
     """bc_solvers.jl:942-956: log mean is symmetric, exact at aL == aR, and
     continuous across the series threshold (test_jac.jl:2001-2050 probes it)."""
