@@ -72,6 +72,14 @@ enum { F_DONE = 0, F_JDONE = 1, F_ITS = 2, F_CONV = 3, F_ITERMAX = 4, F_REORTH =
 enum { S_TOL = 0, S_RESID = 1, S_BETA = 2, S_BNORM = 3, S_RELTOL = 4, S_ABSTOL = 5, S_BETA0 = 6 };
 // the whole GMRES solve as one persistent cooperative kernel (eg_arnoldi.cu)
 #define EG_COOP_MAX_BLOCKS 1024
+// blocks of the stream GMRES path's reduction kernels (4 per SM)
+#define EG_GMRES_STREAM_BLOCKS 608
+// partial-sum slots of a GMRES(m) solver: the stream path's [blocks][m+2][2]
+// or the persistent kernel's [4][blocks][33], whichever is larger
+inline size_t eg_gmres_partials(int m) {
+  const size_t a = (size_t)EG_GMRES_STREAM_BLOCKS * (m + 2) * 2, b = (size_t)4 * EG_COOP_MAX_BLOCKS * 33;
+  return a > b ? a : b;
+}
 int eg_gmres_coop(eg_ls* ls);
 // one cooperative GMRES grid at a time per device (held across launch and
 // completion of multi-block grids, single or batched)

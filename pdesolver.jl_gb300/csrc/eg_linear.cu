@@ -932,7 +932,7 @@ extern "C" int eg_ls_create(eg_lo* lo, eg_pc* pc, int32_t restart, eg_ls** out) 
   ls->abstol = 1e-12;
   ls->dtol = 1e5;
   ls->itermax = 1000;    // read_input.jl:496 krylov_itermax
-  ls->nblk = 608;
+  ls->nblk = EG_GMRES_STREAM_BLOCKS;
   const int64_t N = lo->mesh->ndof;
   const size_t es = lo->prec == EG_F64 ? 8 : 4;
   cudaError_t e = cudaMalloc(&ls->V, es * (size_t)(restart + 1) * N);
@@ -942,13 +942,7 @@ extern "C" int eg_ls_create(eg_lo* lo, eg_pc* pc, int32_t restart, eg_ls** out) 
     e = cudaMalloc(&ls->cfs, es * (size_t)lo->mesh->I * 2 * lo->nb);
   if (e == cudaSuccess) e = cudaMalloc(&ls->xT, es * N);
   if (e == cudaSuccess) e = cudaMalloc(&ls->bT, es * N);
-  {
-    // partial sums: stream kernels use nblk * (m + 2) * 2, the persistent
-    // Arnoldi kernel 4 * blocks * 33
-    size_t np = (size_t)ls->nblk * (restart + 2) * 2;
-    if (np < (size_t)4 * EG_COOP_MAX_BLOCKS * 33) np = (size_t)4 * EG_COOP_MAX_BLOCKS * 33;
-    if (e == cudaSuccess) e = cudaMalloc(&ls->part, es * np);
-  }
+  if (e == cudaSuccess) e = cudaMalloc(&ls->part, es * eg_gmres_partials(restart));
   if (e == cudaSuccess) e = cudaMalloc(&ls->h, es * 4 * (restart + 2));
   if (e == cudaSuccess) e = cudaMalloc(&ls->y, es * (restart + 1));
   // Hessenberg, Givens and least-squares state in FP64: H[(m+1) m] | cs[m] |

@@ -104,7 +104,7 @@ extern "C" int eg_estimate_mem(const eg_mem_query* qy, eg_mem_estimate* out) {
     kry.add(es * I * 2 * nb);                   // pushed coupling products
     kry.add(es * N);                            // x
     kry.add(es * N);                            // b
-    kry.add(es * std::max<uint64_t>((uint64_t)608 * (m + 2) * 2, (uint64_t)4 * EG_COOP_MAX_BLOCKS * 33));
+    kry.add(es * eg_gmres_partials((int)m));     // partial sums
     kry.add(es * 4 * (m + 2));                  // h
     kry.add(es * (m + 1));                      // y
     kry.add(8 * ((m + 1) * m + 4 * (m + 1)));   // Hessenberg, Givens, least squares

@@ -119,12 +119,10 @@ class MeshPool:
         self._idle.move_to_end(key)
         self.bytes += nbytes
 
-    def evict(self, keep=None):
-        """remove the least recently used idle entry (not of key `keep`);
-        returns (meshes, bytes) or None.  The caller destroys the meshes."""
+    def evict(self):
+        """remove the least recently used idle entry; returns (meshes, bytes)
+        or None.  The caller destroys the meshes."""
         for key in list(self._idle):
-            if key == keep:
-                continue
             meshes, nbytes = self._idle[key].pop(0)
             if not self._idle[key]:
                 del self._idle[key]
@@ -172,7 +170,6 @@ class SteadySolveServer:
         self._head_bypassed = 0
         self._closed = False
         self._results = {}
-        self._expected = 0
         self._threads = []
         self.peak_bytes = 0
         self.peak_running = 0
@@ -246,7 +243,7 @@ class SteadySolveServer:
         taken = self.pool.take(req.key) if req.key is not None else None
         evicted = []
         while self._in_flight + self.pool.bytes + req.footprint > self.budget:
-            ev = self.pool.evict(keep=None)
+            ev = self.pool.evict()
             if ev is None:
                 break
             evicted.append(ev[0])

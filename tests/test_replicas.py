@@ -63,7 +63,7 @@ def _rank(rank, world, port, work, out):
 
 def test_job_rate_over_two_gloo_ranks():
     work = [3.0, 1.0, 2.0, 2.0, 5.0]
-    with mp.Manager() as mgr:
+    with mp.get_context("spawn").Manager() as mgr:
         out = mgr.dict()
         mp.spawn(_rank, args=(2, _free_port(), work, out), nprocs=2, join=True)
         res = dict(out)
