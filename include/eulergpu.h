@@ -320,7 +320,13 @@ typedef struct {
    norm < res_reltol, or ||dq|| <= step_tol.  q is FP64 in host or device
    memory.  The Jacobian, preconditioner, Krylov basis and work vectors are
    kept by the mesh after the first solve (for this precision and restart
-   length), so later solves on the mesh allocate nothing. */
+   length), so later solves on the mesh allocate nothing.  When the persistent
+   GMRES kernel takes the system and the phase timers are off, each iteration
+   runs as three CUDA graphs around the GMRES launch with one synchronisation
+   (captured on the first solve, on the mesh stream, which must not be the
+   legacy default stream; else the same launches run eagerly, with the same
+   results); q is then iterated in a copy the mesh owns and written back when
+   the solve ends without error. */
 int eg_newton_solve(eg_mesh* mesh, double* q, int32_t mem, const eg_newton_opts* opts,
                     eg_newton_stats* stats);
 
