@@ -325,8 +325,8 @@ typedef struct {
    runs as three CUDA graphs around the GMRES launch with one synchronisation
    (captured on the first solve, on the mesh stream, which must not be the
    legacy default stream; else the same launches run eagerly, with the same
-   results); q is then iterated in a copy the mesh owns and written back when
-   the solve ends without error. */
+   results); q is then iterated in a copy the mesh owns and written back at
+   the end, also when Newton stops unconverged (not after a device error). */
 int eg_newton_solve(eg_mesh* mesh, double* q, int32_t mem, const eg_newton_opts* opts,
                     eg_newton_stats* stats);
 
