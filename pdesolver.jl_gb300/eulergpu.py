@@ -385,6 +385,56 @@ def calcNorm(eqn, res_vec, strongres=False):
     return eqn.gpu.calc_norm(r, strongres)
 
 
+def physicsRhs(mesh, sbp, eqn, opts, rhs_vec=None, t=0.0):
+    """physicsRhs (reference src/jacobian/residual_evaluation.jl:64-84): R(eqn.q)
+    into eqn.res (and rhs_vec when given, which may alias eqn.res_vec); returns
+    calcNorm(R, strongres=true), the M^-1-weighted norm Newton tests."""
+    evalResidual(mesh, sbp, eqn, opts, t)
+    if rhs_vec is not None and rhs_vec is not eqn.res_vec:
+        rhs_vec[...] = eqn.res_vec
+    return calcNorm(eqn, eqn.res_vec, strongres=True)
+
+
+def evalJacobian(mesh, sbp, eqn, opts, assembler, t=0.0):
+    """evalJacobian (reference src/solver/euler/evalJacobian.jl:6-72): the
+    explicit Jacobian at eqn.q into `assembler`, a LinearOperator of this
+    mesh.  Its blocks are overwritten (the reference adds into a matrix its
+    caller zeroed first, jacobian.jl:118-121)."""
+    assembler.calc(eqn.q)
+    return assembler
+
+
+def calcMaxWaveSpeed(mesh, sbp, eqn, opts):
+    """calcMaxWaveSpeed (reference euler_funcs.jl:1810-1834) of eqn.q."""
+    return eqn.gpu.max_wave_speed(eqn.q)
+
+
+def _euler_rhs_only(func):
+    if func is not None and func is not evalResidual and func is not physicsRhs:
+        raise NotImplementedError("the device drivers evaluate the Euler residual only")
+
+
+def newton(func, mesh, sbp, eqn, opts, pmesh=None, precision=0):
+    """newton (reference src/NonlinearSolvers/newton.jl:54): eqn.q is driven
+    to the steady state in place with the options' res_abstol / res_reltol /
+    step_tol / krylov_reltol / newton_globalize_euler / euler_tau; func must be
+    the Euler residual (evalResidual or physicsRhs).  precision 1 runs the
+    Jacobian, preconditioner and Krylov solve in FP32.  Raises EulerGPUError
+    (EG_ERR_NOT_CONVERGED) when the tolerances are not met."""
+    _euler_rhs_only(func)
+    return eqn.gpu.newton(eqn.q, opts, precision=precision)
+
+
+def rk4(func, h, t_max, mesh, sbp, eqn, opts, res_tol=-1.0, real_time=False, itermax=0):
+    """rk4 (reference src/NonlinearSolvers/rk4.jl:404): eqn.q advanced in
+    place by round(t_max / h) classical RK4 steps (fewer when itermax > 0 or
+    the stage-1 norm drops below res_tol > 0); func must be the Euler
+    residual.  real_time is accepted for the signature (the residual is
+    time-independent)."""
+    _euler_rhs_only(func)
+    return eqn.gpu.rk4(eqn.q, h, t_max, itermax=itermax, res_tol=res_tol)
+
+
 class LinearOperator:
     """Explicit Jacobian (reference AbstractLO: calcLinearOperator /
     applyLinearOperator), element-block sparse on the device."""
