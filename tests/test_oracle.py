@@ -347,3 +347,32 @@ def test_oracle_newton_converges_small(oracle):
     st = eulergpu.NewtonStats()
     rc = oracle.oracle_newton(C.byref(desc.desc), C.byref(P), abi.dptr(q), C.byref(o), C.byref(st))
     assert rc == 0 and st.converged == 1 and st.res_norm < 1e-10
+
+
+@pytest.mark.parametrize("fam,p,slope", [("omega", 2, 3.0), ("omega", 1, 2.0)])
+def test_vortex_convergence_slope(oracle, fam, p, slope):
+    """Steady isentropic vortex on the quarter annulus (exact Dirichlet data),
+    Newton to |R| < 1e-12 on 4x4, 8x8 and 16x16 meshes: the SBP-norm error
+    against the exact vortex falls at p+1 (the reference's p=2 DG vortex
+    convergence test expects slope 3.00 +- 0.1, test/euler/convergence)."""
+    from pdesolver_gb300 import mesh, sbp
+    opts = {"gamma": 1.4, "Ma": 0.5, "aoa": 0.0, "vortex_M_in": 0.5, "Flux_name": "RoeFlux",
+            "volume_integral_type": 1}
+    P = eulergpu_params(opts)
+    newton_opts = {"res_abstol": 1e-12, "res_reltol": 1e-15, "itermax": 60, "krylov_reltol": 1e-6,
+                   "newton_globalize_euler": False}
+    from pdesolver_gb300 import eulergpu
+    errs = []
+    for n in (4, 8, 16):
+        ms = mesh.annulus(sbp.get_operator(2, fam, p), n, n, bc=mesh.BC_VORTEX)
+        qex = problems.vortex_state(ms.coords, M_in=0.5)
+        q = np.ascontiguousarray(qex.copy())
+        desc = abi.MeshDesc(ms)
+        o = eulergpu.NewtonOpts.from_opts(newton_opts, 0)
+        st = eulergpu.NewtonStats()
+        assert oracle.oracle_newton(C.byref(desc.desc), C.byref(P), abi.dptr(q), C.byref(o),
+                                    C.byref(st)) == 0
+        M = ms.M[:, :, None]
+        errs.append(math.sqrt((M * (q - qex) ** 2).sum() / ms.M.sum()))
+    slopes = [math.log2(errs[k] / errs[k + 1]) for k in range(2)]
+    assert all(abs(s - slope) < 0.1 for s in slopes), slopes
