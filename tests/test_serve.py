@@ -9,6 +9,7 @@ import threading
 import time
 
 import numpy as np
+import pytest
 
 from pdesolver_gb300 import eulergpu, problems, serve
 
@@ -177,3 +178,27 @@ def test_serving_stream_specs():
     assert all(8 <= s["n"] <= 96 and 1 <= s["p"] <= 4 for s in d2)
     assert all(0.3 <= s["M_in"] <= 0.7 and s["gap"] >= 0 for s in specs)
     assert problems.config5_specs(count=400, seed=6) == specs
+
+
+def test_estimate_mem_face_diagonal_coupling(gpu_lib):
+    """diagonal-E tets keep one nv x nv coupling block per stencil node: the
+    estimate's Jacobian part drops by the dense blocks' share."""
+    ms = problems.request_meshes((3, 4, 2))[-1]
+    q = eulergpu.mem_query(ms, precision=1)
+    assert q.face_diagonal == 1
+    e_diag = eulergpu.estimate_mem(ms, precision=1)
+    q.face_diagonal = 0
+    e_dense = abi_estimate(q)
+    nv, S, I = ms.numDofPerNode, ms.sbp.stencilsize, ms.numInterfaces
+    dense_cpl = 4 * I * 2 * (S * nv) ** 2
+    diag_cpl = 4 * I * 2 * S * nv * nv
+    assert e_dense.jacobian - e_diag.jacobian == pytest.approx(dense_cpl - diag_cpl, abs=1024)
+    assert eulergpu.mem_query(problems.request_meshes((2, 8, 3))[-1], 1).face_diagonal == 0
+
+
+def abi_estimate(q):
+    import ctypes as C
+    from pdesolver_gb300 import abi
+    out = abi.EgMemEstimate()
+    eulergpu.check(eulergpu.library().eg_estimate_mem(C.byref(q), C.byref(out)))
+    return out
