@@ -994,6 +994,13 @@ def run_c5(args, rank, world):
             cpu_t += ms.numEl * (st["iters"] * (rr[0] + rr[1] + rr[2]) + rr[0] + st["krylov_iters"] * rr[3])
     h2d = sum(r.q0.nbytes for r in _c5_requests(specs, meshes, rate))
     d2h = sum(r.q.nbytes for r in results["mixed"] if r.q is not None)
+    # the mixed stream's persistent GMRES solves (gmres_bytes per level) over its span
+    abytes = 0
+    for sp, r in zip(specs, results["mixed"]):
+        for ms, st in zip(meshes[problems.geometry_key(sp)], r.stats):
+            abytes += gmres_bytes(ms, st["krylov_iters"], 30, 4)
+    peaks, src = measured_peaks()
+    n_launch = sum(r.launches for r in results["mixed"])
     line = {
         "metric": "served steady solves/s (p50/p99 latency)", "value": mixed["solves_per_s"] * world,
         "unit": "solves/s", "n_gpus": world, "steps": 1, "warmup": 1,
@@ -1020,6 +1027,13 @@ def run_c5(args, rank, world):
                                    "and this run's Newton/GMRES counts, no queueing"},
         "e2e": {"value": mixed["solves_per_s"] * world, "unit": "solves/s",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "roofline": {"bound": "hbm", "achieved": abytes / mixed["span_s"] / 1e9,
+                     "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": abytes / mixed["span_s"] / 1e9 / peaks["hbm_gbs"], "peak_source": src,
+                     "traffic": None,
+                     "kernel": "sum of the mixed stream's persistent GMRES solves (gmres_bytes) over "
+                               "the stream span; arrivals, not the GPU, set the pace at 0.8x capacity"},
+        "gpu_launches": int(n_launch),
         "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)

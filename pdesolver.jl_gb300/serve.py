@@ -70,6 +70,7 @@ class RequestResult:
     done: float = 0.0
     footprint: int = 0
     retries: int = 0
+    launches: int = 0                # library kernel launches of the request
     error: str | None = None
 
     @property
@@ -192,13 +193,20 @@ class SteadySolveServer:
             g.close()
 
     def _gpu_run_request(self, req, meshes, stream, res):
-        import torch
-
-        from .batch import SteadyProblem, solve_one
         for g, (_, opts) in zip(meshes, req.levels):
             g.set_stream(stream.cuda_stream)
             if g.opts != opts:
                 g.set_params(opts)
+        l0 = sum(g.timings().launches for g in meshes)
+        try:
+            self._gpu_solve(req, meshes, stream, res)
+        finally:
+            res.launches = sum(g.timings().launches for g in meshes) - l0
+
+    def _gpu_solve(self, req, meshes, stream, res):
+        import torch
+
+        from .batch import SteadyProblem, solve_one
         with torch.cuda.stream(stream):
             q0 = torch.from_numpy(np.ascontiguousarray(req.q0)).to("cuda", non_blocking=False)
             pr = SteadyProblem(levels=meshes, q0=q0, opts=req.opts, level_tol=req.level_tol,
