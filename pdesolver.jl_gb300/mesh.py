@@ -25,7 +25,7 @@ import dataclasses
 
 import numpy as np
 
-from .sbp import SBPOperator, TET_FACES, TRI_FACES, TET_VERTS, TRI_VERTS
+from .sbp import SBPOperator, TET_FACES, TRI_FACES
 
 BC_VORTEX = 0      # isentropicVortexBC (src/solver/euler/bc.jl:542-568)
 BC_FREESTREAM = 1  # FreeStreamBC (src/solver/euler/bc.jl:1562-1647)
