@@ -12,13 +12,21 @@ Jacobian / preconditioner / Krylov); the plain-FP64 solve rate is reported
 beside it.  A second section measures FP64 residual evaluations/s.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload c1|c2|c3|c4|c5|tune|gmres-grid] [--only KERNELS]
+
+Other workloads: c1 (512-triangle vortex, RK4 at CFL 0.4, residual evals/s),
+c3 (82,944-tet entropy-stable RK4), c4 (batch of 96 uneven steady solves),
+c5 (served Poisson stream of steady solves, mixed against FP64), tune (the
+element-kernel autotuner sweep), gmres-grid (persistent GMRES grid sizes);
+--only runs isolated kernels for profiler captures.
 
 --impl reference times the CPU restatement of the reference algorithm (the
 oracle port; Julia, SummationByParts.jl, PUMI and PETSc are not available)
 on the host cores with all threads.
 
-Multi-GPU: independent problems have no exchange step, so N ranks solve N
-independent replicas (weak scaling, no collective on the data path).
+Multi-GPU: independent problems have no exchange step: N ranks solve N
+replicas of one mesh (c2, c3) or shards of the batch (c4), with no collective
+on the data path.
 """
 from __future__ import annotations
 
