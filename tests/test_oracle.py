@@ -255,6 +255,70 @@ def test_split_form_conservation(oracle):
     np.testing.assert_allclose(tot, -bflux, rtol=1e-11, atol=1e-13)
 
 
+def _weak_volume(oracle, ms, q):
+    """sum_k Q_k^T F_k per element, F_k the Euler flux along the scaled
+    metric column dxidx[:, k] at each node (euler.jl:628-690)."""
+    op = ms.sbp
+    out = np.zeros_like(q)
+    for e in range(q.shape[0]):
+        for k in range(ms.dim):
+            F = np.array([euler(oracle, q[e, j], ms.dxidx[e, j, :, k]) for j in range(op.numnodes)])
+            out[e] += op.Q[k].T @ F
+    return out
+
+
+def _split_volume_linear(oracle, ms, q):
+    """the straight-element split form (calcVolumeIntegralsSplitFormLinear,
+    euler_funcs.jl:240-293), restated independently of the oracle's
+    curvilinear S_x: res_i -= 2 sum_j sum_k S_k[i, j] F_IR(q_i, q_j; a_k),
+    S_k = (Q_k - Q_k^T)/2 the skew part, a_k = dxidx[:, k] of the element
+    (constant on a straight element)."""
+    op = ms.sbp
+    S = 0.5 * (op.Q - np.swapaxes(op.Q, 1, 2))
+    out = np.zeros_like(q)
+    for e in range(q.shape[0]):
+        a = ms.dxidx[e, 0]
+        for i in range(op.numnodes):
+            for j in range(op.numnodes):
+                if i == j:
+                    continue
+                for k in range(ms.dim):
+                    out[e, i] -= 2 * S[k, i, j] * ir(oracle, q[e, i], q[e, j], a[:, k])
+    return out
+
+
+@pytest.mark.parametrize("dim,fam,p", [(2, "omega", 2), (2, "gamma", 3), (3, "diage", 2)])
+def test_split_form_curvilinear_equals_linear_on_straight_elements(oracle, dim, fam, p):
+    """test/euler/test_flux.jl:170-200: on straight-sided elements the
+    curvilinear split form (S_x built from per-node metrics, the form the
+    oracle and the GPU evaluate) equals the linear split form at 1e-12, and
+    each element's volume term sums to zero at 1e-13 (S skew, F_IR
+    symmetric).  The oracle's volume term is isolated as
+    R_split - R_weak + (weak volume), the two residuals sharing their face
+    and boundary terms (IR at faces in both)."""
+    op = sbp.get_operator(dim, fam, p)
+    if dim == 2:
+        ms = mesh.annulus(op, 3, 3, bc=mesh.BC_FREESTREAM)
+    else:
+        ms = mesh.cube(op, 1, warp=0.0, bc=mesh.BC_FREESTREAM)
+    # straight elements: one metric per element
+    assert np.allclose(ms.dxidx, ms.dxidx[:, :1], rtol=0, atol=1e-14)
+    desc = abi.MeshDesc(ms)
+    rng = np.random.default_rng(11)
+    q = problems.free_stream(dim, ms.coords.shape[:2], Ma=0.5, aoa=0.3)
+    q *= 1 + rng.uniform(-0.05, 0.05, size=q.shape)
+    q = np.ascontiguousarray(q)
+    P_split = _p(Ma=0.5, face_flux=abi.EG_FLUX_IR, volume_integral_type=2)
+    P_weak = _p(Ma=0.5, face_flux=abi.EG_FLUX_IR, volume_integral_type=1)
+    vol = (oracle_residual(oracle, desc, P_split, q) - oracle_residual(oracle, desc, P_weak, q)
+           + _weak_volume(oracle, ms, q))
+    lin = _split_volume_linear(oracle, ms, q)
+    np.testing.assert_allclose(vol, lin, rtol=0, atol=1e-12)
+    assert np.abs(vol.sum(axis=(1, 2))).max() < 1e-13
+    # the split and weak volume terms differ (the check above is not vacuous)
+    assert np.abs(lin - _weak_volume(oracle, ms, q)).max() > 1e-4
+
+
 def test_calc_norm(oracle):
     """calcNorm (Utils.jl:427-449) with M and M^-1 weights."""
     op = sbp.get_operator(2, "omega", 2)
