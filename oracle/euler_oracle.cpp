@@ -283,6 +283,17 @@ void oracle_ir_flux(const eg_params* ep, int dim, const double* qL, const double
 
 double oracle_logavg(double a, double b) { return logavg(a, b); }
 
+// d logavg / d(aL, aR) by forward-mode dual numbers (the derivative that the
+// Jacobian assembly uses; logavg_diff, bc_solvers_diff.jl:5644-5716)
+void oracle_logavg_diff(double a, double b, double* dL_da, double* dL_db) {
+  Dual<2> x(a), y(b);
+  x.d[0] = 1.0;
+  y.d[1] = 1.0;
+  Dual<2> L = logavg(x, y);
+  *dL_da = L.d[0];
+  *dL_db = L.d[1];
+}
+
 void oracle_vortex(const eg_params* ep, const double* x, double* q) {
   Params p = make_params(ep);
   isentropic_vortex(p, x, q);

@@ -4,6 +4,7 @@ Each case restates a check from PDESolver.jl's test suite (file:line in the
 test names' docstrings) against the oracle's C++ point functions and
 residual.  CPU only.
 """
+import cmath
 import ctypes as C
 import math
 
@@ -201,6 +202,37 @@ def test_logavg(oracle):
     lo = oracle.oracle_logavg(xi * (1 - 1e-9), 1.0)
     hi = oracle.oracle_logavg(xi * (1 + 1e-9), 1.0)
     assert abs(hi - lo) < 1e-8
+
+
+def _logavg_complex(a, b):
+    """logavg (bc_solvers.jl:942-956) in complex arithmetic, for complex-step
+    derivatives: the series branch is taken on the real part, as the
+    reference's complex evaluation does."""
+    xi = a / b
+    f = (xi - 1) / (xi + 1)
+    u = f * f
+    if u.real < 1e-3:
+        F = 1 + u * (1 / 3 + u * (1 / 5 + u * (1 / 7 + u / 9)))
+    else:
+        F = cmath.log(xi) / 2 / f
+    return (a + b) / (2 * F)
+
+
+@pytest.mark.parametrize("aL,aR", [(1.0, 2.0), (1.0 + 1e-4, 1.0)])
+def test_logavg_derivative_vs_complex_step(oracle, aL, aR):
+    """test/euler/test_jac.jl:2001-2050: the derivative of logavg that the
+    Jacobian assembly uses equals the complex-step derivative at 1e-13, on
+    both branches (log form at (1, 2), series form at (1 + 1e-4, 1))."""
+    h = 1e-20
+    cs_L = _logavg_complex(complex(aL, h), complex(aR, 0)).imag / h
+    cs_R = _logavg_complex(complex(aL, 0), complex(aR, h)).imag / h
+    dL, dR = C.c_double(), C.c_double()
+    oracle.oracle_logavg_diff(C.c_double(aL), C.c_double(aR), C.byref(dL), C.byref(dR))
+    assert abs(dL.value - cs_L) < 1e-13
+    assert abs(dR.value - cs_R) < 1e-13
+    # the value of the complex restatement is the oracle's
+    assert math.isclose(_logavg_complex(complex(aL), complex(aR)).real,
+                        oracle.oracle_logavg(aL, aR), rel_tol=1e-15)
 
 
 def test_freestream_residual_roundoff(oracle):
