@@ -430,9 +430,33 @@ def rk4(func, h, t_max, mesh, sbp, eqn, opts, res_tol=-1.0, real_time=False, ite
     place by round(t_max / h) classical RK4 steps (fewer when itermax > 0 or
     the stage-1 norm drops below res_tol > 0); func must be the Euler
     residual.  real_time is accepted for the signature (the residual is
-    time-independent)."""
+    time-independent).
+
+    With opts["use_checkpointing"] the state is saved every
+    opts["checkpoint_freq"] steps into opts["ncheckpoints"] rotating
+    checkpoints under opts.get("checkpoint_dir", cwd) (rk4.jl:165-229); with
+    opts["is_restart"] the run continues from the step of the most recent
+    complete checkpoint, whose state the caller loads first with
+    checkpoint.loadRestartState (as the reference's startup does).  The device
+    advances the state between checkpoint steps; the results equal an
+    uninterrupted run's."""
     _euler_rhs_only(func)
-    return eqn.gpu.rk4(eqn.q, h, t_max, itermax=itermax, res_tol=res_tol)
+    if not opts.get("use_checkpointing", False):
+        return eqn.gpu.rk4(eqn.q, h, t_max, itermax=itermax, res_tol=res_tol)
+    from . import checkpoint
+
+    last = [0.0]
+
+    def advance(n, itermax_local):
+        st = eqn.gpu.rk4(eqn.q, h, n * h, itermax=itermax_local, res_tol=res_tol)
+        last[0] = st.res_norm
+        return st.steps
+
+    steps, t, _ = checkpoint.rk4_checkpointed(advance, eqn.q, h, t_max, opts, itermax=itermax,
+                                              root=opts.get("checkpoint_dir"))
+    st = Rk4Stats()
+    st.steps, st.t, st.res_norm = steps, t, last[0]
+    return st
 
 
 class LinearOperator:
