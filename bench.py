@@ -259,18 +259,27 @@ def run_reference(args, rank, world):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    rates = []
+    # one step = one bounded sample (a GMRES(30) cycle per level, a few
+    # seconds) that estimates the time of one full solve; W untimed samples,
+    # then K timed ones, so that the whole run stays within a few minutes
+    n_gmres = 30
+    for _ in range(max(0, args.warmup)):
+        cpu_solve_estimate(threads, DEFAULT_COUNTS, n_gmres)
+    est_s = []
     used, parts, el = threads, {}, 0.0
-    for _ in range(max(1, min(args.steps, 2))):
-        r, used, parts, el = cpu_solve_estimate(threads, DEFAULT_COUNTS)
-        rates.append(r)
-    rate = statistics.median(rates)
-    sample = ("per level p=1,3: 1 residual + 1 Jacobian + 1 block-LU + 100 GMRES iterations of the "
-              "full problem timed (%.1f s), scaled by the Newton/GMRES iteration counts of a full "
-              "solve %s" % (el, json.dumps({str(k): list(v) for k, v in DEFAULT_COUNTS.items()})))
+    for _ in range(max(1, args.steps)):
+        r, used, parts, el = cpu_solve_estimate(threads, DEFAULT_COUNTS, n_gmres)
+        est_s.append(1.0 / r)
+    # K estimated solves over their summed estimated time
+    rate = len(est_s) / sum(est_s)
+    sample = ("per level p=1,3: 1 residual + 1 Jacobian + 1 block-LU + %d GMRES iterations of the "
+              "full problem timed (last sample %.1f s), scaled by the Newton/GMRES iteration counts "
+              "of a full solve %s" % (n_gmres, el,
+                                      json.dumps({str(k): list(v) for k, v in DEFAULT_COUNTS.items()})))
     line = {
         "metric": "steady solves/s", "value": rate, "unit": "solves/s", "impl": "reference",
-        "n_gpus": args.gpus, "steps": len(rates), "warmup": 0, "ms_per_step": 1e3 / rate,
+        "n_gpus": args.gpus, "steps": len(est_s), "warmup": max(0, args.warmup),
+        "ms_per_step": 1e3 / rate,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "config": {"workload": WORKLOAD},
         "cpu_baseline": {"value": rate, "unit": "solves/s", "cores": used, "kind": "port",
