@@ -183,18 +183,7 @@ def annulus(sbp: SBPOperator, nr: int, ntheta: int, r_in=1.0, r_out=3.0,
     elements).  Boundary tags: 0 r = r_in, 1 r = r_out, 2 theta = 0,
     3 theta = pi/2."""
     assert sbp.dim == 2
-    r = np.linspace(r_in, r_out, nr + 1)
-    th = np.linspace(0.0, np.pi / 2, ntheta + 1)
-    R, T = np.meshgrid(r, th, indexing="ij")
-    vx = np.stack([(R * np.cos(T)).ravel(), (R * np.sin(T)).ravel()], axis=1)
-    vid = lambda i, j: i * (ntheta + 1) + j  # noqa: E731
-    els = []
-    for i in range(nr):
-        for j in range(ntheta):
-            a, b, c, d = vid(i, j), vid(i + 1, j), vid(i + 1, j + 1), vid(i, j + 1)
-            els.append((a, b, c))
-            els.append((a, c, d))
-    elverts = np.array(els, dtype=np.int64)
+    vx, elverts, _ = annulus_grid(nr, ntheta, r_in, r_out)
     X = vx[elverts]                                  # [E, 3, 2]
     # affine map from the reference triangle: x = X0 + (X1-X0)(xi+1)/2 + (X2-X0)(eta+1)/2
     J = np.stack([(X[:, 1] - X[:, 0]) / 2, (X[:, 2] - X[:, 0]) / 2], axis=2)  # [E, p, k]
@@ -289,24 +278,7 @@ def cube(sbp: SBPOperator, n: int, warp=0.05, seed=3, bc=BC_FREESTREAM) -> Mesh:
     z=0, z=1 of the unwarped cube."""
     assert sbp.dim == 3
     phi = float(np.random.default_rng(seed).uniform(0.0, 2 * np.pi)) if warp else 0.0
-    g = np.linspace(0.0, 1.0, n + 1)
-    Xg, Yg, Zg = np.meshgrid(g, g, g, indexing="ij")
-    vx = np.stack([Xg.ravel(), Yg.ravel(), Zg.ravel()], axis=1)
-    vid = lambda i, j, k: (i * (n + 1) + j) * (n + 1) + k  # noqa: E731
-    # Kuhn split: the 6 monotone paths from corner 000 to 111
-    paths = [(0, 1, 2), (0, 2, 1), (1, 0, 2), (1, 2, 0), (2, 0, 1), (2, 1, 0)]
-    els = []
-    for i in range(n):
-        for j in range(n):
-            for k in range(n):
-                for pth in paths:
-                    c = [i, j, k]
-                    vs = [vid(*c)]
-                    for ax in pth:
-                        c[ax] += 1
-                        vs.append(vid(*c))
-                    els.append(vs)
-    elverts = np.array(els, dtype=np.int64)
+    vx, elverts, _ = cube_grid(n)
     X = vx[elverts]
     # orient positively
     J0 = np.stack([X[:, 1] - X[:, 0], X[:, 2] - X[:, 0], X[:, 3] - X[:, 0]], axis=2)
@@ -365,6 +337,153 @@ def cube(sbp: SBPOperator, n: int, warp=0.05, seed=3, bc=BC_FREESTREAM) -> Mesh:
     return Mesh(3, sbp, coords, dxidx, jac, iface, nbrperm, nrm_f, crd_f, bfaces, offs,
                 bct, crd_b, nrm_b, tags, name=f"cube{n}",
                 min_el_size=_min_node_spacing(coords))
+
+
+# ---------------------------------------------------------------- any simplex mesh
+
+def _bc_lookup(bc_of_tag, bc):
+    if bc_of_tag is None:
+        return lambda t: bc
+    if callable(bc_of_tag):
+        return bc_of_tag
+
+    def look(t):
+        if t not in bc_of_tag:
+            raise ValueError(f"mesh: no boundary condition for boundary tag {t}")
+        return bc_of_tag[t]
+    return look
+
+
+def from_elements(sbp: SBPOperator, vertices, elements, boundary_tags, bc_of_tag=None,
+                  bc=BC_FREESTREAM, default_tag=None, name="mesh") -> Mesh:
+    """Mesh of straight-sided simplices from a neutral description: vertex
+    coordinates [nv, d] (a third column of zeros is accepted in 2-D),
+    elements [E, d+1] (0-based vertex ids, either orientation; negatively
+    oriented ones are reordered), and the tag of every boundary face as a
+    mapping {sorted tuple of its vertex ids: tag}.  Boundary faces missing
+    from the mapping get `default_tag`, or raise when it is None.  Each tag
+    is one boundary-condition group (the reference's BC1..BCn over
+    geometric edges); its condition is bc_of_tag[tag] (a mapping or a
+    callable), or `bc` for every tag.  This is the role PUMI's mesh reader
+    plays for the reference (PumiInterface.jl, not vendored); the node
+    placement, metrics and face matching are those of the structured
+    generators, so a structured mesh described this way gives the same
+    arrays."""
+    d = sbp.dim
+    vx = np.asarray(vertices, dtype=np.float64)
+    if vx.ndim != 2 or vx.shape[1] < d:
+        raise ValueError(f"mesh: vertices must be [nv, {d}]")
+    if vx.shape[1] > d:
+        if np.abs(vx[:, d:]).max(initial=0.0) > 0.0:
+            raise ValueError(f"mesh: vertices of a {d}-D mesh have non-zero extra coordinates")
+        vx = vx[:, :d]
+    vx = np.ascontiguousarray(vx)
+    elverts = np.array(elements, dtype=np.int64)
+    if elverts.ndim != 2 or elverts.shape[1] != d + 1 or len(elverts) == 0:
+        raise ValueError(f"mesh: elements must be a non-empty [E, {d + 1}] array")
+    if elverts.min() < 0 or elverts.max() >= len(vx):
+        raise ValueError("mesh: element vertex id out of range")
+    X = vx[elverts]
+    J0 = np.stack([X[:, k + 1] - X[:, 0] for k in range(d)], axis=2)
+    neg = np.linalg.det(J0) < 0
+    elverts[neg, d - 1], elverts[neg, d] = elverts[neg, d].copy(), elverts[neg, d - 1].copy()
+    X = vx[elverts]                                  # [E, d+1, d]
+    # affine map from the reference simplex: x = X0 + sum_k (X_{k+1} - X0)(xi_k + 1)/2
+    J = np.stack([(X[:, k + 1] - X[:, 0]) / 2 for k in range(d)], axis=2)   # [E, p, k]
+    dx, jac_e = _metrics_from_jacobian(J)
+    Np, Nf = sbp.numnodes, sbp.numfacenodes
+    bary = _bary_tri if d == 2 else _bary_tet
+    faces_local = TRI_FACES if d == 2 else TET_FACES
+    F = len(faces_local)
+    coords = np.einsum("nv,evp->enp", bary(sbp.nodes), X)
+    dxidx = np.repeat(dx[:, None], Np, axis=1)
+    jac = np.repeat(jac_e[:, None], Np, axis=1)
+    fpts = np.stack([np.einsum("nv,evp->enp", bary(sbp.face_xi[f]), X) for f in range(F)], 1)
+    tagmap = {tuple(sorted(int(v) for v in k)): int(t) for k, t in dict(boundary_tags).items()}
+    fl = np.array(faces_local)
+
+    def tags_of(be, bf):
+        keys = np.sort(elverts[be[:, None], fl[bf]], axis=1)
+        out = np.empty(len(be), dtype=np.int32)
+        missing = 0
+        for n, k in enumerate(map(tuple, keys.tolist())):
+            t = tagmap.get(k, default_tag)
+            if t is None:
+                missing += 1
+                t = -1
+            out[n] = t
+        if missing:
+            raise ValueError(f"mesh: {missing} boundary faces have no tag (and no default_tag)")
+        return out
+
+    iface, nbrperm, bfaces, offs, bct, tags = _connect(elverts, faces_local, sbp, fpts, tags_of,
+                                                       _bc_lookup(bc_of_tag, bc))
+    dxf = np.repeat(np.repeat(dx[:, None, None], F, axis=1), Nf, axis=2)   # [E, F, Nf, d, d]
+    nrm_f = _face_normals(sbp, dxf, iface[:, [0, 2]])
+    crd_f = fpts[iface[:, 0], iface[:, 2]]
+    nrm_b = _face_normals(sbp, dxf, bfaces)
+    crd_b = fpts[bfaces[:, 0], bfaces[:, 1]]
+    return Mesh(d, sbp, coords, dxidx, jac, iface, nbrperm, nrm_f, crd_f, bfaces, offs,
+                bct, crd_b, nrm_b, tags, name=name, min_el_size=_min_node_spacing(coords))
+
+
+def annulus_grid(nr, ntheta, r_in=1.0, r_out=3.0):
+    """the vertices [nv, 2] and triangles [E, 3] of ``annulus`` and the tag
+    of each boundary edge ({sorted vertex pair: tag}, tags as in annulus),
+    as a neutral description for ``from_elements``."""
+    r = np.linspace(r_in, r_out, nr + 1)
+    th = np.linspace(0.0, np.pi / 2, ntheta + 1)
+    R, T = np.meshgrid(r, th, indexing="ij")
+    vx = np.stack([(R * np.cos(T)).ravel(), (R * np.sin(T)).ravel()], axis=1)
+    vid = lambda i, j: i * (ntheta + 1) + j  # noqa: E731
+    els = []
+    for i in range(nr):
+        for j in range(ntheta):
+            a, b, c, dd = vid(i, j), vid(i + 1, j), vid(i + 1, j + 1), vid(i, j + 1)
+            els.append((a, b, c))
+            els.append((a, c, dd))
+    tags = {}
+    for j in range(ntheta):
+        tags[tuple(sorted((vid(0, j), vid(0, j + 1))))] = 0
+        tags[tuple(sorted((vid(nr, j), vid(nr, j + 1))))] = 1
+    for i in range(nr):
+        tags[tuple(sorted((vid(i, 0), vid(i + 1, 0))))] = 2
+        tags[tuple(sorted((vid(i, ntheta), vid(i + 1, ntheta))))] = 3
+    return vx, np.array(els, dtype=np.int64), tags
+
+
+def cube_grid(n):
+    """the vertices [nv, 3] and tetrahedra [6 n^3, 4] of ``cube`` before its
+    warp (the Kuhn split of each hex: the 6 monotone vertex paths from its
+    corner 000 to 111; orientation as generated) and the tag of every
+    boundary triangle ({sorted vertex triple: tag}, tags as in cube)."""
+    g = np.linspace(0.0, 1.0, n + 1)
+    Xg, Yg, Zg = np.meshgrid(g, g, g, indexing="ij")
+    vx = np.stack([Xg.ravel(), Yg.ravel(), Zg.ravel()], axis=1)
+    vid = lambda i, j, k: (i * (n + 1) + j) * (n + 1) + k  # noqa: E731
+    paths = [(0, 1, 2), (0, 2, 1), (1, 0, 2), (1, 2, 0), (2, 0, 1), (2, 1, 0)]
+    els = []
+    for i in range(n):
+        for j in range(n):
+            for k in range(n):
+                for pth in paths:
+                    c = [i, j, k]
+                    vs = [vid(*c)]
+                    for ax in pth:
+                        c[ax] += 1
+                        vs.append(vid(*c))
+                    els.append(vs)
+    elverts = np.array(els, dtype=np.int64)
+    tags = {}
+    for tet in elverts:
+        for fv in TET_FACES:
+            tri = tet[list(fv)]
+            P = vx[tri]
+            for ax in range(3):
+                for side in (0, 1):
+                    if np.all(P[:, ax] == float(side)):
+                        tags[tuple(sorted(int(v) for v in tri))] = 2 * ax + side
+    return vx, elverts, tags
 
 
 # ---------------------------------------------------------------- on-disk form

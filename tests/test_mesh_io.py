@@ -1,0 +1,116 @@
+"""Neutral mesh input (the role of PUMI's reader for the reference): any
+straight-sided simplex mesh from vertices, elements and boundary tags
+(mesh.from_elements), and Gmsh MSH 2.2 ASCII files (mesh_io).  CPU only."""
+import numpy as np
+import pytest
+
+from conftest import oracle_residual
+from pdesolver_gb300 import abi, mesh, mesh_io, problems, sbp
+
+
+def _same(a, b, atol=0.0):
+    for k in mesh._MESH_ARRAYS:
+        x, y = getattr(a, k), getattr(b, k)
+        assert x.shape == y.shape, k
+        if x.dtype.kind in "iu" or atol == 0.0:
+            assert np.array_equal(x, y), k
+        else:
+            np.testing.assert_allclose(x, y, rtol=1e-13, atol=atol, err_msg=k)
+
+
+@pytest.mark.parametrize("fam,p", [("omega", 2), ("gamma", 3)])
+def test_gmsh_annulus_round_trip_is_bit_exact(tmp_path, fam, p):
+    op = sbp.get_operator(2, fam, p)
+    ref = mesh.annulus(op, 4, 6)
+    vx, el, tags = mesh.annulus_grid(4, 6)
+    path = tmp_path / "annulus.msh"
+    mesh_io.write_gmsh(path, vx, el, tags)
+    got = mesh_io.read_gmsh(path, op, bc=mesh.BC_VORTEX)
+    _same(got, ref)
+    assert got.min_el_size == ref.min_el_size
+
+
+@pytest.mark.parametrize("p", [1, 2])
+def test_gmsh_cube_round_trip(tmp_path, p):
+    op = sbp.get_operator(3, "diage", p)
+    ref = mesh.cube(op, 2, warp=0.0)
+    vx, el, tags = mesh.cube_grid(2)
+    path = tmp_path / "cube.msh"
+    mesh_io.write_gmsh(path, vx, el, tags)
+    got = mesh_io.read_gmsh(path, op)
+    # the generator maps through quadratic geometry nodes, the reader affinely
+    _same(got, ref, atol=1e-12)
+    assert got.min_el_size == pytest.approx(ref.min_el_size, rel=1e-14)
+
+
+def test_boundary_conditions_by_physical_name(tmp_path, oracle):
+    """physical names select the condition of each boundary group; the
+    oracle residual on the file's mesh equals the one on the generated mesh."""
+    op = sbp.get_operator(2, "omega", 2)
+    vx, el, tags = mesh.annulus_grid(3, 3)
+    path = tmp_path / "named.msh"
+    mesh_io.write_gmsh(path, vx, el, tags, names={0: "inner", 1: "outer", 2: "bottom", 3: "left"})
+    got = mesh_io.read_gmsh(path, op, bc_of_tag={"inner": mesh.BC_VORTEX, "outer": mesh.BC_VORTEX,
+                                                 "bottom": mesh.BC_FREESTREAM, 3: mesh.BC_FREESTREAM})
+    assert got.bc_types.tolist() == [mesh.BC_VORTEX, mesh.BC_VORTEX, mesh.BC_FREESTREAM,
+                                     mesh.BC_FREESTREAM]
+    ref = mesh.annulus(op, 3, 3)
+    ref.bc_types = got.bc_types.copy()
+    P = abi.EgParams.make(Ma=0.5, M_in=0.5)
+    q = np.ascontiguousarray(problems.vortex_state(ref.coords, M_in=0.5) * 1.001)
+    r1 = oracle_residual(oracle, abi.MeshDesc(got), P, q)
+    r2 = oracle_residual(oracle, abi.MeshDesc(ref), P, q)
+    assert np.array_equal(r1, r2)
+    with pytest.raises(ValueError):
+        mesh_io.read_gmsh(path, op, bc_of_tag={"inner": mesh.BC_VORTEX})
+
+
+def test_element_orientation_is_normalised(oracle):
+    """elements given clockwise are reordered; with a symmetric operator the
+    residual is the same at every node (nodes permuted within elements)."""
+    op = sbp.get_operator(2, "gamma", 2)
+    vx, el, tags = mesh.annulus_grid(3, 4)
+    flipped = el[:, [0, 2, 1]]
+    a = mesh.from_elements(op, vx, el, tags, bc=mesh.BC_VORTEX)
+    b = mesh.from_elements(op, vx, flipped, tags, bc=mesh.BC_VORTEX)
+    assert (b.jac > 0).all()
+    P = abi.EgParams.make(Ma=0.5, M_in=0.5)
+    ra, rb = [], []
+    for ms, out in ((a, ra), (b, rb)):
+        q = problems.vortex_state(ms.coords, M_in=0.5)
+        q = np.ascontiguousarray(q * (1 + 1e-3 * np.sin(7 * ms.coords[..., :1])))
+        out.append(oracle_residual(oracle, abi.MeshDesc(ms), P, q))
+    for e in range(a.numEl):
+        ia = np.lexsort(a.coords[e].T)
+        ib = np.lexsort(b.coords[e].T)
+        np.testing.assert_allclose(a.coords[e, ia], b.coords[e, ib], atol=1e-14)
+        np.testing.assert_allclose(ra[0][e, ia], rb[0][e, ib], atol=1e-12)
+
+
+def test_reader_refusals(tmp_path):
+    op = sbp.get_operator(2, "omega", 1)
+    vx, el, tags = mesh.annulus_grid(2, 2)
+    some = dict(list(tags.items())[:-1])               # one boundary edge untagged
+    with pytest.raises(ValueError):
+        mesh.from_elements(op, vx, el, some)
+    m = mesh.from_elements(op, vx, el, some, default_tag=7)
+    assert 7 in m.bndry_tag.tolist()
+    with pytest.raises(ValueError):
+        mesh.from_elements(op, vx, el[:, :2], tags)    # not triangles
+    with pytest.raises(ValueError):
+        mesh.from_elements(op, vx, el + len(vx), tags)  # vertex ids out of range
+    with pytest.raises(ValueError):
+        mesh.from_elements(op, np.c_[vx, np.ones(len(vx))], el, tags)   # not planar
+    p4 = tmp_path / "v4.msh"
+    p4.write_text("$MeshFormat\n4.1 0 8\n$EndMeshFormat\n")
+    with pytest.raises(ValueError, match="2.x ASCII"):
+        mesh_io.read_gmsh(p4, op)
+    p9 = tmp_path / "curved.msh"
+    p9.write_text("$MeshFormat\n2.2 0 8\n$EndMeshFormat\n$Nodes\n1\n1 0 0 0\n$EndNodes\n"
+                  "$Elements\n1\n1 9 2 0 1 1 1 1 1 1 1\n$EndElements\n")
+    with pytest.raises(ValueError, match="not supported"):
+        mesh_io.read_gmsh(p9, op)
+    p3 = tmp_path / "only_lines.msh"
+    mesh_io.write_gmsh(p3, vx, el, tags)
+    with pytest.raises(ValueError, match="3-D"):
+        mesh_io.read_gmsh(p3, sbp.get_operator(3, "diage", 1))
