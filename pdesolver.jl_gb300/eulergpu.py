@@ -582,9 +582,20 @@ class LinearSolver:
         h = C.c_void_p()
         check(self.lib.eg_ls_create(lo.handle, pc.handle, restart, C.byref(h)))
         self.handle = h
+        self.restart = restart
+        self.reltol, self.abstol, self.itermax = -1.0, -1.0, -1
 
     def set_tolerances(self, reltol=-1.0, abstol=-1.0, dtol=-1.0, itermax=-1):
+        """setTolerances (reference ls_standard.jl): negative values keep the
+        current setting.  The values are also kept here for the transposed
+        solve (adjoint.linearSolveTranspose)."""
         check(self.lib.eg_ls_set_tolerances(self.handle, reltol, abstol, dtol, itermax))
+        if reltol >= 0:
+            self.reltol = reltol
+        if abstol >= 0:
+            self.abstol = abstol
+        if itermax > 0:
+            self.itermax = itermax
 
     def set_grid(self, blocks=0):
         """blocks of the persistent GMRES kernel (0: automatic)."""
