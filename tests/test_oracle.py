@@ -431,6 +431,48 @@ def test_oracle_rk4_fourth_order(oracle):
     assert 12.0 < e1 / e2 < 20.0, (e1, e2)
 
 
+def test_oracle_rk4_step_is_the_degree4_taylor_polynomial(oracle):
+    """test/euler/test_rk4.jl:23-50 checks that rk4 is exact for a quartic
+    (the classical RK4 tableau).  The Euler RK4 here is autonomous, so the
+    same property is pinned on the linearisation: around a free stream
+    (R(q0) = 0) one step of a perturbation eps v is q0 + eps P4(hA) v,
+    A = M^-1 dR/dq, P4(z) = 1 + z + z^2/2 + z^3/6 + z^4/24, to O(eps); with
+    h |A| ~ 0.4 a degree-3 polynomial misses by ~1e-3 relative.  The step
+    reports t = h."""
+    from conftest import block_apply, oracle_jacobian
+    from pdesolver_gb300 import eulergpu
+    op = sbp.get_operator(2, "omega", 1)
+    ms = mesh.annulus(op, 2, 2, bc=mesh.BC_FREESTREAM)
+    desc = abi.MeshDesc(ms)
+    opts = {"Ma": 0.5, "aoa": 0.0}
+    P = eulergpu.params_from_opts(opts)
+    q0 = np.ascontiguousarray(problems.free_stream(2, ms.coords.shape[:2], Ma=0.5))
+    assert np.abs(oracle_residual(oracle, desc, P, q0)).max() < 1e-13
+    diag, cpl = oracle_jacobian(oracle, desc, P, ms, q0)
+    N = q0.size
+    Jd = np.stack([block_apply(ms, diag, cpl, np.eye(N)[i].reshape(q0.shape)).reshape(-1)
+                   for i in range(N)], axis=1)
+    minv = np.repeat(1.0 / ms.M, ms.numDofPerNode).reshape(-1)
+    A = minv[:, None] * Jd
+    h = 0.4 / np.abs(np.linalg.eigvals(A)).max()
+    v = np.random.default_rng(5).normal(size=N)
+    eps = 1e-7
+    q = np.ascontiguousarray((q0.reshape(-1) + eps * v).reshape(q0.shape))
+    st = eulergpu.Rk4Stats()
+    assert oracle.oracle_rk4(C.byref(desc.desc), C.byref(P), abi.dptr(q), C.c_double(h),
+                             C.c_double(h), 0, C.c_double(-1.0), C.byref(st)) == 0
+    assert st.steps == 1 and st.t == pytest.approx(h, rel=1e-14)
+    got = (q.reshape(-1) - q0.reshape(-1)) / eps
+    terms, t = [], v.copy()
+    for k in range(5):
+        terms.append(t)
+        t = h * (A @ t) / (k + 1)
+    p4, p3 = sum(terms), sum(terms[:4])
+    scale = np.abs(p4).max()
+    assert np.abs(got - p4).max() < 1e-5 * scale
+    assert np.abs(p4 - p3).max() > 1e-4 * scale
+
+
 def test_oracle_newton_converges_small(oracle):
     """newton.jl with pseudo-transient continuation reaches |R| < 1e-10 from the
     perturbed free stream on a small annulus (Gamma p=2)."""
