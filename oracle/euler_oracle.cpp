@@ -14,6 +14,7 @@
 // interiorfaceintegrate!, boundaryinterpolate!, boundaryintegrate!) belong to
 // SummationByParts.jl, which is not vendored; they are restated from their
 // call sites with the operator fields interp / perm / nbrperm / wface.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -500,11 +501,18 @@ void jac_apply(const eg_mesh_desc* d, int n, int nb, const double* diag, const d
     }
   }
   (void)Np;
-  for (int nI = 0; nI < d->num_interfaces; ++nI) {
+  // the coupling terms of every interface, computed in parallel, then added
+  // to y in interface order (the sums of a serial loop, bit for bit)
+  const int I = d->num_interfaces;
+  std::vector<double> t((size_t)I * 2 * nb);
+#pragma omp parallel for schedule(static)
+  for (int nI = 0; nI < I; ++nI) {
     const int32_t* itf = d->interfaces + 5 * nI;
     const int eL = itf[0], eR = itf[1], fL = itf[2], fR = itf[3];
     const double* CLR = cpl + ((size_t)nI * 2 + 0) * nb * nb;
     const double* CRL = cpl + ((size_t)nI * 2 + 1) * nb * nb;
+    double* tL = &t[((size_t)nI * 2 + 0) * nb];
+    double* tR = &t[((size_t)nI * 2 + 1) * nb];
     for (int s = 0; s < S; ++s)
       for (int a = 0; a < NV; ++a) {
         double aL = 0, aR = 0;
@@ -515,8 +523,19 @@ void jac_apply(const eg_mesh_desc* d, int n, int nb, const double* diag, const d
             aR += CRL[(size_t)(sp * NV + b) * nb + s * NV + a] *
                   x[(size_t)eL * n + d->perm[fL * S + sp] * NV + b];
           }
-        y[(size_t)eL * n + d->perm[fL * S + s] * NV + a] += aL;
-        y[(size_t)eR * n + d->perm[fR * S + s] * NV + a] += aR;
+        tL[s * NV + a] = aL;
+        tR[s * NV + a] = aR;
+      }
+  }
+  for (int nI = 0; nI < I; ++nI) {
+    const int32_t* itf = d->interfaces + 5 * nI;
+    const int eL = itf[0], eR = itf[1], fL = itf[2], fR = itf[3];
+    const double* tL = &t[((size_t)nI * 2 + 0) * nb];
+    const double* tR = &t[((size_t)nI * 2 + 1) * nb];
+    for (int s = 0; s < S; ++s)
+      for (int a = 0; a < NV; ++a) {
+        y[(size_t)eL * n + d->perm[fL * S + s] * NV + a] += tL[s * NV + a];
+        y[(size_t)eR * n + d->perm[fR * S + s] * NV + a] += tR[s * NV + a];
       }
   }
 }
@@ -575,9 +594,23 @@ struct BlockLU {
   }
 };
 
+// sum of a[i] b[i]: partial sums over fixed chunks of 8192 (in parallel),
+// then over the chunks in order, so the result does not depend on the
+// number of threads
 double dot(const std::vector<double>& a, const std::vector<double>& b) {
+  constexpr size_t kChunk = 8192;
+  const size_t N = a.size();
+  const long nc = (long)((N + kChunk - 1) / kChunk);
+  std::vector<double> part(nc);
+#pragma omp parallel for schedule(static)
+  for (long c = 0; c < nc; ++c) {
+    double s = 0;
+    const size_t hi = std::min(N, (size_t)(c + 1) * kChunk);
+    for (size_t i = (size_t)c * kChunk; i < hi; ++i) s += a[i] * b[i];
+    part[c] = s;
+  }
   double s = 0;
-  for (size_t i = 0; i < a.size(); ++i) s += a[i] * b[i];
+  for (long c = 0; c < nc; ++c) s += part[c];
   return s;
 }
 
@@ -596,11 +629,13 @@ int gmres(const eg_mesh_desc* d, int n, int nb, const double* diag, const double
   int its = 0;
   while (true) {
     jac_apply(d, n, nb, diag, cpl, x.data(), w.data());
-    for (size_t i = 0; i < N; ++i) w[i] = b[i] - w[i];
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < (long)N; ++i) w[i] = b[i] - w[i];
     const double beta = std::sqrt(dot(w, w));
     if (conv_out) *conv_out = !(beta > tol);
     if (!(beta > tol) || its >= itermax) break;
-    for (size_t i = 0; i < N; ++i) V[0][i] = w[i] / beta;
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < (long)N; ++i) V[0][i] = w[i] / beta;
     std::fill(g.begin(), g.end(), 0.0);
     g[0] = beta;
     int j = 0;
@@ -612,11 +647,18 @@ int gmres(const eg_mesh_desc* d, int n, int nb, const double* diag, const double
       double* Hc = &H[(size_t)j * (m + 1)];
       for (int k = 0; k <= j; ++k) {
         Hc[k] = dot(V[k], w);
-        for (size_t i = 0; i < N; ++i) w[i] -= Hc[k] * V[k][i];
+        const double hk = Hc[k];
+        const double* vk = V[k].data();
+#pragma omp parallel for schedule(static)
+        for (long i = 0; i < (long)N; ++i) w[i] -= hk * vk[i];
       }
       Hc[j + 1] = std::sqrt(dot(w, w));
-      if (Hc[j + 1] > 0)
-        for (size_t i = 0; i < N; ++i) V[j + 1][i] = w[i] / Hc[j + 1];
+      if (Hc[j + 1] > 0) {
+        const double hn = Hc[j + 1];
+        double* vn = V[j + 1].data();
+#pragma omp parallel for schedule(static)
+        for (long i = 0; i < (long)N; ++i) vn[i] = w[i] / hn;
+      }
       for (int k = 0; k < j; ++k) {
         const double t0 = cs[k] * Hc[k] + sn[k] * Hc[k + 1];
         Hc[k + 1] = -sn[k] * Hc[k] + cs[k] * Hc[k + 1];
@@ -637,11 +679,15 @@ int gmres(const eg_mesh_desc* d, int n, int nb, const double* diag, const double
       for (int c = k + 1; c < j; ++c) s -= H[(size_t)c * (m + 1) + k] * y[c];
       y[k] = s / H[(size_t)k * (m + 1) + k];
     }
-    std::fill(w.begin(), w.end(), 0.0);
-    for (int k = 0; k < j; ++k)
-      for (size_t i = 0; i < N; ++i) w[i] += y[k] * V[k][i];
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < (long)N; ++i) {
+      double acc = 0.0;
+      for (int k = 0; k < j; ++k) acc += y[k] * V[k][i];
+      w[i] = acc;
+    }
     pc.solve(d, w.data(), z.data());
-    for (size_t i = 0; i < N; ++i) x[i] += z[i];
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < (long)N; ++i) x[i] += z[i];
   }
   if (iters_out) *iters_out = its;
   return EG_OK;
