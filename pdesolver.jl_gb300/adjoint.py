@@ -188,6 +188,26 @@ def linearSolveTranspose(ls, b, x, reltol=None, abstol=None, itermax=None, devic
     return st
 
 
+def evalResidual_revq(mesh, sbp, eqn, opts, res_bar, q_bar, lo=None, zero_output=True):
+    """q_bar <- (dR/dq)^T res_bar at eqn.q, or q_bar += it with
+    zero_output=False (the reference's reverse-mode residual product,
+    interface2.jl:391-430): the explicit Jacobian at eqn.q (into `lo`, a
+    LinearOperator of the mesh, or a new FP64 one) applied transposed on the
+    device.  res_bar and q_bar are numpy arrays of the state's size.
+    Returns q_bar."""
+    if lo is None:
+        from . import eulergpu
+        lo = eulergpu.LinearOperator(eqn.gpu, precision=0)
+    lo.calc(eqn.q)
+    rb = np.ascontiguousarray(res_bar, dtype=np.float64).reshape(np.shape(eqn.q))
+    out = lo.apply_transpose(rb, np.zeros(np.shape(eqn.q))).reshape(np.shape(q_bar))
+    if zero_output:
+        q_bar[...] = out
+    else:
+        q_bar += out
+    return q_bar
+
+
 def calcAdjoint(mesh, sbp, eqn, opts, ls, functional, adjoint_vec, recalc_jac=False,
                 recalc_pc=False, device=None):
     """adjoint_vec <- psi with (dR/dq)^T psi = -dJ/dq at eqn.q

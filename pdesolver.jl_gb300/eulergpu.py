@@ -441,6 +441,7 @@ def rk4(func, h, t_max, mesh, sbp, eqn, opts, res_tol=-1.0, real_time=False, ite
     advances the state between checkpoint steps; the results equal an
     uninterrupted run's."""
     _euler_rhs_only(func)
+    opts = {} if opts is None else opts
     if not opts.get("use_checkpointing", False):
         return eqn.gpu.rk4(eqn.q, h, t_max, itermax=itermax, res_tol=res_tol)
     from . import checkpoint

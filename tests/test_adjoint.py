@@ -126,3 +126,37 @@ def test_calc_adjoint_against_dense_solve(oracle):
     np.testing.assert_allclose(psi.reshape(-1), ref, rtol=0, atol=1e-9 * np.abs(ref).max())
     v = np.random.default_rng(4).normal(size=N)
     assert psi.reshape(-1) @ (J @ v) == pytest.approx(-(dj @ v), rel=1e-9)
+
+
+def test_eval_residual_revq_with_the_oracle_blocks(oracle):
+    """evalResidual_revq: q_bar = (dR/dq)^T res_bar, overwritten or summed
+    into (zero_output), against the oracle's directional derivative:
+    res_bar . (J v) = q_bar . v."""
+    from conftest import oracle_jvp
+
+    class LO:
+        def __init__(self, ms, diag, cpl):
+            self.ms, self.diag, self.cpl = ms, diag, cpl
+
+        def calc(self, q):
+            self.q = q
+
+        def apply_transpose(self, x, y):
+            y[...] = block_apply_t(self.ms, self.diag, self.cpl, x)
+            return y
+
+    ms, opts, q = problems.config1(n=3, p=2, family="gamma", seed=10)
+    desc = abi.MeshDesc(ms)
+    P = eulergpu.params_from_opts(opts)
+    lo = LO(ms, *oracle_jacobian(oracle, desc, P, ms, q))
+    eqn = SimpleNamespace(q=q)
+    rng = np.random.default_rng(6)
+    rb, v = rng.normal(size=q.shape), rng.normal(size=q.shape)
+    qb = np.full(q.size, 7.0)
+    adjoint.evalResidual_revq(ms, ms.sbp, eqn, opts, rb.reshape(-1), qb, lo=lo)
+    assert lo.q is q
+    jv = oracle_jvp(oracle, desc, P, q, v)
+    assert (rb * jv).sum() == pytest.approx(qb @ v.reshape(-1), rel=1e-11)
+    qb2 = np.ones(q.size)
+    adjoint.evalResidual_revq(ms, ms.sbp, eqn, opts, rb.reshape(-1), qb2, lo=lo, zero_output=False)
+    np.testing.assert_allclose(qb2, qb + 1.0, rtol=0, atol=1e-14 * np.abs(qb).max())
