@@ -49,3 +49,41 @@ def test_host_arrays_are_size_checked():
         eulergpu.GPUMesh._ptr(np.zeros(12, dtype=np.float32), 12)
     ptr, mem = eulergpu.GPUMesh._ptr(np.zeros(12), 12)
     assert mem == 0 and ptr.value
+
+
+def test_ctypes_structures_match_the_header(tmp_path):
+    """every ctypes structure of the Python binding has the size and field
+    offsets of its C struct in include/eulergpu.h (compiled with the host C
+    compiler), so no argument block drifts from the ABI."""
+    import shutil
+    import subprocess
+    import pytest
+    from pdesolver_gb300 import abi, eulergpu
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    structs = {
+        "eg_params": abi.EgParams, "eg_mesh_desc": abi.EgMeshDesc, "eg_timings": eulergpu.Timings,
+        "eg_ls_stats": eulergpu.LsStats, "eg_newton_opts": eulergpu.NewtonOpts,
+        "eg_newton_stats": eulergpu.NewtonStats, "eg_rk4_stats": eulergpu.Rk4Stats,
+        "eg_mem_query": abi.EgMemQuery, "eg_mem_estimate": abi.EgMemEstimate,
+        "eg_launch_config": abi.EgLaunchConfig, "eg_tune_entry": abi.EgTuneEntry,
+    }
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "eulergpu.h"', "int main(void) {"]
+    for cname, cls in structs.items():
+        lines.append(f'  printf("{cname} %zu\\n", sizeof({cname}));')
+        for fname, _ in cls._fields_:
+            lines.append(f'  printf("{cname}.{fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "abi_probe.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "abi_probe"
+    r = subprocess.run([cc, "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout
+    got = dict(line.rsplit(" ", 1) for line in out.strip().splitlines())
+    for cname, cls in structs.items():
+        assert int(got[cname]) == C.sizeof(cls), f"sizeof({cname})"
+        for fname, _ in cls._fields_:
+            assert int(got[f"{cname}.{fname}"]) == getattr(cls, fname).offset, f"{cname}.{fname}"
