@@ -87,3 +87,34 @@ def test_ctypes_structures_match_the_header(tmp_path):
         assert int(got[cname]) == C.sizeof(cls), f"sizeof({cname})"
         for fname, _ in cls._fields_:
             assert int(got[f"{cname}.{fname}"]) == getattr(cls, fname).offset, f"{cname}.{fname}"
+
+
+def test_binding_argument_counts_match_the_prototypes():
+    """every function the Python binding declares argtypes for takes as
+    many arguments in include/eulergpu.h (a drifted prototype would pass
+    misaligned arguments through ctypes)."""
+    from pdesolver_gb300 import eulergpu
+    src = open(os.path.join(ROOT, "include", "eulergpu.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    protos = {}
+    for m in re.finditer(r"\b(eg_[a-z0-9_]+)\s*\(([^;{]*?)\)\s*;", src):
+        args = m.group(2).strip()
+        protos[m.group(1)] = 0 if args in ("", "void") else args.count(",") + 1
+
+    class Recorder:
+        def __init__(self):
+            self.fns = {}
+
+        def __getattr__(self, name):
+            fn = self.fns.setdefault(name, type("Fn", (), {})())
+            return fn
+
+    rec = Recorder()
+    eulergpu._declare(rec)
+    checked = 0
+    for name, fn in rec.fns.items():
+        if hasattr(fn, "argtypes"):
+            assert name in protos, f"{name} is not declared in eulergpu.h"
+            assert len(fn.argtypes) == protos[name], f"{name}: {len(fn.argtypes)} vs {protos[name]}"
+            checked += 1
+    assert checked >= 30
