@@ -53,6 +53,16 @@ def test_pressure_and_euler_flux(oracle):
     np.testing.assert_allclose(euler(oracle, q, [1.0, 0.0]), [2.0, 4.2, 6.0, 14.4], atol=1e-14)
 
 
+def test_pressure_and_sound_speed_3d(oracle):
+    """test/euler/test_3d.jl:216-226: q = [1, 2, 3, 4, 15] has speed of sound
+    sqrt(0.28) (1e-13), i.e. p = 0.2, and entropy log(0.4 * 0.5)."""
+    P = _p()
+    q = np.array([1.0, 2.0, 3.0, 4.0, 15.0])
+    p = oracle.oracle_pressure(C.byref(P), 3, abi.dptr(q))
+    assert abs(math.sqrt(1.4 * p / q[0]) - math.sqrt(0.28)) < 1e-13
+    assert abs(math.log(p / q[0] ** 1.4) - math.log(0.4 * 0.5)) < 1e-12
+
+
 def test_isentropic_vortex_known_answer(oracle):
     """test/euler/test_lowlevel.jl:644-649: vortex at (1,0) with the
     reference's inner Mach 0.95 is [2.000, 0.000, -1.3435, 2.236960] (1e-4)."""
