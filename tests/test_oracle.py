@@ -63,6 +63,15 @@ def test_pressure_and_sound_speed_3d(oracle):
     assert abs(math.log(p / q[0] ** 1.4) - math.log(0.4 * 0.5)) < 1e-12
 
 
+def test_euler_flux_3d_known_answers(oracle):
+    """test/euler/test_3d.jl:164-198: the 3-D Euler flux of q = [1,2,3,4,15]
+    along the coordinate directions (atol 1e-12)."""
+    q = np.array([1.0, 2.0, 3.0, 4.0, 15.0])
+    for nrm, F in (([1.0, 0, 0], [2, 4.2, 6, 8, 30.4]), ([0, 1.0, 0], [3, 6, 9.2, 12, 45.6]),
+                   ([0, 0, 1.0], [4, 8, 12, 16.2, 60.8])):
+        np.testing.assert_allclose(euler(oracle, q, np.array(nrm)), F, rtol=0, atol=1e-12)
+
+
 def test_isentropic_vortex_known_answer(oracle):
     """test/euler/test_lowlevel.jl:644-649: vortex at (1,0) with the
     reference's inner Mach 0.95 is [2.000, 0.000, -1.3435, 2.236960] (1e-4)."""
