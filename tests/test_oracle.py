@@ -267,6 +267,18 @@ def test_freestream_residual_roundoff(oracle):
         assert np.abs(res).max() < 1e-13
 
 
+@pytest.mark.parametrize("fam,p", [("omega", 2), ("gamma", 3)])
+def test_freestream_residual_roundoff_tri_split_form(oracle, fam, p):
+    """test/euler/test_flux.jl:236-250: a constant field has zero residual
+    with the Ismail-Roe split form (volume_integral_type 2, IRFlux) at 1e-12."""
+    op = sbp.get_operator(2, fam, p)
+    ms = mesh.annulus(op, 4, 4, bc=mesh.BC_FREESTREAM)
+    P = _p(Ma=0.5, aoa_deg=10.0, face_flux=abi.EG_FLUX_IR, volume_integral_type=2)
+    q = problems.free_stream(2, ms.coords.shape[:2], Ma=0.5, aoa=10.0 * math.pi / 180)
+    res = oracle_residual(oracle, abi.MeshDesc(ms), P, np.ascontiguousarray(q))
+    assert np.abs(res).max() < 1e-12
+
+
 def test_freestream_residual_roundoff_tet_split_form(oracle):
     """Free-stream preservation of the Ismail-Roe split form on warped
     (curvilinear) tetrahedra: the discrete metric identities hold."""
