@@ -291,6 +291,36 @@ def test_freestream_residual_roundoff_tet_split_form(oracle):
     assert np.abs(res).max() < 1e-12
 
 
+def test_split_form_entropy_conservation_whole_residual(oracle):
+    """test/euler/test_ESS.jl (entropy conservation of the split-form volume
+    terms with entropy-conservative interface fluxes): on warped diagonal-E
+    tetrahedra with the Ismail-Roe volume and face fluxes, the entropy
+    production of the whole residual is the boundary term alone,
+    sum_nodes w . R = sum_boundary nodes wface (psi . n - w . F_bc), psi =
+    rho u, at 1e-12 relative, for a non-uniform state."""
+    op = sbp.get_operator(3, "diage", 2)
+    ms = mesh.cube(op, 2, warp=0.05, seed=3, bc=mesh.BC_FREESTREAM)
+    P = _p(Ma=0.5, face_flux=abi.EG_FLUX_IR, volume_integral_type=2)
+    x = ms.coords
+    q = problems.free_stream(3, x.shape[:2], Ma=0.5)
+    q[..., 0] *= 1 + 0.05 * np.sin(2 * x[..., 0] + 1) * np.cos(3 * x[..., 1])
+    q[..., 1] += 0.05 * np.sin(3 * x[..., 2])
+    q[..., 4] *= 1 + 0.03 * np.cos(2 * x[..., 0] * x[..., 1])
+    q = np.ascontiguousarray(q)
+    res = oracle_residual(oracle, abi.MeshDesc(ms), P, q)
+    W = np.array([[_entropy_vars(qn) for qn in qe] for qe in q])
+    production = (W * res).sum()
+    qg = problems.free_stream(3, (1,), Ma=0.5)[0]
+    bterm = 0.0
+    for b, (e, f) in enumerate(ms.bndryfaces):
+        for i in range(op.numfacenodes):
+            qf = op.interp[f, i] @ q[e, op.perm[f]]
+            n = ms.nrm_bndry[b, i]
+            bterm += op.wface[i] * (qf[1:4] @ n - _entropy_vars(qf) @ roe(oracle, qf, qg, n))
+    assert abs(production - bterm) <= 1e-12 * abs(bterm)
+    assert abs(bterm) > 1e-3
+
+
 def test_split_form_conservation(oracle):
     """test/euler/test_flux.jl:195-200: with S skew-symmetric and F
     symmetric, 1^T (volume split-form residual) = 0 per element.  Faces are
