@@ -292,8 +292,10 @@ def test_freestream_residual_roundoff_tet_split_form(oracle):
 
 
 def test_split_form_entropy_conservation_whole_residual(oracle):
-    """test/euler/test_ESS.jl (entropy conservation of the split-form volume
-    terms with entropy-conservative interface fluxes): on warped diagonal-E
+    """test/euler/test_ESS.jl:446-572 (lemma 2: the split-form volume terms
+    contracted with w give the potential-flux boundary term; lemma 3: EC face
+    integrals) and 722-736 (W^T R = 0 for EC interface fluxes on diagonal-E
+    operators), taken together over the whole residual: on warped diagonal-E
     tetrahedra with the Ismail-Roe volume and face fluxes, the entropy
     production of the whole residual is the boundary term alone,
     sum_nodes w . R = sum_boundary nodes wface (psi . n - w . F_bc), psi =
