@@ -278,7 +278,7 @@ def cube(sbp: SBPOperator, n: int, warp=0.05, seed=3, bc=BC_FREESTREAM) -> Mesh:
     z=0, z=1 of the unwarped cube."""
     assert sbp.dim == 3
     phi = float(np.random.default_rng(seed).uniform(0.0, 2 * np.pi)) if warp else 0.0
-    vx, elverts, _ = cube_grid(n)
+    vx, elverts, _ = cube_grid(n, with_tags=False)
     X = vx[elverts]
     # orient positively
     J0 = np.stack([X[:, 1] - X[:, 0], X[:, 2] - X[:, 0], X[:, 3] - X[:, 0]], axis=2)
@@ -452,11 +452,12 @@ def annulus_grid(nr, ntheta, r_in=1.0, r_out=3.0):
     return vx, np.array(els, dtype=np.int64), tags
 
 
-def cube_grid(n):
+def cube_grid(n, with_tags=True):
     """the vertices [nv, 3] and tetrahedra [6 n^3, 4] of ``cube`` before its
     warp (the Kuhn split of each hex: the 6 monotone vertex paths from its
-    corner 000 to 111; orientation as generated) and the tag of every
-    boundary triangle ({sorted vertex triple: tag}, tags as in cube)."""
+    corner 000 to 111; orientation as generated) and, with `with_tags`, the
+    tag of every boundary triangle ({sorted vertex triple: tag}, tags as in
+    cube; else None)."""
     g = np.linspace(0.0, 1.0, n + 1)
     Xg, Yg, Zg = np.meshgrid(g, g, g, indexing="ij")
     vx = np.stack([Xg.ravel(), Yg.ravel(), Zg.ravel()], axis=1)
@@ -474,15 +475,16 @@ def cube_grid(n):
                         vs.append(vid(*c))
                     els.append(vs)
     elverts = np.array(els, dtype=np.int64)
+    if not with_tags:
+        return vx, elverts, None
+    tris = elverts[:, np.array(TET_FACES)].reshape(-1, 3)          # every local face
+    P = vx[tris]                                                     # [F, 3 vertices, 3]
     tags = {}
-    for tet in elverts:
-        for fv in TET_FACES:
-            tri = tet[list(fv)]
-            P = vx[tri]
-            for ax in range(3):
-                for side in (0, 1):
-                    if np.all(P[:, ax] == float(side)):
-                        tags[tuple(sorted(int(v) for v in tri))] = 2 * ax + side
+    for ax in range(3):
+        for side in (0, 1):
+            on = np.all(P[:, :, ax] == float(side), axis=1)
+            for tri in np.sort(tris[on], axis=1).tolist():
+                tags[tuple(tri)] = 2 * ax + side
     return vx, elverts, tags
 
 
