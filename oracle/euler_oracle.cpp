@@ -4,6 +4,13 @@
 // check libeulergpu.so.  Only tests/, __graft_entry__.smoke() and the CPU
 // baseline leg of bench.py load it.
 //
+// Pin status: the point functions, split form, entropy identities, Jacobian
+// and RK4 are pinned to the known answers and properties of the reference's
+// own tests (tests/test_oracle.py cites each one).  The SBP operator entries
+// come from SummationByParts.jl, which is absent: they are pinned by their
+// defining properties only, so entry-wise parity with that package is
+// unpinned.
+//
 // Residual: src/solver/euler/euler.jl:111-175 (evalResidual), 441-519
 // (dataPrep), 628-690 (volume + boundary integrals), 770-802 (face integrals);
 // src/solver/euler/euler_funcs.jl:23-66 (getEulerFlux), 240-362 (split form);
