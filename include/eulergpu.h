@@ -166,7 +166,8 @@ int eg_calc_max_wave_speed(eg_mesh* mesh, const double* q, int32_t mem, double* 
 
 /* Run this mesh's work on `stream` (a cudaStream_t; NULL is CUDA's default
    stream), or on the library's own stream when use_own != 0.  Lets a caller
-   order library work with its own kernels and CUDA events. */
+   order library work with its own kernels and CUDA events.  A stream of
+   another device than the mesh's is refused (EG_ERR_INVALID). */
 int eg_mesh_set_stream(eg_mesh* mesh, void* stream, int32_t use_own);
 
 /* evalResidual with device pointers, enqueued on the mesh stream without a
@@ -220,8 +221,10 @@ typedef struct eg_ls eg_ls;   /* right-preconditioned GMRES(m)             */
 int eg_lo_create(eg_mesh* mesh, int32_t precision, eg_lo** out);
 int eg_lo_destroy(eg_lo* lo);
 /* calcLinearOperator -> evalJacobian (reference evalJacobian.jl:6-72,
-   jacobian.jl:69-176): J = dR/dq at q, overwriting the blocks.
-   Weak-form volume (volume_integral_type 1), Roe or IR faces. */
+   jacobian.jl:69-176): J = dR/dq at q, overwriting the blocks.  Weak-form
+   volume (volume_integral_type 1) or the entropy-stable split form
+   (volume_integral_type 2, reference calcVolumeIntegralsSplitForm_diff,
+   euler_funcs_diff.jl:330-430); Roe or IR faces. */
 int eg_lo_calc(eg_lo* lo, const double* q, int32_t mem);
 /* applyLinearOperator: y = J x; x, y FP64 in host or device memory */
 int eg_lo_apply(eg_lo* lo, const double* x, double* y, int32_t mem);
@@ -411,15 +414,24 @@ int eg_get_launch_config(eg_mesh* mesh, eg_launch_config* config);
 int eg_autotune(eg_mesh* mesh, const double* q_dev, int32_t reps, eg_tune_entry* table,
                 int32_t max_entries, int32_t* n_entries);
 
-/* Frees the Newton work objects a mesh keeps between solves (the reference
-   frees its linear solver with `free(ls)`, LinearSolvers.jl).  Mesh destroy
-   frees them too. */
+/* Frees the work objects a mesh keeps between solves: Newton's operator,
+   preconditioner, Krylov basis and vectors, and eg_rk4's work vectors and
+   step graphs (the reference frees its linear solver with `free(ls)`,
+   LinearSolvers.jl).  Mesh destroy frees them too. */
 int eg_newton_release(eg_mesh* mesh);
 
 /* rk4 (reference src/NonlinearSolvers/rk4.jl:144-336, 404-456): classical
    4-stage RK4 on dq/dt = M^-1 R(q) with step h for round(t_max/h) steps
    (fewer if itermax > 0 is reached, or if res_tol > 0 and the stage-1 norm
-   drops below it). */
+   drops below it).  The first call on a mesh allocates six state-sized work
+   vectors (48 bytes per unknown) that the mesh keeps (eg_newton_release or
+   destroy frees them).  With the phase timers off and a mesh stream that can
+   be captured (not the legacy default stream), each time step is replayed as
+   a CUDA graph captured on first use for this h (one graph per step; with
+   res_tol > 0, one for stage 1 with the norm read-back and one for stages
+   2-4); otherwise the same kernels launch one by one, with the same results.
+   q (host or device per `mem`) is copied in at the start and written back at
+   the end, not after a device error. */
 int eg_rk4(eg_mesh* mesh, double* q, double h, double t_max, int32_t itermax, double res_tol,
            int32_t mem, eg_rk4_stats* stats);
 
@@ -434,9 +446,13 @@ int eg_rk4(eg_mesh* mesh, double* q, double h, double t_max, int32_t itermax, do
    eg_rk4, for meshes of at most EG_RK4_STATIC_MAX_DOF unknowns (larger ones:
    EG_ERR_INVALID); the work vectors live in one static 24 MiB device array
    per device.  The first call on a device resolves that array's address with
-   the device current and should come before any stream capture.  Phase timers
-   must be off (EG_ERR_INVALID otherwise).  Calls that overlap in time on one
-   device race on the shared array. */
+   the device current and should come before any stream capture (the address
+   is resolved again if the device's context has changed, e.g. after
+   cudaDeviceReset).  The mesh must belong to the current device, and its
+   stream to that device (EG_ERR_INVALID otherwise, before any device work).
+   Phase timers must be off (EG_ERR_INVALID otherwise).  Kernels launch one by
+   one (no graphs).  Calls that overlap in time on one device race on the
+   shared array. */
 int eg_rk4_static(eg_mesh* mesh, double* q, double h, double t_max, int32_t itermax,
                   double res_tol, int32_t mem, eg_rk4_stats* stats);
 

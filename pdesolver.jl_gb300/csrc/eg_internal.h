@@ -49,11 +49,13 @@ enum { EG_PHASE_FACE = 0, EG_PHASE_ELEMENT = 1, EG_PHASE_NORM = 2, EG_PHASE_OTHE
 
 struct TimerState;     // event pool (eg_timing.cu)
 struct eg_newton_ws;   // cached Newton work objects (eg_solvers.cu)
+struct eg_rk4_ws;      // cached RK4 work vectors and step graphs (eg_solvers.cu)
 
 struct eg_mesh {
   // sizes
   int dim, E, Np, Nf, S, F, I, B, nbc, norient, nv;
   int64_t ndof;
+  int device;       // CUDA device current when the mesh was created (owns its arrays)
   eg_params params;
   DevParams dp;
   cudaStream_t stream;
@@ -95,6 +97,7 @@ struct eg_mesh {
   bool capturing;           // a CUDA graph is being captured on `stream`
   eg_newton_ws* nws;        // Newton operator / preconditioner / solver / vectors, kept
                             // between solves (released by eg_newton_release or destroy)
+  eg_rk4_ws* rws;           // RK4 work vectors and step graphs, kept between eg_rk4 calls
   double* prolong_T;        // device copy of the last prolongation matrix (eg_prolong)
   size_t prolong_T_n;
   // launch configuration of the element kernels (eg_set_launch_config /
@@ -103,6 +106,18 @@ struct eg_mesh {
   int vol_mma;              // weak-form Q^T F on the FP64 tensor cores (mma.sync m8n8k4)
 };
 void eg_newton_ws_free(eg_mesh* m);
+void eg_rk4_ws_free(eg_mesh* m);
+// EG_OK when the calling thread's current device is the mesh's and the mesh
+// stream belongs to it; EG_ERR_INVALID (with a message naming `who`) otherwise
+int eg_check_device(const eg_mesh* m, const char* who);
+// The RK4 step loop of eg_rk4 (reference rk4.jl:201-330) on the device
+// buffers buf[6][ndof] = x_old, k1, k2, k3, res, q, with q = x_old = the
+// start state already in place and the status word cleared.  use_graphs:
+// replay captured CUDA graphs of the step (the mesh keeps them) where the
+// stream can be captured.  On return the stream has no work of the loop left
+// when the status is not EG_OK.
+int eg_rk4_loop(eg_mesh* m, double* buf, double h, double t_max, int itermax, double res_tol,
+                bool use_graphs, eg_rk4_stats* out);
 
 // phase timers: bracket a group of launches on m->stream
 void eg_phase_begin(eg_mesh* m, int phase);

@@ -117,6 +117,7 @@ static void boundary_states(const DevParams& p, int dim, int B, int Nf, const in
 static void free_mesh(eg_mesh* m) {
   if (!m) return;
   eg_newton_ws_free(m);
+  eg_rk4_ws_free(m);
   if (m->prolong_T) cudaFree(m->prolong_T);
   void* bufs[] = {m->Q, m->w, m->interp, m->perm, m->nbrperm, m->wface, m->lift, m->liftS,
                   m->nbrinv, m->dxidx,
@@ -158,8 +159,11 @@ extern "C" int eg_mesh_create(const eg_mesh_desc* d, const eg_params* params, eg
     eg_set_error("eg_mesh_create: volume_integral_type must be 1 or 2");
     return EG_ERR_INVALID;
   }
+  int dev = -1;
+  EG_CUDA(cudaGetDevice(&dev));
   eg_mesh* m = new eg_mesh();
   std::memset(m, 0, sizeof(*m));
+  m->device = dev;
   m->dim = d->dim;
   m->E = d->num_el;
   m->Np = d->nodes_per_el;

@@ -618,71 +618,233 @@ extern "C" int eg_newton_solve(eg_mesh* m, double* q, int32_t mem, const eg_newt
   return st;
 }
 
-extern "C" int eg_rk4(eg_mesh* m, double* q, double h, double t_max, int32_t itermax, double res_tol,
-                      int32_t mem, eg_rk4_stats* stats) {
-  if (!m || !q || !(h > 0)) {
-    eg_set_error("eg_rk4: invalid argument");
-    return EG_ERR_INVALID;
+// RK4 work objects a mesh keeps between eg_rk4 calls: the six state-sized
+// vectors of the step loop, and CUDA graphs of one step (whole step; stage 1
+// with the norm read-back; stages 2-4), captured on first use and bound to
+// the vectors, the step size and the launch configuration they were taken
+// with.
+struct eg_rk4_ws {
+  double* buf = nullptr;  // [6][N]: x_old, k1, k2, k3, res, q
+  bool tried = false;     // capture attempted for `key`
+  bool have = false;      // graphs valid for `key`
+  struct {
+    eg_params params;
+    double h;
+    int elem_epb, vol_mma;
+    cudaStream_t stream;
+  } key;
+  cudaGraphExec_t g_step = nullptr, g_stage1 = nullptr, g_rest = nullptr;
+  int64_t n_step = 0, n_stage1 = 0, n_rest = 0;
+};
+
+namespace {
+
+void rk4_graphs_free(eg_rk4_ws* w) {
+  cudaGraphExec_t gs[] = {w->g_step, w->g_stage1, w->g_rest};
+  for (cudaGraphExec_t g : gs)
+    if (g) cudaGraphExecDestroy(g);
+  w->g_step = w->g_stage1 = w->g_rest = nullptr;
+  w->have = false;
+}
+
+// stage 1: k1 = M^-1 R(q), q = x_old + h/2 k1, and (with_norm) the norm of
+// k1 weighted by M, sqrt(sum k1^2 M), read back into m->h_red[0]
+int rk4_stage1(eg_mesh* m, double* buf, double h, bool with_norm) {
+  const int64_t N = m->ndof;
+  double *xold = buf, *k1 = buf + N, *res = buf + 4 * N, *qd = buf + 5 * N;
+  int st = eg_launch_residual(m, qd, res);
+  if (st != EG_OK) return st;
+  eg_launch_rk4_stage(m, res, xold, h / 2, k1, qd);
+  m->launches += 1;
+  if (with_norm) {
+    eg_launch_norm(m, k1, 0, m->red + 2048);
+    EG_CUDA(cudaMemcpyAsync(m->h_red, m->red + 2048, sizeof(double), cudaMemcpyDeviceToHost, m->stream));
   }
-  const int64_t N = m->ndof, nnode = (int64_t)m->E * m->Np;
-  double* buf = nullptr;
-  cudaError_t ce = cudaMalloc((void**)&buf, 8 * N * (mem == EG_MEM_HOST ? 6 : 5));
-  if (ce != cudaSuccess) return eg_cuda_fail(ce, "eg_rk4");
-  double* xold = buf;
-  double* k1 = buf + N;
-  double* k2 = buf + 2 * N;
-  double* k3 = buf + 3 * N;
-  double* res = buf + 4 * N;
-  double* qd = mem == EG_MEM_HOST ? buf + 5 * N : q;
-  if (mem == EG_MEM_HOST) cudaMemcpyAsync(qd, q, 8 * N, cudaMemcpyHostToDevice, m->stream);
-  cudaMemcpyAsync(xold, qd, 8 * N, cudaMemcpyDeviceToDevice, m->stream);
-  const int g = grid64(N);
+  EG_CUDA(cudaGetLastError());
+  return EG_OK;
+}
+
+// stages 2, 3, 4 and the update of x_old and q
+int rk4_rest(eg_mesh* m, double* buf, double h) {
+  const int64_t N = m->ndof;
+  double *xold = buf, *k1 = buf + N, *k2 = buf + 2 * N, *k3 = buf + 3 * N, *res = buf + 4 * N,
+         *qd = buf + 5 * N;
+  int st = eg_launch_residual(m, qd, res);
+  if (st == EG_OK) {
+    eg_launch_rk4_stage(m, res, xold, h / 2, k2, qd);
+    st = eg_launch_residual(m, qd, res);
+  }
+  if (st == EG_OK) {
+    eg_launch_rk4_stage(m, res, xold, h, k3, qd);
+    st = eg_launch_residual(m, qd, res);
+  }
+  if (st != EG_OK) return st;
+  eg_launch_rk4_final(m, k1, k2, k3, res, h, xold, qd);
+  m->launches += 3;
+  EG_CUDA(cudaGetLastError());
+  return EG_OK;
+}
+
+// graphs of the step for (h, the mesh's launch configuration and parameters,
+// the stream); false when the stream cannot be captured (the caller falls
+// back to eager launches of the same kernels)
+bool rk4_graphs(eg_mesh* m, eg_rk4_ws* w, double h) {
+  const bool same = w->tried && w->key.h == h && w->key.elem_epb == m->elem_epb &&
+                    w->key.vol_mma == m->vol_mma && w->key.stream == m->stream &&
+                    std::memcmp(&w->key.params, &m->params, sizeof(eg_params)) == 0;
+  if (same) return w->have;
+  rk4_graphs_free(w);
+  w->tried = true;
+  w->key.params = m->params;
+  w->key.h = h;
+  w->key.elem_epb = m->elem_epb;
+  w->key.vol_mma = m->vol_mma;
+  w->key.stream = m->stream;
+  double* buf = w->buf;
+  bool ok = capture_graph(m, [&]() {
+    rk4_stage1(m, buf, h, false);
+    rk4_rest(m, buf, h);
+  }, &w->g_step, &w->n_step);
+  ok = ok && capture_graph(m, [&]() { rk4_stage1(m, buf, h, true); }, &w->g_stage1, &w->n_stage1);
+  ok = ok && capture_graph(m, [&]() { rk4_rest(m, buf, h); }, &w->g_rest, &w->n_rest);
+  if (!ok) rk4_graphs_free(w);
+  w->have = ok;
+  return ok;
+}
+
+int rk4_ws(eg_mesh* m, eg_rk4_ws** out) {
+  if (!m->rws) {
+    eg_rk4_ws* w = new eg_rk4_ws();
+    cudaError_t ce = cudaMalloc((void**)&w->buf, 6 * 8 * (size_t)m->ndof);
+    if (ce != cudaSuccess) {
+      delete w;
+      return eg_cuda_fail(ce, "eg_rk4");
+    }
+    m->rws = w;
+  }
+  *out = m->rws;
+  return EG_OK;
+}
+
+}  // namespace
+
+void eg_rk4_ws_free(eg_mesh* m) {
+  eg_rk4_ws* w = m ? m->rws : nullptr;
+  if (!w) return;
+  rk4_graphs_free(w);
+  if (w->buf) cudaFree(w->buf);
+  delete w;
+  m->rws = nullptr;
+}
+
+int eg_rk4_loop(eg_mesh* m, double* buf, double h, double t_max, int itermax, double res_tol,
+                bool use_graphs, eg_rk4_stats* out) {
+  eg_rk4_ws* w = m->rws;
+  const bool graphs = use_graphs && w && w->buf == buf && !eg_timing_on(m) && !m->capturing &&
+                      rk4_graphs(m, w, h);
+  const bool with_norm = res_tol > 0;
   const long t_steps = lround(t_max / h);
   double t = 0.0, last_norm = 0.0;
   int steps = 0, st = EG_OK;
-  cudaMemsetAsync(m->status, 0, sizeof(unsigned int), m->stream);
   // loop i = 2 .. t_steps+1 of the reference (rk4.jl:201)
   for (long i = 2; i <= t_steps + 1; ++i) {
     t = (i - 2) * h;
+    const bool stop_after_stage1 = itermax > 0 && i > itermax;
+    if (graphs && !with_norm && !stop_after_stage1) {
+      cudaError_t ce = cudaGraphLaunch(w->g_step, m->stream);
+      if (ce != cudaSuccess) {
+        st = eg_cuda_fail(ce, "eg_rk4 graph");
+        break;
+      }
+      m->launches += w->n_step;
+      ++steps;
+      continue;
+    }
     // stage 1 (with the norm, as pde_post_func with calc_norm=true)
-    st = eg_launch_residual(m, qd, res);
-    if (st != EG_OK) break;
-    k_rk4_stage<<<g, 256, 0, m->stream>>>(res, m->Minv, xold, h / 2, k1, qd, nnode, m->nv);
-    m->launches += 1;
-    if (res_tol > 0) {
-      // norm of k1 = M^-1 R weighted by M: sqrt(sum k1^2 M)
-      eg_launch_norm(m, k1, 0, m->red + 2048);
-      cudaMemcpyAsync(m->h_red, m->red + 2048, sizeof(double), cudaMemcpyDeviceToHost, m->stream);
-      cudaStreamSynchronize(m->stream);
+    if (graphs && with_norm) {
+      cudaError_t ce = cudaGraphLaunch(w->g_stage1, m->stream);
+      if (ce != cudaSuccess) {
+        st = eg_cuda_fail(ce, "eg_rk4 graph");
+        break;
+      }
+      m->launches += w->n_stage1;
+    } else {
+      st = rk4_stage1(m, buf, h, with_norm);
+      if (st != EG_OK) break;
+    }
+    if (with_norm) {
+      cudaError_t ce = cudaStreamSynchronize(m->stream);
+      if (ce != cudaSuccess) {
+        st = eg_cuda_fail(ce, "eg_rk4");
+        break;
+      }
       last_norm = m->h_red[0];
       // the reference breaks after the stage-1 update of q (rk4.jl:258-280)
       if (last_norm < res_tol) break;
     }
-    if (itermax > 0 && i > itermax) break;
+    if (stop_after_stage1) break;
     // stages 2, 3, 4
-    eg_launch_residual(m, qd, res);
-    k_rk4_stage<<<g, 256, 0, m->stream>>>(res, m->Minv, xold, h / 2, k2, qd, nnode, m->nv);
-    eg_launch_residual(m, qd, res);
-    k_rk4_stage<<<g, 256, 0, m->stream>>>(res, m->Minv, xold, h, k3, qd, nnode, m->nv);
-    eg_launch_residual(m, qd, res);
-    k_rk4_final<<<g, 256, 0, m->stream>>>(k1, k2, k3, res, m->Minv, h, xold, qd, nnode, m->nv);
-    m->launches += 3;
+    if (graphs) {
+      cudaError_t ce = cudaGraphLaunch(w->g_rest, m->stream);
+      if (ce != cudaSuccess) {
+        st = eg_cuda_fail(ce, "eg_rk4 graph");
+        break;
+      }
+      m->launches += w->n_rest;
+    } else {
+      st = rk4_rest(m, buf, h);
+      if (st != EG_OK) break;
+    }
     ++steps;
   }
   t += h;
+  // a failed launch leaves earlier work queued: let it finish before the
+  // caller reuses or frees the buffers
+  if (st != EG_OK) cudaStreamSynchronize(m->stream);
+  if (out) {
+    out->steps = steps;
+    out->t = t;
+    out->res_norm = last_norm;
+  }
+  return st;
+}
+
+extern "C" int eg_rk4(eg_mesh* m, double* q, double h, double t_max, int32_t itermax, double res_tol,
+                      int32_t mem, eg_rk4_stats* stats) {
+  if (!m || !q || !(h > 0) || (mem != EG_MEM_HOST && mem != EG_MEM_DEVICE)) {
+    eg_set_error("eg_rk4: invalid argument");
+    return EG_ERR_INVALID;
+  }
+  int st = eg_check_device(m, "eg_rk4");
+  if (st != EG_OK) return st;
+  eg_rk4_ws* w = nullptr;
+  if ((st = rk4_ws(m, &w)) != EG_OK) return st;
+  const int64_t N = m->ndof;
+  double* buf = w->buf;
+  double* qd = buf + 5 * N;
+  // the loop iterates in the mesh's own copy of the state (the graphs are
+  // bound to it); x_old starts as the same state
+  EG_CUDA(cudaMemcpyAsync(qd, q, 8 * N, mem == EG_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice,
+                          m->stream));
+  EG_CUDA(cudaMemcpyAsync(buf, qd, 8 * N, cudaMemcpyDeviceToDevice, m->stream));
+  EG_CUDA(cudaMemsetAsync(m->status, 0, sizeof(unsigned int), m->stream));
+  eg_rk4_stats s;
+  st = eg_rk4_loop(m, buf, h, t_max, itermax, res_tol, true, &s);
   if (st == EG_OK) {
-    cudaMemcpyAsync(m->h_status, m->status, sizeof(unsigned int), cudaMemcpyDeviceToHost, m->stream);
-    if (mem == EG_MEM_HOST) cudaMemcpyAsync(q, qd, 8 * N, cudaMemcpyDeviceToHost, m->stream);
-    ce = cudaStreamSynchronize(m->stream);
-    if (ce != cudaSuccess) st = eg_cuda_fail(ce, "eg_rk4");
-    else st = eg_check_status(m);
+    cudaError_t ce = cudaMemcpyAsync(m->h_status, m->status, sizeof(unsigned int), cudaMemcpyDeviceToHost,
+                                     m->stream);
+    if (ce == cudaSuccess)
+      ce = cudaMemcpyAsync(q, qd, 8 * N, mem == EG_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice,
+                           m->stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(m->stream);
+    if (ce != cudaSuccess) {
+      cudaStreamSynchronize(m->stream);
+      st = eg_cuda_fail(ce, "eg_rk4");
+    } else {
+      st = eg_check_status(m);
+    }
   }
-  cudaFree(buf);
-  if (stats) {
-    stats->steps = steps;
-    stats->t = t;
-    stats->res_norm = last_norm;
-  }
+  if (stats) *stats = s;
   return st;
 }
 

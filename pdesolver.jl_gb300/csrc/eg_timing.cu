@@ -108,8 +108,42 @@ extern "C" int eg_reset_timings(eg_mesh* m) {
 
 extern "C" int eg_mesh_set_stream(eg_mesh* m, void* stream, int32_t use_own) {
   if (!m) return EG_ERR_INVALID;
+  cudaStream_t s = use_own ? m->own_stream : (cudaStream_t)stream;
+  if (s != 0 && s != cudaStreamLegacy && s != cudaStreamPerThread) {
+    // a stream of another device would run the mesh's kernels there
+    int sdev = -1;
+    EG_CUDA(cudaStreamGetDevice(s, &sdev));
+    if (sdev != m->device) {
+      eg_set_error("eg_mesh_set_stream: the stream belongs to device %d, the mesh to device %d",
+                   sdev, m->device);
+      return EG_ERR_INVALID;
+    }
+  }
   EG_CUDA(cudaStreamSynchronize(m->stream));
-  m->stream = use_own ? m->own_stream : (cudaStream_t)stream;
+  m->stream = s;
+  return EG_OK;
+}
+
+int eg_check_device(const eg_mesh* m, const char* who) {
+  int dev = -1;
+  cudaError_t ce = cudaGetDevice(&dev);
+  if (ce != cudaSuccess) return eg_cuda_fail(ce, who);
+  if (dev != m->device) {
+    eg_set_error("%s: the current device is %d, the mesh was created on device %d", who, dev,
+                 m->device);
+    return EG_ERR_INVALID;
+  }
+  cudaStream_t s = m->stream;
+  if (s != 0 && s != cudaStreamLegacy && s != cudaStreamPerThread) {
+    int sdev = -1;
+    ce = cudaStreamGetDevice(s, &sdev);
+    if (ce != cudaSuccess) return eg_cuda_fail(ce, who);
+    if (sdev != m->device) {
+      eg_set_error("%s: the mesh stream belongs to device %d, the mesh to device %d", who, sdev,
+                   m->device);
+      return EG_ERR_INVALID;
+    }
+  }
   return EG_OK;
 }
 

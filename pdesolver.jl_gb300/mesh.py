@@ -133,6 +133,13 @@ def _connect(elverts, faces_local, sbp, face_pts_all, tags_of_faces, bc_of_tag):
     order = np.lexsort(keys.T[::-1])
     ks = keys[order]
     same = np.all(ks[1:] == ks[:-1], axis=1)
+    if np.any(same[1:] & same[:-1]):
+        # a run of three or more equal keys: a face shared by more than two
+        # elements (non-manifold or duplicated elements) would become two
+        # overlapping interfaces and be integrated twice
+        nbad = int(np.count_nonzero(same[1:] & same[:-1]))
+        raise ValueError(f"mesh: {nbad} faces are shared by more than two elements "
+                         "(non-manifold mesh or duplicated elements)")
     first = np.nonzero(same)[0]
     a, b = order[first], order[first + 1]          # element-face ids sharing a face
     pair_lo = np.minimum(a, b)
@@ -385,7 +392,15 @@ def from_elements(sbp: SBPOperator, vertices, elements, boundary_tags, bc_of_tag
         raise ValueError("mesh: element vertex id out of range")
     X = vx[elverts]
     J0 = np.stack([X[:, k + 1] - X[:, 0] for k in range(d)], axis=2)
-    neg = np.linalg.det(J0) < 0
+    det0 = np.linalg.det(J0)
+    # zero-volume elements (repeated or collinear/coplanar vertices) have no
+    # metric terms: refuse them instead of dividing by zero later
+    edge = np.linalg.norm(J0, axis=1).max(axis=1)
+    flat = np.abs(det0) <= 64 * np.finfo(np.float64).eps * edge ** d
+    if np.any(flat):
+        raise ValueError(f"mesh: {int(np.count_nonzero(flat))} elements are degenerate "
+                         f"(zero volume; first: element {int(np.nonzero(flat)[0][0])})")
+    neg = det0 < 0
     elverts[neg, d - 1], elverts[neg, d] = elverts[neg, d].copy(), elverts[neg, d - 1].copy()
     X = vx[elverts]                                  # [E, d+1, d]
     # affine map from the reference simplex: x = X0 + sum_k (X_{k+1} - X0)(xi_k + 1)/2

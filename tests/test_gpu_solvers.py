@@ -192,6 +192,35 @@ def test_rk4_matches_oracle(gpu_lib, oracle):
     assert np.abs(qg - qo).max() <= 1e-11 * np.abs(qo).max()
 
 
+def test_rk4_graph_path_equals_eager_path(gpu_lib):
+    """eg_rk4 replays each step as a CUDA graph when the timers are off and
+    launches the same kernels one by one when they are on: the states, step
+    counts and norms are bitwise equal, for whole steps, for the per-step
+    norm test (res_tol) and for the itermax stop after stage 1."""
+    ms, opts, q0 = problems.config1(n=6, p=2, seed=12)
+    g = eulergpu.GPUMesh(ms, opts)
+    h = 2e-3
+    for itermax, res_tol in ((0, -1.0), (0, 1e-30), (4, -1.0)):
+        out = []
+        for timers in (False, True, False):
+            g.set_timing(timers)
+            q = q0.copy()
+            st = g.rk4(q, h, 7 * h, itermax=itermax, res_tol=res_tol)
+            out.append((q, st.steps, st.t, st.res_norm))
+        g.set_timing(False)
+        for q, steps, t, nrm in out[1:]:
+            assert np.array_equal(q, out[0][0])
+            assert (steps, t, nrm) == out[0][1:]
+    # one device step of the graph path counts its kernels like the eager path
+    l0 = g.timings().launches
+    g.rk4(q0.copy(), h, 3 * h)
+    l1 = g.timings().launches
+    g.set_timing(True)
+    g.rk4(q0.copy(), h, 3 * h)
+    g.set_timing(False)
+    assert g.timings().launches - l1 == l1 - l0
+
+
 def test_wrong_sized_state_is_refused(gpu_lib):
     """a state of another degree's mesh is refused before any device work."""
     import torch

@@ -116,6 +116,36 @@ def test_reader_refusals(tmp_path):
         mesh_io.read_gmsh(p3, sbp.get_operator(3, "diage", 1))
 
 
+def test_degenerate_and_non_manifold_meshes_are_refused(tmp_path):
+    """a flat triangle (zero volume, e.g. a bad Gmsh file) and a face shared
+    by three elements are refused with a message, not turned into a
+    non-finite residual or a doubly integrated interface."""
+    op = sbp.get_operator(2, "omega", 1)
+    vx, el, tags = mesh.annulus_grid(2, 2)
+    flat = np.array([[0, 1, 1]] + el[1:].tolist())     # repeated vertex
+    with pytest.raises(ValueError, match="degenerate"):
+        mesh.from_elements(op, vx, flat, tags, default_tag=0)
+    vx2 = np.r_[vx, [[(vx[el[0, 0]] + vx[el[0, 1]])[0] / 2, (vx[el[0, 0]] + vx[el[0, 1]])[1] / 2]]]
+    collinear = np.r_[el, [[el[0, 0], el[0, 1], len(vx)]]]   # vertices on one line
+    with pytest.raises(ValueError, match="degenerate"):
+        mesh.from_elements(op, vx2, collinear, tags, default_tag=0)
+    path = tmp_path / "flat.msh"
+    mesh_io.write_gmsh(path, vx2, collinear, tags)
+    with pytest.raises(ValueError, match="degenerate"):
+        mesh_io.read_gmsh(path, op)
+    # a third element on an interior edge (one two elements share), on a new vertex
+    edges = {}
+    for e in el.tolist():
+        for a, b in ((0, 1), (1, 2), (0, 2)):
+            k = tuple(sorted((e[a], e[b])))
+            edges[k] = edges.get(k, 0) + 1
+    inner = next(k for k, c in edges.items() if c == 2)
+    vx3 = np.r_[vx, [[5.0, 5.0]]]
+    third = np.r_[el, [[inner[0], inner[1], len(vx)]]]
+    with pytest.raises(ValueError, match="more than two elements"):
+        mesh.from_elements(op, vx3, third, tags, default_tag=0)
+
+
 @pytest.mark.parametrize("fam,p", [("omega", 2), ("gamma", 3)])
 def test_distorted_mesh_preserves_free_stream(oracle, fam, p):
     """a mesh of irregular straight-sided triangles (the annulus grid with its
