@@ -50,8 +50,11 @@ typedef enum { EG_MEM_HOST = 0, EG_MEM_DEVICE = 1 } eg_mem;
 /* numerical flux names (reference FluxDict, src/solver/euler/flux.jl) */
 typedef enum { EG_FLUX_ROE = 0, EG_FLUX_IR = 1 } eg_flux;
 
-/* boundary condition functors (reference BCDict, src/solver/euler/bc.jl) */
-typedef enum { EG_BC_VORTEX = 0, EG_BC_FREESTREAM = 1 } eg_bc;
+/* boundary condition functors (reference BCDict, src/solver/euler/bc.jl):
+   isentropicVortexBC (bc.jl:542-568), FreeStreamBC (bc.jl:1562-1647),
+   noPenetrationESBC (bc.jl:767-795: mirror state and Lax-Friedrichs flux,
+   entropy stable with diagonal-E operators) */
+typedef enum { EG_BC_VORTEX = 0, EG_BC_FREESTREAM = 1, EG_BC_NOPENETRATION_ES = 2 } eg_bc;
 
 /*
  * Physics parameters: the subset of ParamType / opts the hot path reads
@@ -286,6 +289,13 @@ int eg_ls_set_grid(eg_ls* ls, int32_t blocks);
 int eg_set_gmres_batching(int32_t enable, double window_us);
 /* linearSolve: x <- A^-1 b (x is also the initial guess) */
 int eg_ls_solve(eg_ls* ls, const double* b, double* x, int32_t mem, eg_ls_stats* stats);
+/* linearSolveTranspose (reference ls_standard.jl:230-244, the adjoint solve of
+   calcAdjoint): x <- A^-T b by GMRES(restart) right-preconditioned with the
+   transposed block-Jacobi inverses, on J^T M^-T = I + C^T D^-T (coupling
+   blocks applied transposed, element blocks cancel); same tolerances, device
+   Hessenberg and Givens, and restart cycles replayed as CUDA graphs as the
+   forward solve's stream path.  x is also the initial guess. */
+int eg_ls_solve_transpose(eg_ls* ls, const double* b, double* x, int32_t mem, eg_ls_stats* stats);
 
 /* ---- Newton and RK4 drivers ------------------------------------------- */
 typedef struct {

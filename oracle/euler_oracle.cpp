@@ -165,6 +165,10 @@ int eval_residual(const eg_mesh_desc* d, const eg_params* ep, const T* q, T* res
         }
         const double* x = d->coords_bndry + ((size_t)b * Nf + i) * DIM;
         const double* nrm = d->nrm_bndry + ((size_t)b * Nf + i) * DIM;
+        if (bc == EG_BC_NOPENETRATION_ES) {
+          nopenetration_es_flux<DIM>(p, qf, nrm, fl[i]);
+          continue;
+        }
         boundary_state<DIM>(p, bc, x, qg);
         for (int c = 0; c < nv; ++c) qgT[c] = T(qg[c]);
         roe_solver<DIM>(p, qf, qgT, nrm, fl[i]);
@@ -290,6 +294,18 @@ void oracle_ir_flux(const eg_params* ep, int dim, const double* qL, const double
 }
 
 double oracle_logavg(double a, double b) { return logavg(a, b); }
+
+// boundary flux of noPenetrationESBC at one face node (bc.jl:767-795)
+void oracle_wall_es_flux(const eg_params* ep, int dim, const double* q, const double* nrm, double* F) {
+  Params p = make_params(ep);
+  if (dim == 2) nopenetration_es_flux<2>(p, q, nrm, F); else nopenetration_es_flux<3>(p, q, nrm, F);
+}
+
+void oracle_lf_flux(const eg_params* ep, int dim, const double* qL, const double* qR, const double* nrm,
+                    double* F) {
+  Params p = make_params(ep);
+  if (dim == 2) lf_flux<2>(p, qL, qR, nrm, F); else lf_flux<3>(p, qL, qR, nrm, F);
+}
 
 // d logavg / d(aL, aR) by forward-mode dual numbers (the derivative that the
 // Jacobian assembly uses; logavg_diff, bc_solvers_diff.jl:5644-5716)
@@ -433,10 +449,15 @@ int eval_jacobian(const eg_mesh_desc* d, const eg_params* ep, const double* q, d
       for (int s = 0; s < S; ++s)
         for (int c = 0; c < NV; ++c) qf[c].v += v.interp(f, i, s) * q[((size_t)e * Np + v.perm(f, s)) * NV + c];
       for (int c = 0; c < NV; ++c) qf[c].d[c] = 1.0;
-      double qg[5];
-      boundary_state<DIM>(p, bc, d->coords_bndry + ((size_t)b * Nf + i) * DIM, qg);
-      for (int c = 0; c < NV; ++c) qgD[c] = Dual<NV>(qg[c]);
-      roe_solver<DIM>(p, qf, qgD, d->nrm_bndry + ((size_t)b * Nf + i) * DIM, fl);
+      if (bc == EG_BC_NOPENETRATION_ES) {
+        // the mirror state follows q: differentiated through it
+        nopenetration_es_flux<DIM>(p, qf, d->nrm_bndry + ((size_t)b * Nf + i) * DIM, fl);
+      } else {
+        double qg[5];
+        boundary_state<DIM>(p, bc, d->coords_bndry + ((size_t)b * Nf + i) * DIM, qg);
+        for (int c = 0; c < NV; ++c) qgD[c] = Dual<NV>(qg[c]);
+        roe_solver<DIM>(p, qf, qgD, d->nrm_bndry + ((size_t)b * Nf + i) * DIM, fl);
+      }
       for (int s = 0; s < S; ++s)
         for (int sp = 0; sp < S; ++sp) {
           const double c0 = v.interp(f, i, s) * d->wface[i] * v.interp(f, i, sp);

@@ -171,6 +171,59 @@ inline void roe_solver(const Params& p, const T* q, const T* qg, const Tn* nrm, 
   for (int i = 0; i < nv; ++i) flux[i] = sat[i] + ef[i];
 }
 
+// ------------------------------------------------------------ noPenetrationESBC
+// bc.jl:767-795.  getDirichletState (bc.jl:860-919): qg = q with the normal
+// momentum reversed, qg_m = -2 (n^ . m) n^ + m with n^ = nrm / |nrm|.
+template <int DIM, typename T>
+inline void nopenetration_state(const T* q, const double* nrm, T* qg) {
+  double n2 = 0;
+  for (int k = 0; k < DIM; ++k) n2 += nrm[k] * nrm[k];
+  const double fac = 1.0 / std::sqrt(n2);
+  double nh[3];
+  for (int k = 0; k < DIM; ++k) nh[k] = nrm[k] * fac;
+  T Unrm = T(0.0);
+  for (int k = 0; k < DIM; ++k) Unrm = Unrm + nh[k] * q[1 + k];
+  qg[0] = q[0];
+  for (int k = 0; k < DIM; ++k) qg[1 + k] = -2 * Unrm * nh[k] + q[1 + k];
+  qg[DIM + 1] = q[DIM + 1];
+}
+
+// getLambdaMax (euler_funcs.jl:1887-1910): |U . dir| + |dir| a
+template <int DIM, typename T>
+inline T lambda_max(const Params& p, const T* q, const double* dir) {
+  T rhoinv = 1.0 / q[0];
+  T pr = pressure<DIM>(p, q);
+  T a = sqrt(p.gamma * pr * rhoinv);
+  T Un = T(0.0);
+  double dA = 0;
+  for (int i = 0; i < DIM; ++i) {
+    Un = Un + dir[i] * q[i + 1] * rhoinv;
+    dA += dir[i] * dir[i];
+  }
+  return absvalue(Un) + std::sqrt(dA) * a;
+}
+
+// calcLFFlux (bc_solvers.jl:428-446) with getLambdaMaxSimple
+// (IR_stab.jl:310-326: lambda_max at the arithmetic mean of the states)
+template <int DIM, typename T>
+inline void lf_flux(const Params& p, const T* qL, const T* qR, const double* dir, T* F) {
+  const int nv = DIM + 2;
+  T fL[5], fR[5], qa[5];
+  euler_flux<DIM>(p, qL, dir, fL);
+  euler_flux<DIM>(p, qR, dir, fR);
+  for (int i = 0; i < nv; ++i) qa[i] = 0.5 * (qL[i] + qR[i]);
+  T lam = lambda_max<DIM>(p, qa, dir);
+  for (int i = 0; i < nv; ++i) F[i] = 0.5 * (fL[i] + fR[i] - lam * (qR[i] - qL[i]));
+}
+
+// the boundary flux of noPenetrationESBC at one face node
+template <int DIM, typename T>
+inline void nopenetration_es_flux(const Params& p, const T* q, const double* nrm, T* F) {
+  T qg[5];
+  nopenetration_state<DIM>(q, nrm, qg);
+  lf_flux<DIM>(p, q, qg, nrm, F);
+}
+
 // ------------------------------------------------------------ logavg
 // bc_solvers.jl:942-956: logarithmic mean, 5-term series for u < 1e-3
 template <typename T>

@@ -4,15 +4,16 @@ evalFunctionalDeriv_q, interface2.jl:259-300; calcAdjoint,
 optimization/steady_adjoint.jl:30-89).
 
 The adjoint psi of a functional J at a converged state q solves
-(dR/dq)^T psi = -dJ/dq.  The transposed Jacobian and preconditioner applies
-run on the device in the library (eg_lo_apply_transpose,
-eg_pc_apply_transpose); the Krylov vectors are torch tensors on the same
-device, and the Krylov method is GMRES(restart) with right preconditioning,
-classical Gram-Schmidt with one re-orthogonalisation pass and Givens
-rotations, the method of the library's forward solve, here applied to
-J^T M^-T u = b, x = M^-T u.  The functional derivative is a sum over the
-boundary faces of one BC group (a few thousand face nodes), evaluated on the
-host from the state.
+(dR/dq)^T psi = -dJ/dq.  With the library's linear solver (an
+eulergpu.LinearSolver) the transposed solve is eg_ls_solve_transpose:
+GMRES(restart) on J^T M^-T u = b, x = M^-T u, entirely on the device (the
+transposed coupling and block-Jacobi applies, device Hessenberg and Givens,
+restart cycles replayed as CUDA graphs).  This module orchestrates: it forms
+the right-hand side and calls that solve.  For operators of the caller's own
+that expose apply_transpose (no library solver), `gmres` below runs the same
+Krylov method over those applies with torch vectors.  The functional
+derivative is a sum over the boundary faces of one BC group (a few thousand
+face nodes), evaluated on the host from the state.
 """
 from __future__ import annotations
 
@@ -161,12 +162,30 @@ def _as_tensor(a, device):
 
 def linearSolveTranspose(ls, b, x, reltol=None, abstol=None, itermax=None, device=None):
     """x <- solution of J^T x = b with the operator and preconditioner of
-    `ls` (an eulergpu.LinearSolver, or any object with .lo.apply_transpose,
-    .pc.apply_transpose and .restart); b and x are numpy arrays or float64
-    torch tensors of the mesh's size, x the initial guess.  The Krylov
-    vectors live on `device` (default: the CUDA device when there is one).
-    Tolerances default to those set on `ls` (set_tolerances), else 1e-10
-    relative.  Returns the gmres statistics."""
+    `ls`; b and x are numpy arrays or float64 torch tensors of the mesh's
+    size, x the initial guess.  Tolerances default to those set on `ls`
+    (set_tolerances), else 1e-10 relative.  An eulergpu.LinearSolver solves
+    on the device in the library (eg_ls_solve_transpose; `device` is not
+    used); any other object with .lo.apply_transpose, .pc.apply_transpose and
+    .restart runs `gmres` with its Krylov vectors on `device` (default: the
+    CUDA device when there is one).  Returns the solve's statistics as a dict
+    (iters, restarts, converged, res0, res_final)."""
+    from . import eulergpu
+    if isinstance(ls, eulergpu.LinearSolver):
+        if reltol is not None or abstol is not None or itermax is not None:
+            ls.set_tolerances(reltol=-1.0 if reltol is None else reltol,
+                              abstol=-1.0 if abstol is None else abstol,
+                              itermax=-1 if itermax is None else itermax)
+        elif ls.reltol is None or ls.reltol <= 0:
+            ls.set_tolerances(reltol=1e-10)
+        if isinstance(x, np.ndarray):
+            xb = np.ascontiguousarray(x, dtype=np.float64).reshape(-1).copy()
+            st = ls.solve_transpose(np.ascontiguousarray(b, dtype=np.float64).reshape(-1), xb)
+            x[...] = xb.reshape(x.shape)
+        else:
+            st = ls.solve_transpose(b.reshape(-1).contiguous(), x.reshape(-1))
+        return {"iters": st.iters, "restarts": st.restarts, "converged": bool(st.converged),
+                "res0": st.res0, "res_final": st.res_final}
     import torch
     if device is None:
         device = ("cuda" if torch.cuda.is_available() else "cpu") if isinstance(b, np.ndarray) else b.device

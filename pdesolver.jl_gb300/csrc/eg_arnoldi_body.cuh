@@ -6,21 +6,57 @@
 #pragma once
 #include <cooperative_groups.h>
 
+#include <algorithm>
+
 #include "eg_internal.h"
 #include "eg_kernels.cuh"
 #include "eg_krylov.cuh"
 #include "eg_linalg.h"
+#include "eg_tma.cuh"
 
 namespace cg = cooperative_groups;
 
 namespace {
 
-constexpr int NT = 1024;  // one block per SM
+constexpr int NT = 512;  // one block per SM (16 warps, up to 128 registers a thread)
+constexpr int NW = NT / 32;
 constexpr int NB_MAX = 64;  // coupling-block rows handled by the face-side pass
 // systems whose element blocks take at most this many bytes run on one block
 constexpr size_t kSmallOperatorBytes = size_t(2) << 20;
 
 constexpr int PSTRIDE = 33;  // partial slots per block
+
+// dynamic shared memory of one block, at most (the static GmresShared block
+// comes on top, within the 227 KB of an SM)
+constexpr size_t kSmemMax = 200 * 1024;
+// bytes of operator copies in flight per block (the ring of slots), at most
+constexpr size_t kRingBudget = 160 * 1024;
+// target bytes of one ring slot (elements per slot chosen to reach it)
+constexpr size_t kSlotTarget = 12 * 1024;
+
+// Operator ring of the Arnoldi apply: the block's elements are cut into units
+// of `eps` consecutive elements; unit u goes through slot u % nstage, which
+// belongs to consumer group u % nstage (wpg warps).  One thread of the group
+// issues the bulk copies of a unit (its inverse blocks, one contiguous range,
+// and, for 2-D dense coupling, the neighbours' coupling blocks of its faces)
+// on the slot's mbarrier; the group computes z = D^-1 v for the unit from
+// the slot, pushes the coupling products C z to the neighbours' face sides,
+// and issues the next unit into the slot.  After its last unit a group
+// issues its first unit again: the copies of the next Arnoldi iteration's
+// first units are in flight during the grid barriers and vector passes.
+struct RingCfg {
+  int on;          // 1: the Arnoldi apply runs through the ring
+  int nstage;      // slots = consumer groups
+  int eps;         // elements per unit
+  int wpg;         // warps per consumer group
+  int cpl_tma;     // coupling blocks arrive in the slot (2-D dense coupling)
+  int slot_bytes;  // bytes of one slot (multiple of 128)
+  int inv_cap;     // bytes of a slot's inverse-block region (multiple of 16)
+  int cpl_bytes;   // bytes of one coupling block
+  int fside_smem;  // the block's [epb][F] face-side table is staged in shared memory
+  // dynamic shared memory offsets (bytes)
+  int off_ring, off_bar, off_z, off_v, off_red, off_fside, off_sz;
+};
 
 template <typename T>
 struct CoopArgs {
@@ -42,6 +78,7 @@ struct CoopArgs {
   int m, n, E;
   int nb, S, F, nv, ec;  // coupling block size, stencil size, faces, variables, elements per chunk
   int64_t N;
+  RingCfg rc;
 };
 
 // NV consecutive values of a coupling row (16-byte loads for 2-D FP32)
@@ -190,7 +227,9 @@ __device__ void block_reduce_all(const T* __restrict__ part, int nblk, int cnt, 
 }
 
 // y = (x - sum_{k<cnt} V[k] h[k]) * s on the block's rows, by threads
-// t0 .. NT-1 (x and y may alias)
+// t0 .. NT-1 (x and y may alias).  The basis loads of a row are issued in
+// batches of 4 before their updates, so 4 loads per thread are in flight;
+// the sum runs over k in order.
 template <typename T>
 __device__ void block_sub_scale(const T* __restrict__ V, const T* __restrict__ h, int cnt, int64_t N,
                                 const T* x, T s, T* y, int64_t r0, int nrow, bool vec, int t0) {
@@ -200,26 +239,30 @@ __device__ void block_sub_scale(const T* __restrict__ V, const T* __restrict__ h
     for (int i = threadIdx.x - t0; i < n4; i += NT - t0) {
       const int64_t row = r0 + (int64_t)i * VT::W;
       typename VT::V a = *reinterpret_cast<const typename VT::V*>(x + row);
-      int k = 0;
-      for (; k + 4 <= cnt; k += 4) {
-        const typename VT::V v0 = *reinterpret_cast<const typename VT::V*>(V + (size_t)k * N + row);
-        const typename VT::V v1 = *reinterpret_cast<const typename VT::V*>(V + (size_t)(k + 1) * N + row);
-        const typename VT::V v2 = *reinterpret_cast<const typename VT::V*>(V + (size_t)(k + 2) * N + row);
-        const typename VT::V v3 = *reinterpret_cast<const typename VT::V*>(V + (size_t)(k + 3) * N + row);
-        a = VT::fma(v0, h[k], a);
-        a = VT::fma(v1, h[k + 1], a);
-        a = VT::fma(v2, h[k + 2], a);
-        a = VT::fma(v3, h[k + 3], a);
+      for (int k0 = 0; k0 < cnt; k0 += 4) {
+        typename VT::V v[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if (k0 + q < cnt) v[q] = *reinterpret_cast<const typename VT::V*>(V + (size_t)(k0 + q) * N + row);
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if (k0 + q < cnt) a = VT::fma(v[q], h[k0 + q], a);
       }
-      for (; k < cnt; ++k)
-        a = VT::fma(*reinterpret_cast<const typename VT::V*>(V + (size_t)k * N + row), h[k], a);
       *reinterpret_cast<typename VT::V*>(y + row) = VT::scale(a, s);
     }
   } else {
     for (int i = threadIdx.x - t0; i < nrow; i += NT - t0) {
       const int64_t row = r0 + i;
       T a = x[row];
-      for (int k = 0; k < cnt; ++k) a -= V[(size_t)k * N + row] * h[k];
+      for (int k0 = 0; k0 < cnt; k0 += 8) {
+        T v[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+          if (k0 + q < cnt) v[q] = V[(size_t)(k0 + q) * N + row];
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+          if (k0 + q < cnt) a -= v[q] * h[k0 + q];
+      }
       y[row] = a * s;
     }
   }
@@ -240,6 +283,322 @@ __device__ void block_lincomb(const T* __restrict__ V, const T* __restrict__ y, 
     if (k < cnt) a0 += V[(size_t)k * N + row] * y[k];
     u[row] = a0 + a1;
   }
+}
+
+// W consecutive values of one row unit
+template <typename T, int W>
+struct Pack {
+  T v[W];
+};
+template <typename T, int W>
+__device__ __forceinline__ Pack<T, W> ldp(const T* p) {
+  Pack<T, W> r;
+  if constexpr (W == 4 && sizeof(T) == 4) {
+    const float4 q = *reinterpret_cast<const float4*>(p);
+    r.v[0] = q.x; r.v[1] = q.y; r.v[2] = q.z; r.v[3] = q.w;
+  } else if constexpr (W == 2 && sizeof(T) == 8) {
+    const double2 q = *reinterpret_cast<const double2*>(p);
+    r.v[0] = q.x; r.v[1] = q.y;
+  } else {
+#pragma unroll
+    for (int c = 0; c < W; ++c) r.v[c] = p[c];
+  }
+  return r;
+}
+template <typename T, int W>
+__device__ __forceinline__ void stp(T* p, const Pack<T, W>& r) {
+  if constexpr (W == 4 && sizeof(T) == 4) {
+    *reinterpret_cast<float4*>(p) = make_float4(r.v[0], r.v[1], r.v[2], r.v[3]);
+  } else if constexpr (W == 2 && sizeof(T) == 8) {
+    *reinterpret_cast<double2*>(p) = make_double2(r.v[0], r.v[1]);
+  } else {
+#pragma unroll
+    for (int c = 0; c < W; ++c) p[c] = r.v[c];
+  }
+}
+
+// Sum of v[k] over the 32 lanes for each of the KC slots, as a transposed
+// butterfly (KC - 1 shuffles for KC = 32): afterwards lane l holds the sum
+// of slot l * KC / 32 (lanes 2i and 2i+1 both hold slot i when KC = 16).
+template <typename T, int KC>
+__device__ __forceinline__ void transpose_reduce(T (&v)[KC], int lane) {
+  int o = 16;
+#pragma unroll
+  for (int c = KC; c > 1; c >>= 1, o >>= 1) {
+    const bool up = (lane & o) != 0;
+#pragma unroll
+    for (int i = 0; i < c / 2; ++i) {
+      const T send = up ? v[i] : v[i + c / 2];
+      const T keep = up ? v[i + c / 2] : v[i];
+      v[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+    }
+  }
+#pragma unroll
+  for (; o > 0; o >>= 1) v[0] += __shfl_xor_sync(0xffffffffu, v[0], o);
+}
+
+// Partial sums of the block's rows for one Gram-Schmidt reduction:
+// pb[k] = V_k . w for k < cnt and pb[cnt] = w . w.  With `gather`, w is
+// formed first from the pushed coupling products, w = v_j + the products of
+// the faces holding the row's node, and written to a.w.  Each thread owns
+// whole row units (W consecutive values) and keeps the sums of all slots in
+// registers, so the loads of every basis vector of its rows are in flight
+// together; lanes are combined by a transposed butterfly and warps through
+// shared memory, always in the same order.
+template <int DIM, typename T, int W>
+__device__ void gs_dots_w(const CoopArgs<T>& a, const T* __restrict__ vj, bool gather, int cnt, int64_t r0,
+                          int nrow, int e0, const int* __restrict__ sSpos, const int* __restrict__ sFside,
+                          T* __restrict__ sRed, T* __restrict__ pb) {
+  constexpr int NV = DIM + 2;
+  constexpr int KC = 16;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nu = nrow / W, n = a.n, F = a.F, Np = a.md.Np, nb = a.nb;
+  const int64_t N = a.N;
+  T accw = T(0);
+  for (int k0 = 0; k0 == 0 || k0 < cnt; k0 += KC) {
+    const int nk = min(KC, cnt - k0);
+    T acc[KC];
+#pragma unroll
+    for (int k = 0; k < KC; ++k) acc[k] = T(0);
+    for (int i = threadIdx.x; i < nu; i += NT) {
+      const int64_t row = r0 + (int64_t)i * W;
+      Pack<T, W> wv;
+      if (gather && k0 == 0) {
+        const int rb = i * W;  // row within the block
+        const int le = rb / n, r = rb - le * n;
+        wv = ldp<T, W>(vj + row);
+        const int fbase = a.rc.fside_smem ? le * F : (e0 + le) * F;
+        const int* fsd = a.rc.fside_smem ? sFside : a.fside;
+        if (NV % W == 0) {
+          // the unit lies inside one node: one W-wide load per face
+          const int jn = r / NV, av = r - jn * NV;
+          for (int f = 0; f < F; ++f) {
+            const int sp = sSpos[f * Np + jn];
+            if (sp < 0) continue;
+            const int fs = fsd[fbase + f];
+            if (fs < 0) continue;
+            const Pack<T, W> c = ldp<T, W>(a.cfs + (size_t)fs * nb + sp * NV + av);
+#pragma unroll
+            for (int q = 0; q < W; ++q) wv.v[q] += c.v[q];
+          }
+        } else {
+#pragma unroll
+          for (int q = 0; q < W; ++q) {
+            const int rq = r + q;
+            const int lq = le + rq / n, rr = rq - (rq / n) * n;
+            const int jn = rr / NV, av = rr - jn * NV;
+            const int fb = a.rc.fside_smem ? lq * F : (e0 + lq) * F;
+            for (int f = 0; f < F; ++f) {
+              const int sp = sSpos[f * Np + jn];
+              if (sp < 0) continue;
+              const int fs = fsd[fb + f];
+              if (fs >= 0) wv.v[q] += a.cfs[(size_t)fs * nb + sp * NV + av];
+            }
+          }
+        }
+        stp<T, W>(a.w + row, wv);
+      } else {
+        wv = ldp<T, W>(a.w + row);
+      }
+      if (k0 == 0) {
+#pragma unroll
+        for (int q = 0; q < W; ++q) accw += wv.v[q] * wv.v[q];
+      }
+      // basis loads in batches of 4 (in flight together), then their dots
+#pragma unroll
+      for (int kb = 0; kb < KC; kb += 4) {
+        if (kb < nk) {
+          Pack<T, W> v[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+            if (kb + q < nk) v[q] = ldp<T, W>(a.V + (size_t)(k0 + kb + q) * N + row);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            if (kb + q < nk) {
+              T d = T(0);
+#pragma unroll
+              for (int c = 0; c < W; ++c) d += v[q].v[c] * wv.v[c];
+              acc[kb + q] += d;
+            }
+          }
+        }
+      }
+    }
+    transpose_reduce<T, KC>(acc, lane);
+    if (KC == 32) sRed[warp * 33 + lane] = acc[0];
+    else if ((lane & 1) == 0) sRed[warp * 33 + (lane >> 1)] = acc[0];
+    if (k0 == 0) {
+      const T ww = wsum(accw);
+      if (lane == 0) sRed[warp * 33 + 32] = ww;
+    }
+    __syncthreads();
+    if (threadIdx.x < nk) {
+      T v = T(0);
+      for (int q = 0; q < NW; ++q) v += sRed[q * 33 + threadIdx.x];
+      pb[k0 + threadIdx.x] = v;
+    }
+    if (k0 == 0 && threadIdx.x == 32) {
+      T v = T(0);
+      for (int q = 0; q < NW; ++q) v += sRed[q * 33 + 32];
+      pb[cnt] = v;
+    }
+    __syncthreads();
+  }
+}
+
+template <int DIM, typename T>
+__device__ void gs_dots(const CoopArgs<T>& a, const T* __restrict__ vj, bool gather, int cnt, int64_t r0,
+                        int nrow, int e0, bool vec, const int* __restrict__ sSpos,
+                        const int* __restrict__ sFside, T* __restrict__ sRed, T* __restrict__ pb) {
+  if (vec)
+    gs_dots_w<DIM, T, Vec<T>::W>(a, vj, gather, cnt, r0, nrow, e0, sSpos, sFside, sRed, pb);
+  else
+    gs_dots_w<DIM, T, 1>(a, vj, gather, cnt, r0, nrow, e0, sSpos, sFside, sRed, pb);
+}
+
+// ---- operator ring (see RingCfg) -----------------------------------------
+struct RingState {
+  uint32_t parity;  // phase of the group's slot barrier the next wait expects
+  int pending;      // a unit's copies were issued into the group's slot and not waited for
+  int failed;       // a wait of this thread gave up: no further waits
+};
+
+// one thread: issue the copies of unit u into `slot`, armed on `bar`
+template <typename T>
+__device__ void ring_issue(const CoopArgs<T>& a, int u, int e0, int e1, unsigned char* slot, uint64_t* bar,
+                           const int* __restrict__ sFside) {
+  const RingCfg& rc = a.rc;
+  const int n = a.n, F = a.F;
+  const int c0 = e0 + u * rc.eps, nl = min(rc.eps, e1 - c0);
+  const size_t nn = (size_t)n * n * sizeof(T);
+  const char* src = reinterpret_cast<const char*>(a.inv) + (size_t)c0 * nn;
+  const size_t delta = reinterpret_cast<uintptr_t>(src) & 15;
+  // a 16-byte aligned range around the unit's inverse blocks (the inverse
+  // array is allocated with room for the rounded end)
+  const uint32_t binv = (uint32_t)((delta + (size_t)nl * nn + 15) & ~size_t(15));
+  uint32_t total = binv;
+  if (rc.cpl_tma) {
+    for (int le = 0; le < nl; ++le)
+      for (int f = 0; f < F; ++f) {
+        const int fs = rc.fside_smem ? sFside[(c0 - e0 + le) * F + f] : a.fside[(size_t)(c0 + le) * F + f];
+        if (fs >= 0) total += (uint32_t)rc.cpl_bytes;
+      }
+  }
+  mbar_arrive_expect_tx(bar, total);
+  bulk_g2s(slot, src - delta, binv, bar);
+  if (rc.cpl_tma) {
+    const char* cb = reinterpret_cast<const char*>(a.cpl);
+    for (int le = 0; le < nl; ++le)
+      for (int f = 0; f < F; ++f) {
+        const int fs = rc.fside_smem ? sFside[(c0 - e0 + le) * F + f] : a.fside[(size_t)(c0 + le) * F + f];
+        if (fs < 0) continue;
+        bulk_g2s(slot + rc.inv_cap + (size_t)(le * F + f) * rc.cpl_bytes,
+                 cb + (size_t)(fs ^ 1) * rc.cpl_bytes, (uint32_t)rc.cpl_bytes, bar);
+      }
+  }
+}
+
+// The Arnoldi operator apply of iteration j through the ring: for every
+// unit of the block, z = D^-1 v_j per element (inverse blocks from the slot,
+// v from the unit's own rows staged in shared memory), then the push of the
+// coupling products C z to the neighbours' face sides (cfs).
+template <int DIM, int NB, typename T>
+__device__ void ring_apply_push(const CoopArgs<T>& a, const T* __restrict__ vj, int e0, int e1,
+                                unsigned char* dsm, const int* __restrict__ sPerm,
+                                const int* __restrict__ sFside, RingState& rs) {
+  constexpr int NV = DIM + 2;
+  const RingCfg& rc = a.rc;
+  const int n = NB > 0 ? NB : a.n;
+  const int F = a.F, S = a.S, nb = a.nb;
+  const int g = (threadIdx.x >> 5) / rc.wpg;
+  const int nunits = (e1 - e0 + rc.eps - 1) / rc.eps;
+  if (g >= rc.nstage || g >= nunits) return;
+  const int GT = rc.wpg * 32, gt = threadIdx.x - g * GT;
+  unsigned char* slot = dsm + rc.off_ring + (size_t)g * rc.slot_bytes;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(dsm + rc.off_bar) + g;
+  T* zb = reinterpret_cast<T*>(dsm + rc.off_z) + (size_t)g * rc.eps * n;
+  T* vb = reinterpret_cast<T*>(dsm + rc.off_v) + (size_t)g * rc.eps * n;
+  if (!rs.pending && gt == 0) ring_issue<T>(a, g, e0, e1, slot, bar, sFside);
+  for (int u = g; u < nunits; u += rc.nstage) {
+    const int c0 = e0 + u * rc.eps, nl = min(rc.eps, e1 - c0);
+    for (int t = gt; t < nl * n; t += GT) vb[t] = vj[(size_t)c0 * n + t];
+    // after a wait that gave up, the group stops waiting (its results are
+    // void and the host reports EG_ERR_TIMEOUT)
+    if (!rs.failed && !mbar_wait(bar, rs.parity)) {
+      rs.failed = 1;
+      atomicOr(a.flags + F_TMO, 1);
+    }
+    rs.parity ^= 1u;
+    named_sync(1 + g, GT);
+    const T* inv = reinterpret_cast<const T*>(slot + (((size_t)c0 * n * n * sizeof(T)) & 15));
+    for (int t = gt; t < nl * n; t += GT) {
+      const int le = t / n, r = t - le * n;
+      zb[t] = block_row<NB, T>(inv + (size_t)le * n * n, vb + (size_t)le * n, r, n);
+    }
+    named_sync(1 + g, GT);
+    // push: row i of the neighbour's coupling block on face f of element le
+    const int nitem = nl * F * nb;
+    for (int it = gt; it < nitem; it += GT) {
+      const int le = it / (F * nb), rem = it - le * (F * nb);
+      const int f = rem / nb, i = rem - f * nb;
+      const int fs = rc.fside_smem ? sFside[(c0 - e0 + le) * F + f] : a.fside[(size_t)(c0 + le) * F + f];
+      if (fs < 0) continue;
+      const int tgt = fs ^ 1;
+      const T* zs = zb + (size_t)le * n;
+      const int* pf = sPerm + f * S;
+      T acc = T(0);
+      if (a.md.sparse_face) {
+        const int o = a.md.ifaces[5 * (tgt >> 1) + 4];
+        const int* facing = (tgt & 1) ? a.md.nbrinv + o * a.md.Nf : a.md.nbrperm + o * a.md.Nf;
+        const T* Cr = a.cpl + (size_t)tgt * nb * NV + (size_t)i * NV;
+        const T* zz = zs + pf[facing[i / NV]] * NV;
+        T c[NV];
+        load_row_piece<NV, T>(Cr, c);
+#pragma unroll
+        for (int b = 0; b < NV; ++b) acc += c[b] * zz[b];
+      } else if (rc.cpl_tma) {
+        const T* Cr = reinterpret_cast<const T*>(slot + rc.inv_cap + (size_t)(le * F + f) * rc.cpl_bytes) +
+                      (size_t)i * nb;
+        for (int sp = 0; sp < S; ++sp) {
+          const T* zz = zs + pf[sp] * NV;
+#pragma unroll
+          for (int b = 0; b < NV; ++b) acc += Cr[sp * NV + b] * zz[b];
+        }
+      } else {
+        const T* Cr = a.cpl + ((size_t)tgt * nb + i) * nb;
+        for (int sp = 0; sp < S; ++sp) {
+          T c[NV];
+          load_row_piece<NV, T>(Cr + sp * NV, c);
+          const T* zz = zs + pf[sp] * NV;
+#pragma unroll
+          for (int b = 0; b < NV; ++b) acc += c[b] * zz[b];
+        }
+      }
+      a.cfs[(size_t)tgt * nb + i] = acc;
+    }
+    named_sync(1 + g, GT);
+    if (gt == 0) {
+      // the next unit of this group, or (after the last) its first unit for
+      // the next Arnoldi iteration
+      const int nx = u + rc.nstage < nunits ? u + rc.nstage : g;
+      fence_proxy_async_smem();
+      ring_issue<T>(a, nx, e0, e1, slot, bar, sFside);
+    }
+  }
+  rs.pending = 1;
+}
+
+// before the block exits: wait (bounded) for the copies still in flight into
+// the group's slot
+template <typename T>
+__device__ void ring_drain(const CoopArgs<T>& a, unsigned char* dsm, RingState& rs) {
+  if (!a.rc.on || !rs.pending || rs.failed) return;
+  const int g = (threadIdx.x >> 5) / a.rc.wpg;
+  if (g >= a.rc.nstage) return;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(dsm + a.rc.off_bar) + g;
+  if (!mbar_wait(bar, rs.parity)) atomicOr(a.flags + F_TMO, 1);
+  rs.parity ^= 1u;
+  rs.pending = 0;
 }
 
 // Element block times a vector held per element (z_e = A_e x_e) for a chunk
@@ -318,8 +677,8 @@ struct GridBarrier {
 // the reorthogonalisation test, the convergence decision) are bit-identical
 // in every block and all blocks take the same branches.
 template <int DIM, int NB, typename T, class Bar>
-__device__ void gmres_body(const CoopArgs<T>& a, const int b, const int nblk, Bar& grid,
-                           GmresShared<T>& sm) {
+__device__ void gmres_solve(const CoopArgs<T>& a, const int b, const int nblk, Bar& grid,
+                            GmresShared<T>& sm, RingState& rs) {
   constexpr int NV = DIM + 2;
   const int tid = threadIdx.x;
   const int n = NB > 0 ? NB : a.n, m = a.m, M1 = a.m + 1;
@@ -331,8 +690,10 @@ __device__ void gmres_body(const CoopArgs<T>& a, const int b, const int nblk, Ba
   const bool vec = NB > 0 ? (NB % Vec<T>::W) == 0 : (a.n % Vec<T>::W) == 0;
   T* P0 = a.part;                               // first pass: dots and w.w
   T* P2 = a.part + 2 * (size_t)nblk * PSTRIDE;  // second pass: dots and w'.w'
-  extern __shared__ __align__(16) unsigned char dsmem[];
-  T* sZ = reinterpret_cast<T*>(dsmem);  // [ec][n] per-element values of a chunk
+  extern __shared__ __align__(128) unsigned char dsmem[];
+  T* sZ = reinterpret_cast<T*>(dsmem + a.rc.off_sz);  // [ec][n] per-element values of a chunk
+  T* sRed = reinterpret_cast<T*>(dsmem + a.rc.off_red);  // [NW][33] cross-warp sums
+  int* sFside = reinterpret_cast<int*>(dsmem + a.rc.off_fside);  // [epb][F] when staged
   int* sPerm = sm.sPerm;
   int* sSpos = sm.sSpos;
   T* sh1 = sm.sh1;
@@ -355,6 +716,13 @@ __device__ void gmres_body(const CoopArgs<T>& a, const int b, const int nblk, Ba
   double& s_tol = sm.s_tol;
   double& s_bnorm = sm.s_bnorm;
   for (int k = tid; k < a.F * a.S; k += NT) sPerm[k] = a.md.perm[k];
+  if (a.rc.fside_smem)
+    for (int k = tid; k < (e1 - e0) * a.F; k += NT) sFside[k] = a.fside[(size_t)e0 * a.F + k];
+  if (a.rc.on && tid == 0) {
+    uint64_t* bars = reinterpret_cast<uint64_t*>(dsmem + a.rc.off_bar);
+    for (int g = 0; g < a.rc.nstage; ++g) mbar_init(bars + g, 1);
+    fence_mbar_init();
+  }
   for (int k = tid; k < a.F * a.md.Np; k += NT) sSpos[k] = a.spos[k];
   // |b|
   block_dots<T>(a.V, a.bvec, 0, 1, N, r0, nrow, vec, P0 + (size_t)b * PSTRIDE);
@@ -414,30 +782,20 @@ __device__ void gmres_body(const CoopArgs<T>& a, const int b, const int nblk, Ba
       if (s_done) break;
       const T* vj = a.V + (size_t)j * N;
       T* vn = a.V + (size_t)(j + 1) * N;
-      // (1) per chunk: z = D^-1 v_j (shared memory), push C z to the neighbours
-      for (int c0 = e0; c0 < e1; c0 += a.ec) {
-        const int nl = min(a.ec, e1 - c0);
-        chunk_apply_push<DIM, NB, T>(a, a.inv, vj, true, sZ, sPerm, c0, nl, nullptr);
+      // (1) z = D^-1 v_j per element, push C z to the neighbours' face sides
+      if (a.rc.on) {
+        ring_apply_push<DIM, NB, T>(a, vj, e0, e1, dsmem, sPerm, sFside, rs);
+      } else {
+        for (int c0 = e0; c0 < e1; c0 += a.ec) {
+          const int nl = min(a.ec, e1 - c0);
+          chunk_apply_push<DIM, NB, T>(a, a.inv, vj, true, sZ, sPerm, c0, nl, nullptr);
+        }
       }
       if (!grid.sync()) return;
-      // (2) w = v_j + the pushed products of the faces holding the row's node
-      for (int t = tid; t < nrow; t += NT) {
-        const int le = t / n, r = t - le * n;
-        const int jn = r / NV, av = r - jn * NV;
-        const int e = e0 + le;
-        const int64_t row = (int64_t)e * n + r;
-        T acc = vj[row];
-        for (int f = 0; f < a.F; ++f) {
-          const int sp = sSpos[f * a.md.Np + jn];
-          if (sp < 0) continue;
-          const int fs = a.fside[(int64_t)e * a.F + f];
-          if (fs >= 0) acc += a.cfs[(size_t)fs * a.nb + sp * NV + av];
-        }
-        a.w[row] = acc;
-      }
-      __syncthreads();
-      // (3) first pass: h1 = V^T w and w.w in one reduction
-      block_dots<T>(a.V, a.w, j + 1, 1, N, r0, nrow, vec, P0 + (size_t)b * PSTRIDE);
+      // (2) w = v_j + the pushed products of the faces holding the row's
+      // node, and (3) the first pass h1 = V^T w with w.w, in one reduction
+      gs_dots<DIM, T>(a, vj, true, j + 1, r0, nrow, e0, vec, sSpos, sFside, sRed,
+                      P0 + (size_t)b * PSTRIDE);
       if (!grid.sync()) return;
       block_reduce_all<T>(P0, nblk, j + 2, sh1);
       __syncthreads();
@@ -454,7 +812,8 @@ __device__ void gmres_body(const CoopArgs<T>& a, const int b, const int nblk, Ba
         // (4) second pass on w' = w - V h1: h2 = V^T w' and w'.w' in one reduction
         block_sub_scale<T>(a.V, sh1, j + 1, N, a.w, T(1), a.w, r0, nrow, vec, 0);
         __syncthreads();
-        block_dots<T>(a.V, a.w, j + 1, 1, N, r0, nrow, vec, P2 + (size_t)b * PSTRIDE);
+        gs_dots<DIM, T>(a, vj, false, j + 1, r0, nrow, e0, vec, sSpos, sFside, sRed,
+                        P2 + (size_t)b * PSTRIDE);
         if (!grid.sync()) return;
         block_reduce_all<T>(P2, nblk, j + 2, sh2);
         __syncthreads();
@@ -543,6 +902,18 @@ __device__ void gmres_body(const CoopArgs<T>& a, const int b, const int nblk, Ba
   }
 }
 
+// The solve, then (on every way out, including a failed barrier of a batched
+// launch) a bounded wait for the operator copies still in flight into the
+// block's shared memory.
+template <int DIM, int NB, typename T, class Bar>
+__device__ void gmres_body(const CoopArgs<T>& a, const int b, const int nblk, Bar& grid,
+                           GmresShared<T>& sm) {
+  extern __shared__ __align__(128) unsigned char dsmem[];
+  RingState rs{0u, 0, 0};
+  gmres_solve<DIM, NB, T, Bar>(a, b, nblk, grid, sm, rs);
+  ring_drain<T>(a, dsmem, rs);
+}
+
 // kernel arguments of a solver's GMRES solve (chunk size a->ec set by the
 // launcher, which knows the grid)
 template <typename T>
@@ -572,6 +943,67 @@ void coop_args(const eg_ls* ls, CoopArgs<T>* out) {
   a.E = m->E;
   a.N = m->ndof;
   a.ec = 1;
+}
+
+inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Dynamic shared-memory layout of a solve on nblk blocks: the operator ring
+// (2-D dense coupling, or 3-D face-diagonal coupling, when at least two slots
+// fit), the cross-warp sums, the block's face-side table when it fits, and
+// the chunk buffer of the residual and update passes.  Sets a->rc and a->ec;
+// returns the bytes.
+template <typename T>
+size_t coop_layout(CoopArgs<T>* a, int dim, int nblk) {
+  RingCfg& rc = a->rc;
+  rc = RingCfg{};
+  const int n = a->n, nb = a->nb, F = a->F;
+  const int epb = std::max(1, (a->E + nblk - 1) / nblk);
+  const size_t es = sizeof(T);
+  const size_t nn = (size_t)n * n * es, cb = (size_t)nb * nb * es;
+  const bool sparse = a->md.sparse_face != 0;
+  const bool ring_ok = dim == 2 ? !sparse : sparse;
+  const int cpl_tma = (dim == 2 && !sparse && cb % 16 == 0) ? 1 : 0;
+  const size_t per_el = nn + (cpl_tma ? (size_t)F * cb : 0);
+  int eps = (int)std::max<size_t>(1, std::min<size_t>(16, kSlotTarget / per_el));
+  eps = std::min(eps, epb);
+  // room for the 16-byte rounding at both ends of the unit's inverse range
+  const size_t inv_cap = align_up((size_t)eps * nn + 32, 16);
+  const size_t slot = align_up(inv_cap + (cpl_tma ? (size_t)eps * F * cb : 0), 128);
+  const int nunits = (epb + eps - 1) / eps;
+  const int nstage = (int)std::min<size_t>(std::min<size_t>(8, kRingBudget / slot), (size_t)nunits);
+  size_t off = 0;
+  if (ring_ok && nstage >= 2) {
+    rc.on = 1;
+    rc.nstage = nstage;
+    rc.eps = eps;
+    rc.wpg = NW / nstage;
+    rc.cpl_tma = cpl_tma;
+    rc.slot_bytes = (int)slot;
+    rc.inv_cap = (int)inv_cap;
+    rc.cpl_bytes = (int)cb;
+    rc.off_ring = 0;
+    off = (size_t)nstage * slot;
+    rc.off_bar = (int)off;
+    off += align_up((size_t)nstage * 8, 16);
+    rc.off_z = (int)off;
+    off += align_up((size_t)nstage * eps * n * es, 16);
+    rc.off_v = (int)off;
+    off += align_up((size_t)nstage * eps * n * es, 16);
+  }
+  rc.off_red = (int)off;
+  off += align_up((size_t)NW * 33 * es, 16);
+  const size_t fs_bytes = align_up((size_t)epb * F * sizeof(int), 16);
+  if (fs_bytes <= 16 * 1024 && off + fs_bytes + (size_t)n * es <= kSmemMax) {
+    rc.fside_smem = 1;
+    rc.off_fside = (int)off;
+    off += fs_bytes;
+  }
+  rc.off_sz = (int)off;
+  const size_t room = std::min<size_t>(kSmemMax - off, 40 * 1024);
+  int ec = (int)(room / ((size_t)n * es));
+  ec = std::max(1, std::min(ec, epb));
+  a->ec = ec;
+  return off + (size_t)ec * n * es;
 }
 
 template <int DIM, int NB, typename T>

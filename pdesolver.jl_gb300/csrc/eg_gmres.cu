@@ -469,7 +469,10 @@ void enqueue_init(eg_ls* ls, int first) {
   const T* b = (const T*)ls->bT;
   const T* x = (const T*)ls->xT;
   if (first) norm_T<T>(ls, b, bnorm, nullptr);
-  eg_lo_apply_T(ls->lo, x, w);
+  if (ls->trans)
+    eg_lo_apply_t_T(ls->lo, x, w);
+  else
+    eg_lo_apply_T(ls->lo, x, w);
   k_gm_bminus<T><<<gridN(N), 256, 0, m->stream>>>(b, w, N);
   norm_T<T>(ls, w, beta, nullptr);
   k_gm_init<T><<<1, 32, 0, m->stream>>>(beta, bnorm, first, ls->m, ls->dH, ls->dflags, ls->dscal);
@@ -533,9 +536,15 @@ void enqueue_arnoldi(eg_ls* ls) {
   for (int j = 0; j < mm; ++j) {
     T* vj = V + (size_t)j * N;
     // w = J M^-1 v_j = v_j + C (D^-1 v_j): the element blocks cancel with
-    // their inverses, so only the coupling blocks are read here
-    eg_pc_apply_T(ls->pc, vj, z, fl);
-    eg_cpl_apply_T(ls->lo, vj, z, w, fl);
+    // their inverses, so only the coupling blocks are read here (transposed:
+    // w = J^T M^-T v_j = v_j + C^T (D^-T v_j))
+    if (ls->trans) {
+      eg_pc_apply_t_T(ls->pc, vj, z, fl);
+      eg_cpl_apply_t_T(ls->lo, vj, z, w, fl);
+    } else {
+      eg_pc_apply_T(ls->pc, vj, z, fl);
+      eg_cpl_apply_T(ls->lo, vj, z, w, fl);
+    }
     // classical Gram-Schmidt (with |w|^2 before, for the DGKS test), a second
     // pass only when the test asks, Givens on the device
     T* ww = hn + 3;  // slots hn+1, hn+2 hold beta and |b| (enqueue_init)
@@ -560,7 +569,10 @@ void enqueue_tail(eg_ls* ls) {
   k_gm_lsq<<<1, 256, 0, m->stream>>>(mm, ls->dH, ls->dflags);
   k_gm_Vy<T><<<gridN(N), 256, 0, m->stream>>>(V, ls->dH + (size_t)(mm + 1) * mm + 3 * mm + 1, N, w,
                                               ls->dflags);
-  eg_pc_apply_T(ls->pc, w, z);
+  if (ls->trans)
+    eg_pc_apply_t_T(ls->pc, w, z);
+  else
+    eg_pc_apply_T(ls->pc, w, z);
   k_gm_add<T><<<gridN(N), 256, 0, m->stream>>>(z, (T*)ls->xT, N);
   enqueue_init<T>(ls, 0);
 }
@@ -604,14 +616,15 @@ bool capture(eg_mesh* m, F fn, cudaGraphExec_t* exec, int64_t* nodes) {
 }
 
 template <typename T>
-int gmres_T(eg_ls* ls, eg_ls_stats* st) {
+int gmres_T(eg_ls* ls, eg_ls_stats* st, int transpose) {
   eg_mesh* m = ls->lo->mesh;
+  ls->trans = transpose ? 1 : 0;
   // tolerances into device memory (graphs read them there)
   double sc[8] = {0, 0, 0, 0, ls->reltol, ls->abstol, 0, 0};
   int fl[8] = {0, 0, 0, 0, ls->itermax, 0, 0, 0};
   EG_CUDA(cudaMemcpyAsync(ls->dscal, sc, sizeof(sc), cudaMemcpyHostToDevice, m->stream));
   EG_CUDA(cudaMemcpyAsync(ls->dflags, fl, sizeof(fl), cudaMemcpyHostToDevice, m->stream));
-  const bool coop = eg_coop_usable(ls) && !m->capturing;
+  const bool coop = !transpose && eg_coop_usable(ls) && !m->capturing;
   if (coop) {
     // the whole solve in one persistent launch
     const int rc = eg_gmres_coop(ls);
@@ -623,6 +636,10 @@ int gmres_T(eg_ls* ls, eg_ls_stats* st) {
     EG_CUDA(cudaStreamSynchronize(m->stream));
     std::memcpy(scal, ls->hh, sizeof(scal));
     std::memcpy(flags, ls->hh + 8, sizeof(flags));
+    if (flags[F_TMO]) {
+      eg_set_error("GMRES: a bounded wait on the operator copies gave up");
+      return EG_ERR_TIMEOUT;
+    }
     if (!std::isfinite(scal[S_BETA])) {
       eg_set_error("GMRES: non-finite residual");
       return EG_ERR_NONFINITE;
@@ -636,23 +653,29 @@ int gmres_T(eg_ls* ls, eg_ls_stats* st) {
     }
     return EG_OK;
   }
-  if (!ls->g_init && !ls->g_cycle && !ls->graphs_ok) {
+  // the graphs of this mode (forward or transposed), captured on first use
+  void*& g_init = transpose ? ls->g_init_t : ls->g_init;
+  void*& g_cycle = transpose ? ls->g_cycle_t : ls->g_cycle;
+  int64_t& init_nodes = transpose ? ls->g_init_t_nodes : ls->g_init_nodes;
+  int64_t& cycle_nodes = transpose ? ls->g_cycle_t_nodes : ls->g_cycle_nodes;
+  bool& graphs_ok = transpose ? ls->graphs_t_ok : ls->graphs_ok;
+  if (!g_init && !g_cycle && !graphs_ok) {
     cudaGraphExec_t gi = nullptr, gc = nullptr;
-    bool ok = capture(m, [&]() { enqueue_init<T>(ls, 1); }, &gi, &ls->g_init_nodes);
-    ok = ok && capture(m, [&]() { enqueue_cycle<T>(ls); }, &gc, &ls->g_cycle_nodes);
+    bool ok = capture(m, [&]() { enqueue_init<T>(ls, 1); }, &gi, &init_nodes);
+    ok = ok && capture(m, [&]() { enqueue_cycle<T>(ls); }, &gc, &cycle_nodes);
     if (ok) {
-      ls->g_init = (void*)gi;
-      ls->g_cycle = (void*)gc;
-      ls->graphs_ok = true;
+      g_init = (void*)gi;
+      g_cycle = (void*)gc;
+      graphs_ok = true;
     } else {
       if (gi) cudaGraphExecDestroy(gi);
       if (gc) cudaGraphExecDestroy(gc);
     }
   }
   auto run_init = [&]() -> int {
-    if (ls->graphs_ok) {
-      EG_CUDA(cudaGraphLaunch((cudaGraphExec_t)ls->g_init, m->stream));
-      m->launches += ls->g_init_nodes;
+    if (graphs_ok) {
+      EG_CUDA(cudaGraphLaunch((cudaGraphExec_t)g_init, m->stream));
+      m->launches += init_nodes;
     } else {
       enqueue_init<T>(ls, 1);
       m->launches += 8;
@@ -660,9 +683,9 @@ int gmres_T(eg_ls* ls, eg_ls_stats* st) {
     return EG_OK;
   };
   auto run_cycle = [&]() -> int {
-    if (ls->graphs_ok) {
-      EG_CUDA(cudaGraphLaunch((cudaGraphExec_t)ls->g_cycle, m->stream));
-      m->launches += ls->g_cycle_nodes;
+    if (graphs_ok) {
+      EG_CUDA(cudaGraphLaunch((cudaGraphExec_t)g_cycle, m->stream));
+      m->launches += cycle_nodes;
     } else {
       enqueue_cycle<T>(ls);
       m->launches += 12 * ls->m + 12;
@@ -709,14 +732,18 @@ void eg_gmres_release(eg_ls* ls) {
   if (ls->g_cycle) cudaGraphExecDestroy((cudaGraphExec_t)ls->g_cycle);
   ls->g_init = ls->g_cycle = nullptr;
   ls->graphs_ok = false;
+  if (ls->g_init_t) cudaGraphExecDestroy((cudaGraphExec_t)ls->g_init_t);
+  if (ls->g_cycle_t) cudaGraphExecDestroy((cudaGraphExec_t)ls->g_cycle_t);
+  ls->g_init_t = ls->g_cycle_t = nullptr;
+  ls->graphs_t_ok = false;
 }
 
 // x_T <- GMRES(J, b_T) from the initial guess in x_T; the graphs are bound to
 // ls->bT / ls->xT, so callers stage their vectors there.
-int eg_gmres_T(eg_ls* ls, const void* bT, void* xT, eg_ls_stats* st) {
+int eg_gmres_T(eg_ls* ls, const void* bT, void* xT, eg_ls_stats* st, int transpose) {
   if (bT != ls->bT || xT != ls->xT) {
     eg_set_error("GMRES: right-hand side and solution must be the solver's staging vectors");
     return EG_ERR_INVALID;
   }
-  return ls->lo->prec == EG_F64 ? gmres_T<double>(ls, st) : gmres_T<float>(ls, st);
+  return ls->lo->prec == EG_F64 ? gmres_T<double>(ls, st, transpose) : gmres_T<float>(ls, st, transpose);
 }

@@ -46,6 +46,7 @@ __global__ void k_face_jac(DevMesh md, const double* __restrict__ q, T* __restri
   for (int c = 0; c < NV; ++c) { qLr[c] = T(0); qRr[c] = T(0); }
   T nrm[DIM];
   const bool interior = slot < md.I;
+  const bool wall = !interior && md.bc_of_b[slot - md.I] == EG_BC_NOPENETRATION_ES;
   if (interior) {
     const int* itf = md.ifaces + 5 * slot;
     const int eL = itf[0], eR = itf[1], fL = itf[2], fR = itf[3], o = itf[4];
@@ -87,7 +88,10 @@ __global__ void k_face_jac(DevMesh md, const double* __restrict__ q, T* __restri
     qL[c].d[c] = T(1);
     if (interior) qR[c].d[NV + c] = T(1);
   }
-  if (!interior || md.face_flux == EG_FLUX_ROE) {
+  if (wall) {
+    // the mirror state depends on q: its derivative runs through the flux
+    eg::wall_es_flux<DIM>(g, qL, nrm, fl);
+  } else if (!interior || md.face_flux == EG_FLUX_ROE) {
     eg::roe_flux<DIM>(g, qL, qR, nrm, fl);
   } else {
     auto av = eg::ir_average<DIM>(g, qL, qR);

@@ -19,6 +19,7 @@ struct DevMesh {
   const int* bfaces;      // [B][2]
   const double* nrm_bndry;// [B][Nf][dim]
   const double* qg_bndry; // [B][Nf][nv]
+  const int* bc_of_b;     // [B] boundary condition (eg_bc) of each boundary face
   const EFace* eface;     // [E][F]
   const double* Minv;     // [E][Np]
   const double* w;        // [Np]

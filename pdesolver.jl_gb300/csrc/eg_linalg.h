@@ -60,6 +60,13 @@ struct eg_ls {
   void* g_cycle;   // cudaGraphExec_t: one restart cycle + update + re-initialisation
   int64_t g_init_nodes, g_cycle_nodes;
   bool graphs_ok;  // capture succeeded (else the same launches run eagerly)
+  // transposed solves (linearSolveTranspose): the same cycle on J^T M^-T,
+  // with graphs of its own
+  int trans;       // the enqueue functions build the transposed cycle
+  void* g_init_t;
+  void* g_cycle_t;
+  int64_t g_init_t_nodes, g_cycle_t_nodes;
+  bool graphs_t_ok, graphs_t_tried;
   // batched persistent GMRES: the solve's kernel arguments (device copy and
   // pinned staging) and the event marking them ready on the mesh stream
   void* dargs;
@@ -68,7 +75,8 @@ struct eg_ls {
 };
 void eg_gmres_release(eg_ls* ls);
 // slots of the device GMRES state: dflags[] and dscal[]
-enum { F_DONE = 0, F_JDONE = 1, F_ITS = 2, F_CONV = 3, F_ITERMAX = 4, F_REORTH = 5, F_CYCLES = 6 };
+// (F_TMO: a bounded wait of the persistent kernel on its operator copies gave up)
+enum { F_DONE = 0, F_JDONE = 1, F_ITS = 2, F_CONV = 3, F_ITERMAX = 4, F_REORTH = 5, F_CYCLES = 6, F_TMO = 7 };
 enum { S_TOL = 0, S_RESID = 1, S_BETA = 2, S_BNORM = 3, S_RELTOL = 4, S_ABSTOL = 5, S_BETA0 = 6 };
 // the whole GMRES solve as one persistent cooperative kernel (eg_arnoldi.cu)
 #define EG_COOP_MAX_BLOCKS 1024
@@ -112,8 +120,14 @@ size_t eg_lo_coupling_size(const eg_lo* lo);
 int eg_cpl_apply_T(eg_lo* lo, const void* v, const void* z, void* w, const int* done = nullptr);
 // y = M^-1 x in the operator precision
 int eg_pc_apply_T(eg_pc* pc, const void* x, void* y, const int* done = nullptr);
+// the transposes, in the operator precision: y = J^T x; w = v + C^T z (the
+// transposed right-preconditioned operator J^T M^-T v with z = M^-T v); y = M^-T x
+int eg_lo_apply_t_T(eg_lo* lo, const void* x, void* y, const int* done = nullptr);
+int eg_cpl_apply_t_T(eg_lo* lo, const void* v, const void* z, void* w, const int* done = nullptr);
+int eg_pc_apply_t_T(eg_pc* pc, const void* x, void* y, const int* done = nullptr);
 // precision conversion helpers (device)
 int eg_convert(eg_mesh* m, const double* src, void* dst, int prec, int64_t n, double scale);
 int eg_convert_back(eg_mesh* m, const void* src, double* dst, int prec, int64_t n);
-// x_T <- GMRES solution of J x = b_T; returns status, fills stats
-int eg_gmres_T(eg_ls* ls, const void* bT, void* xT, eg_ls_stats* st);
+// x_T <- GMRES solution of J x = b_T (or J^T x = b_T with `transpose`);
+// returns status, fills stats
+int eg_gmres_T(eg_ls* ls, const void* bT, void* xT, eg_ls_stats* st, int transpose = 0);

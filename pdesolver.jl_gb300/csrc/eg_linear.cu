@@ -336,27 +336,19 @@ int pcapply_T(eg_pc* pc, const T* x, T* y, const int* done = nullptr) {
 }
 
 // ------------------------------------------------------------ transposes
-// y = J^T x (applyLinearOperatorTranspose, LinearSolvers.jl:533; the PETSc
-// operator runs MatMultTranspose, lo_petscmat.jl:143-160), one thread per row
-// of y.  Row (e, j, a) of J^T is column (e, j, a) of J: column r of e's element
-// block, plus, for each interface face of e whose stencil holds node j, column
-// (s, a) of the neighbour's coupling block (the block whose rows are the
-// neighbour's stencil and whose columns are e's).
+// Coupling part of row (e, j, a) of J^T x: row (e, j, a) of J^T is column
+// (e, j, a) of J; for each interface face of e whose stencil holds node j it
+// takes column (s, a) of the neighbour's coupling block (the block whose rows
+// are the neighbour's stencil and whose columns are e's).
 template <int DIM, typename T>
-__global__ void k_spmv_t(DevMesh md, const T* __restrict__ diag, const T* __restrict__ cpl,
-                         const int* __restrict__ spos, const T* __restrict__ x, T* __restrict__ y,
-                         int n) {
+__device__ __forceinline__ T coupling_col(const DevMesh& md, const T* __restrict__ cpl,
+                                          const int* __restrict__ spos, const T* __restrict__ x, int e,
+                                          int r, int n) {
   constexpr int NV = DIM + 2;
   constexpr int F = DIM + 1;
-  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t >= (int64_t)md.E * n) return;
-  const int e = (int)(t / n), r = (int)(t - (int64_t)e * n);
-  const T* col = diag + ((size_t)e * n + r) * n;  // column r of the element block
-  const T* xe = x + (size_t)e * n;
-  T acc = T(0);
-  for (int i = 0; i < n; ++i) acc += col[i] * xe[i];
   const int Np = md.Np, S = md.S, nb = S * NV, Nf = md.Nf;
   const int j = r / NV, a = r - j * NV;
+  T acc = T(0);
   for (int f = 0; f < F; ++f) {
     const int s = spos[f * Np + j];
     if (s < 0) continue;
@@ -382,14 +374,48 @@ __global__ void k_spmv_t(DevMesh md, const T* __restrict__ diag, const T* __rest
       }
     }
   }
-  y[t] = acc;
+  return acc;
+}
+
+// y = J^T x (applyLinearOperatorTranspose, LinearSolvers.jl:533; the PETSc
+// operator runs MatMultTranspose, lo_petscmat.jl:143-160), one thread per row
+// of y: column r of e's element block, plus the coupling columns.  With
+// `done` non-null the launch does nothing while *done != 0.
+template <int DIM, typename T>
+__global__ void k_spmv_t(DevMesh md, const T* __restrict__ diag, const T* __restrict__ cpl,
+                         const int* __restrict__ spos, const T* __restrict__ x, T* __restrict__ y,
+                         int n, const int* __restrict__ done) {
+  if (done && *done) return;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= (int64_t)md.E * n) return;
+  const int e = (int)(t / n), r = (int)(t - (int64_t)e * n);
+  const T* col = diag + ((size_t)e * n + r) * n;  // column r of the element block
+  const T* xe = x + (size_t)e * n;
+  T acc = T(0);
+  for (int i = 0; i < n; ++i) acc += col[i] * xe[i];
+  y[t] = acc + coupling_col<DIM, T>(md, cpl, spos, x, e, r, n);
+}
+
+// w = v + C^T z: the transposed right-preconditioned operator
+// J^T M^-T v = (M^-1 J)^T v = v + C^T D^-T v with z = D^-T v (the element
+// blocks cancel with their inverses), coupling blocks only
+template <int DIM, typename T>
+__global__ void k_cpl_apply_t(DevMesh md, const T* __restrict__ cpl, const int* __restrict__ spos,
+                              const T* __restrict__ v, const T* __restrict__ z, T* __restrict__ w, int n,
+                              const int* __restrict__ done) {
+  if (done && *done) return;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= (int64_t)md.E * n) return;
+  const int e = (int)(t / n), r = (int)(t - (int64_t)e * n);
+  w[t] = v[t] + coupling_col<DIM, T>(md, cpl, spos, z, e, r, n);
 }
 
 // y = M^-T x (applyPCTranspose, LinearSolvers.jl:277): the transposed element
 // inverses, one thread per row
 template <typename T>
 __global__ void k_block_apply_t(const T* __restrict__ inv, const T* __restrict__ x, T* __restrict__ y,
-                                int E, int n) {
+                                int E, int n, const int* __restrict__ done) {
+  if (done && *done) return;
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= (int64_t)E * n) return;
   const int e = (int)(t / n), r = (int)(t - (int64_t)e * n);
@@ -401,19 +427,34 @@ __global__ void k_block_apply_t(const T* __restrict__ inv, const T* __restrict__
 }
 
 template <typename T>
-void launch_transpose(eg_lo* lo, const T* inv, const T* x, T* y) {
+void launch_transpose(eg_lo* lo, const T* inv, const T* x, T* y, const int* done = nullptr) {
   eg_mesh* m = lo->mesh;
   const int64_t rows = (int64_t)m->E * lo->n;
   const int blocks = (int)((rows + 255) / 256);
   eg_phase_begin(m, EG_PHASE_OTHER);
   if (inv)
-    k_block_apply_t<T><<<blocks, 256, 0, m->stream>>>(inv, x, y, m->E, lo->n);
+    k_block_apply_t<T><<<blocks, 256, 0, m->stream>>>(inv, x, y, m->E, lo->n, done);
   else if (m->dim == 2)
     k_spmv_t<2, T><<<blocks, 256, 0, m->stream>>>(dev_mesh(m), (const T*)lo->diag, (const T*)lo->cpl,
-                                                  lo->spos, x, y, lo->n);
+                                                  lo->spos, x, y, lo->n, done);
   else
     k_spmv_t<3, T><<<blocks, 256, 0, m->stream>>>(dev_mesh(m), (const T*)lo->diag, (const T*)lo->cpl,
-                                                  lo->spos, x, y, lo->n);
+                                                  lo->spos, x, y, lo->n, done);
+  eg_phase_end(m, EG_PHASE_OTHER, 1);
+}
+
+template <typename T>
+void launch_cpl_transpose(eg_lo* lo, const T* v, const T* z, T* w, const int* done) {
+  eg_mesh* m = lo->mesh;
+  const int64_t rows = (int64_t)m->E * lo->n;
+  const int blocks = (int)((rows + 255) / 256);
+  eg_phase_begin(m, EG_PHASE_OTHER);
+  if (m->dim == 2)
+    k_cpl_apply_t<2, T><<<blocks, 256, 0, m->stream>>>(dev_mesh(m), (const T*)lo->cpl, lo->spos, v, z, w,
+                                                       lo->n, done);
+  else
+    k_cpl_apply_t<3, T><<<blocks, 256, 0, m->stream>>>(dev_mesh(m), (const T*)lo->cpl, lo->spos, v, z, w,
+                                                       lo->n, done);
   eg_phase_end(m, EG_PHASE_OTHER, 1);
 }
 
@@ -636,6 +677,30 @@ int eg_pc_apply_T(eg_pc* pc, const void* x, void* y, const int* done) {
                                 : pcapply_T<float>(pc, (const float*)x, (float*)y, done);
 }
 
+int eg_lo_apply_t_T(eg_lo* lo, const void* x, void* y, const int* done) {
+  if (lo->prec == EG_F64)
+    launch_transpose<double>(lo, nullptr, (const double*)x, (double*)y, done);
+  else
+    launch_transpose<float>(lo, nullptr, (const float*)x, (float*)y, done);
+  return EG_OK;
+}
+
+int eg_cpl_apply_t_T(eg_lo* lo, const void* v, const void* z, void* w, const int* done) {
+  if (lo->prec == EG_F64)
+    launch_cpl_transpose<double>(lo, (const double*)v, (const double*)z, (double*)w, done);
+  else
+    launch_cpl_transpose<float>(lo, (const float*)v, (const float*)z, (float*)w, done);
+  return EG_OK;
+}
+
+int eg_pc_apply_t_T(eg_pc* pc, const void* x, void* y, const int* done) {
+  if (pc->lo->prec == EG_F64)
+    launch_transpose<double>(pc->lo, (const double*)pc->inv, (const double*)x, (double*)y, done);
+  else
+    launch_transpose<float>(pc->lo, (const float*)pc->inv, (const float*)x, (float*)y, done);
+  return EG_OK;
+}
+
 static void lo_free(eg_lo* lo) {
   if (!lo) return;
   void* bufs[] = {lo->diag, lo->cpl, lo->dF, lo->spos, lo->fside, lo->xT, lo->yT, lo->xd, lo->yd};
@@ -846,7 +911,9 @@ extern "C" int eg_pc_create(eg_lo* lo, eg_pc** out) {
   pc->lo = lo;
   pc->valid = false;
   const size_t es = lo->prec == EG_F64 ? 8 : 4;
-  cudaError_t e = cudaMalloc(&pc->inv, es * (size_t)lo->mesh->E * lo->n * lo->n);
+  // 256 bytes beyond the blocks: the persistent GMRES kernel copies the
+  // inverse blocks in 16-byte aligned ranges that may round past the last one
+  cudaError_t e = cudaMalloc(&pc->inv, es * (size_t)lo->mesh->E * lo->n * lo->n + 256);
   if (e != cudaSuccess) {
     delete pc;
     return eg_cuda_fail(e, "eg_pc_create");
@@ -989,9 +1056,10 @@ extern "C" int eg_ls_set_tolerances(eg_ls* ls, double reltol, double abstol, dou
   return EG_OK;
 }
 
-extern "C" int eg_ls_solve(eg_ls* ls, const double* b, double* x, int32_t mem, eg_ls_stats* stats) {
-  if (!ls || !b || !x || !ls->lo->valid || !ls->pc->valid) {
-    eg_set_error("eg_ls_solve: invalid argument or operator/preconditioner not computed");
+static int ls_solve(eg_ls* ls, const double* b, double* x, int32_t mem, eg_ls_stats* stats, int transpose) {
+  if (!ls || !b || !x || !ls->lo->valid || !ls->pc->valid || (mem != EG_MEM_HOST && mem != EG_MEM_DEVICE)) {
+    eg_set_error("%s: invalid argument or operator/preconditioner not computed",
+                 transpose ? "eg_ls_solve_transpose" : "eg_ls_solve");
     return EG_ERR_INVALID;
   }
   eg_mesh* m = ls->lo->mesh;
@@ -1006,13 +1074,22 @@ extern "C" int eg_ls_solve(eg_ls* ls, const double* b, double* x, int32_t mem, e
   }
   eg_convert(m, bd, ls->bT, ls->lo->prec, N, 1.0);
   eg_convert(m, xd, ls->xT, ls->lo->prec, N, 1.0);
-  int st = eg_gmres_T(ls, ls->bT, ls->xT, stats);
+  int st = eg_gmres_T(ls, ls->bT, ls->xT, stats, transpose);
   if (st != EG_OK) return st;
   eg_convert_back(m, ls->xT, xd, ls->lo->prec, N);
   EG_CUDA(cudaGetLastError());
   if (mem == EG_MEM_HOST) EG_CUDA(cudaMemcpyAsync(x, xd, 8 * N, cudaMemcpyDeviceToHost, m->stream));
   EG_CUDA(cudaStreamSynchronize(m->stream));
   return EG_OK;
+}
+
+extern "C" int eg_ls_solve(eg_ls* ls, const double* b, double* x, int32_t mem, eg_ls_stats* stats) {
+  return ls_solve(ls, b, x, mem, stats, 0);
+}
+
+extern "C" int eg_ls_solve_transpose(eg_ls* ls, const double* b, double* x, int32_t mem,
+                                     eg_ls_stats* stats) {
+  return ls_solve(ls, b, x, mem, stats, 1);
 }
 
 extern "C" int eg_lo_apply_native(eg_lo* lo, const void* x, void* y) {

@@ -20,6 +20,10 @@ void eg_set_error(const char* fmt, ...) {
 
 int eg_cuda_fail(cudaError_t e, const char* what) {
   eg_set_error("%s: %s", what, cudaGetErrorString(e));
+  // the error is reported through the status code: clear it from the
+  // thread's last-error slot (a launch-configuration error is not sticky and
+  // would otherwise surface in the caller's next, unrelated CUDA call)
+  cudaGetLastError();
   return e == cudaErrorMemoryAllocation ? EG_ERR_OOM : EG_ERR_CUDA;
 }
 
@@ -109,6 +113,8 @@ static void boundary_states(const DevParams& p, int dim, int B, int Nf, const in
       double* s = &qg[((size_t)b * Nf + i) * nv];
       if (bc_of_b[b] == EG_BC_VORTEX)
         vortex_state(p, coords_bndry + ((size_t)b * Nf + i) * dim, s);
+      else if (bc_of_b[b] == EG_BC_NOPENETRATION_ES)
+        for (int c = 0; c < nv; ++c) s[c] = 0.0;  // the wall's state follows q (no data)
       else
         freestream_state(p, dim, s);
     }
@@ -236,7 +242,7 @@ extern "C" int eg_mesh_create(const eg_mesh_desc* d, const eg_params* params, eg
   for (int g = 0; g <= m->nbc; ++g) m->h_bndry_offsets[g] = d->bndry_offsets[g];
   for (int g = 0; g < m->nbc; ++g) {
     int bct = d->bc_types[g];
-    if (bct != EG_BC_VORTEX && bct != EG_BC_FREESTREAM) {
+    if (bct != EG_BC_VORTEX && bct != EG_BC_FREESTREAM && bct != EG_BC_NOPENETRATION_ES) {
       eg_set_error("eg_mesh_create: unsupported boundary condition %d", bct);
       free_mesh(m);
       return EG_ERR_UNSUPPORTED;

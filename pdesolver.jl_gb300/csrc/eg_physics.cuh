@@ -247,6 +247,49 @@ __device__ __forceinline__ void roe_flux(const Gas& g, const T* q, const T* qg, 
   flux[NV - 1] = (q[NV - 1] + pL) * UL + lambda3 * dq[NV - 1] + c1 * H + c2 * Un;
 }
 
+// Entropy-stable no-penetration wall (reference noPenetrationESBC,
+// bc.jl:767-795): the mirror state qg = q with the normal momentum reversed,
+// m_g = m - 2 (m . n^) n^ (getDirichletState, bc.jl:860-919), and the
+// Lax-Friedrichs flux between q and qg (calcLFFlux, bc_solvers.jl:428-446):
+// F = (F(q).n + F(qg).n - lambda_max (qg - q)) / 2, lambda_max = |U_n| +
+// |n| a at the mean state (q + qg) / 2 (getLambdaMaxSimple, IR_stab.jl:
+// 310-326; getLambdaMax, euler_funcs.jl:1887-1910).  Scalar-generic: with a
+// derivative carrier q the derivative runs through qg as well.
+template <int DIM, typename T, typename Tn>
+__device__ __forceinline__ void wall_es_flux(const Gas& g, const T* q, const Tn* nrm, T* flux) {
+  using R = typename RealOf<T>::type;
+  constexpr int NV = DIM + 2;
+  const R h = R(0.5), two = R(2), gamma = R(g.gamma);
+  Tn n2 = nrm[0] * nrm[0] + nrm[1] * nrm[1];
+  if (DIM == 3) n2 = n2 + nrm[2] * nrm[2];
+  const Tn dA = sqrt(n2);
+  const Tn fac = Tn(1) / dA;
+  Tn nh[DIM];
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) nh[k] = nrm[k] * fac;
+  T Unrm = q[1] * nh[0] + q[2] * nh[1];
+  if (DIM == 3) Unrm = Unrm + q[3] * nh[2];
+  T qg[NV];
+  qg[0] = q[0];
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) qg[1 + k] = q[1 + k] - two * Unrm * nh[k];
+  qg[NV - 1] = q[NV - 1];
+  T FL[NV], FR[NV];
+  euler_flux<DIM>(g, q, nrm, FL);
+  euler_flux<DIM>(g, qg, nrm, FR);
+  T qa[NV];
+#pragma unroll
+  for (int c = 0; c < NV; ++c) qa[c] = h * (q[c] + qg[c]);
+  const T ra = R(1) / qa[0];
+  const T pa = pressure<DIM>(g, qa);
+  const T aa = sqrt(gamma * pa * ra);
+  T Un = nrm[0] * qa[1] * ra + nrm[1] * qa[2] * ra;
+  if (DIM == 3) Un = Un + nrm[2] * qa[3] * ra;
+  const T lam = absval(Un) + dA * aa;
+#pragma unroll
+  for (int c = 0; c < NV; ++c) flux[c] = h * (FL[c] + FR[c] - lam * (qg[c] - q[c]));
+}
+
 // logarithmic mean with the 5-term series below u = 1e-3
 template <typename T>
 __device__ __forceinline__ T logavg(const T& aL, const T& aR) {

@@ -80,9 +80,13 @@ __global__ void k_face_flux(DevMesh md, const double* __restrict__ q, double* __
     double nrm[DIM];
 #pragma unroll
     for (int k = 0; k < DIM; ++k) nrm[k] = md.nrm_bndry[((size_t)b * Nf + i) * DIM + k];
+    if (md.bc_of_b[b] == EG_BC_NOPENETRATION_ES) {
+      eg::wall_es_flux<DIM>(g, qL, nrm, fl);
+    } else {
 #pragma unroll
-    for (int c = 0; c < NV; ++c) qR[c] = md.qg_bndry[((size_t)b * Nf + i) * NV + c];
-    eg::roe_flux<DIM>(g, qL, qR, nrm, fl);
+      for (int c = 0; c < NV; ++c) qR[c] = md.qg_bndry[((size_t)b * Nf + i) * NV + c];
+      eg::roe_flux<DIM>(g, qL, qR, nrm, fl);
+    }
   }
   double* out = fflux + (size_t)t * NV;
 #pragma unroll
@@ -358,7 +362,7 @@ DevMesh dev_mesh(const eg_mesh* m) {
   d.face_flux = m->params.face_flux;
   d.Q = m->Q; d.interp = m->interp; d.perm = m->perm; d.nbrperm = m->nbrperm;
   d.lift = m->lift; d.dxidx = m->dxidx; d.ifaces = m->ifaces; d.nrm_face = m->nrm_face;
-  d.bfaces = m->bfaces; d.nrm_bndry = m->nrm_bndry; d.qg_bndry = m->qg_bndry;
+  d.bfaces = m->bfaces; d.nrm_bndry = m->nrm_bndry; d.qg_bndry = m->qg_bndry; d.bc_of_b = m->bc_of_b;
   d.eface = m->eface; d.Minv = m->Minv; d.w = m->w; d.jac = m->jac;
   d.liftS = m->liftS; d.nbrinv = m->nbrinv; d.wface = m->wface; d.sparse_face = m->sparse_face;
   return d;

@@ -80,6 +80,7 @@ def _declare(lib):
     lib.eg_ls_destroy.argtypes = [vp]
     lib.eg_ls_set_tolerances.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_int32]
     lib.eg_ls_solve.argtypes = [vp, vp, vp, C.c_int32, C.POINTER(LsStats)]
+    lib.eg_ls_solve_transpose.argtypes = [vp, vp, vp, C.c_int32, C.POINTER(LsStats)]
     lib.eg_ls_set_grid.argtypes = [vp, C.c_int32]
     lib.eg_set_gmres_batching.argtypes = [C.c_int32, C.c_double]
     lib.eg_newton_solve.argtypes = [vp, vp, C.c_int32, C.POINTER(NewtonOpts), C.POINTER(NewtonStats)]
@@ -609,6 +610,17 @@ class LinearSolver:
             raise ValueError("b and x must both be host or both be device arrays")
         st = LsStats()
         check(self.lib.eg_ls_solve(self.handle, pb, px, mb, C.byref(st)))
+        return st
+
+    def solve_transpose(self, b, x):
+        """linearSolveTranspose (reference ls_standard.jl:230-244): x <- the
+        solution of J^T x = b (x is also the initial guess), on the device."""
+        pb, mb = GPUMesh._ptr(b, self.lo.g.ndof)
+        px, mx = GPUMesh._ptr(x, self.lo.g.ndof)
+        if mb != mx:
+            raise ValueError("b and x must both be host or both be device arrays")
+        st = LsStats()
+        check(self.lib.eg_ls_solve_transpose(self.handle, pb, px, mb, C.byref(st)))
         return st
 
     def close(self):

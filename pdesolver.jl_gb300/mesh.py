@@ -29,6 +29,7 @@ from .sbp import SBPOperator, TET_FACES, TRI_FACES
 
 BC_VORTEX = 0      # isentropicVortexBC (src/solver/euler/bc.jl:542-568)
 BC_FREESTREAM = 1  # FreeStreamBC (src/solver/euler/bc.jl:1562-1647)
+BC_NOPENETRATION_ES = 2  # noPenetrationESBC (src/solver/euler/bc.jl:767-795)
 
 
 @dataclasses.dataclass
@@ -183,12 +184,13 @@ def _face_normals(sbp, dxidx_face_all, faces):
 
 
 def annulus(sbp: SBPOperator, nr: int, ntheta: int, r_in=1.0, r_out=3.0,
-            bc=BC_VORTEX) -> Mesh:
+            bc=BC_VORTEX, bc_of_tag=None) -> Mesh:
     """Quarter annulus r in [r_in, r_out], theta in [0, pi/2] on nr x ntheta
     (r, theta) quads, each split along the diagonal from (r_i, theta_j) to
     (r_{i+1}, theta_{j+1}) into 2 straight-sided triangles (2 nr ntheta
     elements).  Boundary tags: 0 r = r_in, 1 r = r_out, 2 theta = 0,
-    3 theta = pi/2."""
+    3 theta = pi/2; each tag gets `bc`, or bc_of_tag[tag] (a mapping or a
+    callable) when given."""
     assert sbp.dim == 2
     vx, elverts, _ = annulus_grid(nr, ntheta, r_in, r_out)
     X = vx[elverts]                                  # [E, 3, 2]
@@ -214,7 +216,7 @@ def annulus(sbp: SBPOperator, nr: int, ntheta: int, r_in=1.0, r_out=3.0,
         return t
 
     iface, nbrperm, bfaces, offs, bct, tags = _connect(elverts, TRI_FACES, sbp, fpts, tags_of,
-                                                       lambda t: bc)
+                                                       _bc_lookup(bc_of_tag, bc))
     dxf = np.repeat(np.repeat(dx[:, None, None], 3, axis=1), Nf, axis=2)   # [E, F, Nf, 2, 2]
     nrm_f = _face_normals(sbp, dxf, iface[:, [0, 2]])
     crd_f = fpts[iface[:, 0], iface[:, 2]]
@@ -273,7 +275,7 @@ def _p2_tet_shape(lam):
     return N, dN
 
 
-def cube(sbp: SBPOperator, n: int, warp=0.05, seed=3, bc=BC_FREESTREAM) -> Mesh:
+def cube(sbp: SBPOperator, n: int, warp=0.05, seed=3, bc=BC_FREESTREAM, bc_of_tag=None) -> Mesh:
     """Unit cube of n^3 hexes, each split into 6 tetrahedra around the main
     diagonal (6 n^3 elements).  With ``warp`` != 0 every node is moved by
     x_i += warp * sin(pi x + phi) sin(pi y + phi) sin(pi z + phi) (same shift
@@ -282,7 +284,8 @@ def cube(sbp: SBPOperator, n: int, warp=0.05, seed=3, bc=BC_FREESTREAM) -> Mesh:
     coordinates are interpolated from them, so neighbouring elements share
     their faces exactly and the metric terms, computed analytically from the
     P2 map, vary from node to node.  Boundary tags 0..5: x=0, x=1, y=0, y=1,
-    z=0, z=1 of the unwarped cube."""
+    z=0, z=1 of the unwarped cube; each tag gets `bc`, or bc_of_tag[tag]
+    (a mapping or a callable) when given."""
     assert sbp.dim == 3
     phi = float(np.random.default_rng(seed).uniform(0.0, 2 * np.pi)) if warp else 0.0
     vx, elverts, _ = cube_grid(n, with_tags=False)
@@ -336,7 +339,7 @@ def cube(sbp: SBPOperator, n: int, warp=0.05, seed=3, bc=BC_FREESTREAM) -> Mesh:
         return 2 * ax + hi.astype(np.int32)
 
     iface, nbrperm, bfaces, offs, bct, tags = _connect(elverts, TET_FACES, sbp, fpts, tags_of,
-                                                       lambda t: bc)
+                                                       _bc_lookup(bc_of_tag, bc))
     nrm_f = _face_normals(sbp, fdx, iface[:, [0, 2]])
     crd_f = fpts[iface[:, 0], iface[:, 2]]
     nrm_b = _face_normals(sbp, fdx, bfaces)

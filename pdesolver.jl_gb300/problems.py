@@ -90,6 +90,37 @@ def config3(n=24, p=2, seed=4, warp=0.05, warp_seed=3):
     return ms, opts, np.ascontiguousarray(q)
 
 
+def cube_wall(n=2, p=2, seed=11, warp=0.05, warp_seed=3, Ma=0.5):
+    """Entropy-stable steady problem with a wall: the warped cube of n^3
+    hexes -> 6 n^3 tets, diagonal-E p, Ismail-Roe split-form volume terms and
+    IR interface fluxes, the face z = 0 (tag 4) an entropy-stable
+    no-penetration wall (noPenetrationESBC) and the other faces free-stream
+    Dirichlet data at Mach Ma along x; start: that free stream times
+    (1 + U(-0.01, 0.01)) with `seed`."""
+    op = _sbp.get_operator(3, "diage", p)
+    ms = _mesh.cube(op, n, warp=warp, seed=warp_seed,
+                    bc_of_tag=lambda t: _mesh.BC_NOPENETRATION_ES if t == 4 else _mesh.BC_FREESTREAM)
+    opts = {"gamma": 1.4, "Ma": Ma, "aoa": 0.0, "Flux_name": "IRFlux",
+            "volume_integral_type": 2, "Volume_flux_name": "IRFlux"}
+    rng = np.random.default_rng(seed)
+    q = free_stream(3, ms.coords.shape[:2], Ma=Ma)
+    return ms, opts, np.ascontiguousarray(q * (1.0 + rng.uniform(-0.01, 0.01, size=q.shape)))
+
+
+def annulus_wall(n=4, p=2, family="omega", seed=12, M_in=0.5):
+    """The quarter annulus with its inner arc r = 1 (tag 0) an entropy-stable
+    no-penetration wall (the isentropic vortex is tangential there) and
+    vortex Dirichlet data on the other boundaries; Roe faces, weak-form
+    volume terms; state: the vortex times (1 + N(0, 1e-3)) with `seed`."""
+    op = _sbp.get_operator(2, family, p)
+    ms = _mesh.annulus(op, n, n, bc_of_tag=lambda t: _mesh.BC_NOPENETRATION_ES if t == 0 else _mesh.BC_VORTEX)
+    opts = {"gamma": 1.4, "Ma": M_in, "aoa": 0.0, "vortex_M_in": M_in, "Flux_name": "RoeFlux",
+            "volume_integral_type": 1}
+    rng = np.random.default_rng(seed)
+    q = vortex_state(ms.coords, M_in=M_in)
+    return ms, opts, np.ascontiguousarray(q * (1.0 + rng.normal(0.0, 1e-3, size=q.shape)))
+
+
 def config4_specs(count=96, seed=5):
     """Batched workload: `count` annulus problems with n ~ logU(8, 96) (E = 2 n^2),
     SBP-Gamma p ~ U{1, 2, 3, 4}, vortex M_in ~ U(0.3, 0.7), each started from

@@ -17,9 +17,8 @@ Tolerances (written in each assertion):
   Newton: |R| < 1e-10 on both; the oracle's own residual at the device's
   FP64 and mixed states < 1e-10 (each device state is a converged solution of
   the oracle's discretisation); integral of p along r = 1 within 1e-10 (FP64)
-  and 1e-8 (mixed); FP64 states within 1e-9 relative (the two solves stop at
-  different iterates below |R| = 1e-10, and the state difference is the
-  inverse Jacobian times that residual difference).
+  and 1e-8 (mixed); the FP64 and mixed states within 1e-10 relative of the
+  oracle's (measured on a GB300: 6e-13 and 4e-13).
 """
 import os
 import sys
@@ -65,8 +64,7 @@ def test_c2_steady_solve_full_size_matches_oracle(gpu_lib, olib):
         assert steady.strong_norm(olib, ms3, r) < 1e-10, prec
         fg = gl[-1].functional_pressure(qg, 0)
         assert abs(fg - fo) <= ftol * abs(fo), (prec, fg, fo)
-        if prec == 0:
-            assert np.abs(qg - qo).max() <= 1e-9 * np.abs(qo).max()
+        assert np.abs(qg - qo).max() <= 1e-10 * np.abs(qo).max(), prec
 
 
 def test_c3_residual_and_rk4_full_size_match_oracle(gpu_lib, olib):

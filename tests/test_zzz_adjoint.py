@@ -1,8 +1,8 @@
 """Steady adjoint on the device: calcAdjoint with the library's FP64
-Jacobian and block-Jacobi preconditioner (transposed applies on device
-tensors) against a dense solve with the oracle's Jacobian blocks, at 1e-9.
-The Krylov method and the functional derivative are covered on the CPU by
-test_adjoint.py."""
+Jacobian and block-Jacobi preconditioner (the transposed GMRES solve in the
+library, eg_ls_solve_transpose) against a dense solve with the oracle's
+Jacobian blocks, at 1e-9.  The functional derivative is covered on the CPU
+by test_adjoint.py."""
 import numpy as np
 import pytest
 
