@@ -1106,13 +1106,13 @@ def run_c5(args, rank, world):
 def run_tune(args):
     """Autotuner sweep of the element kernel per operator and degree: weak
     form (Roe) on the 64 x 64 annulus with SBP-Gamma p = 1..4 and on the
-    warped 24^3 x 6 cube with diagonal-E tets p = 1, 2; split form (IR) on the
-    same cubes.  Prints one JSON line with every candidate's time."""
+    warped 24^3 x 6 cube with diagonal-E tets p = 1, 2, 3; split form (IR) on
+    the same cubes.  Prints one JSON line with every candidate's time."""
     import torch
     from pdesolver_gb300 import eulergpu
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
     cases = [("2d weak gamma", p, problems.config2(p=p)) for p in (1, 2, 3, 4)]
-    for p in (1, 2):
+    for p in (1, 2, 3):
         ms, opts, q = problems.config3(n=24, p=p)
         cases.append(("3d split diage", p, (ms, opts, q)))
         cases.append(("3d weak diage", p, (ms, dict(opts, Flux_name="RoeFlux", volume_integral_type=1), q)))

@@ -155,19 +155,24 @@ __device__ void elem_face_terms(const DevMesh& md, const T* __restrict__ dF, T* 
 }
 
 // Element block: one CTA per element.  Shared: A[k][m][a][b] (flux
-// Jacobians at the nodes), the block blk[col][row] and face tables.
+// Jacobians at the nodes), the block blk[col][row] and face tables.  With
+// block_in_global (blocks too large for shared memory, e.g. 225 unknowns of
+// the p=3 diagonal-E tetrahedron) the block is accumulated in place in the
+// output: every entry has one writer per pass, passes are separated by
+// __syncthreads, which orders the CTA's global accesses as well.
 template <int DIM, typename T>
 __global__ void k_elem_jac(DevMesh md, const double* __restrict__ q, const T* __restrict__ dF,
-                           T* __restrict__ diag) {
+                           T* __restrict__ diag, int block_in_global) {
   constexpr int NV = DIM + 2;
   using D1 = Fwd<T, NV>;
   extern __shared__ unsigned char smraw[];
   const int Np = md.Np;
   const int n = Np * NV;
-  T* sA = reinterpret_cast<T*>(smraw);               // [DIM][Np][NV][NV]
-  T* sB = sA + (size_t)DIM * Np * NV * NV;            // [n][n] col-major
-  T* sQ = sB + (size_t)n * n;                         // [DIM][Np][Np] = Q
   const int e = blockIdx.x;
+  T* sA = reinterpret_cast<T*>(smraw);               // [DIM][Np][NV][NV]
+  T* sQ = sA + (size_t)DIM * Np * NV * NV;            // [DIM][Np][Np] = Q
+  T* sB = block_in_global ? diag + (size_t)e * n * n  // [n][n] col-major
+                          : sQ + (size_t)DIM * Np * Np;
   for (int t = threadIdx.x; t < DIM * Np * Np; t += blockDim.x) sQ[t] = T(md.Q[t]);
   const Gas g{md.gamma, md.gamma_1};
   // flux Jacobians A_k(q_m) = dF_k/dq at node m, direction dxidx[.][k]
@@ -205,6 +210,7 @@ __global__ void k_elem_jac(DevMesh md, const double* __restrict__ q, const T* __
   }
   __syncthreads();
   elem_face_terms<DIM, T>(md, dF, sB, e);
+  if (block_in_global) return;
   T* dst = diag + (size_t)e * n * n;
   for (int t = threadIdx.x; t < n * n; t += blockDim.x) dst[t] = sB[t];
 }
@@ -260,14 +266,15 @@ __device__ void split_pair_jac(const DevMesh& md, const Gas& g, const double* __
 // (j, m); a diagonal block sums the pairs of node j, in a fixed order.
 template <int DIM, typename T>
 __global__ void k_elem_jac_split(DevMesh md, const double* __restrict__ q, const T* __restrict__ dF,
-                                 T* __restrict__ diag) {
+                                 T* __restrict__ diag, int block_in_global) {
   constexpr int NV = DIM + 2;
   extern __shared__ unsigned char smraw[];
   const int Np = md.Np;
   const int n = Np * NV;
-  T* sB = reinterpret_cast<T*>(smraw);                // [n][n] col-major
-  T* sQ = sB + (size_t)n * n;                         // [DIM][Np][Np] = Q
   const int e = blockIdx.x;
+  T* sQ = reinterpret_cast<T*>(smraw);                // [DIM][Np][Np] = Q
+  T* sB = block_in_global ? diag + (size_t)e * n * n  // [n][n] col-major (see k_elem_jac)
+                          : sQ + (size_t)DIM * Np * Np;
   for (int t = threadIdx.x; t < DIM * Np * Np; t += blockDim.x) sQ[t] = T(md.Q[t]);
   __syncthreads();
   const Gas g{md.gamma, md.gamma_1};
@@ -297,6 +304,7 @@ __global__ void k_elem_jac_split(DevMesh md, const double* __restrict__ q, const
   }
   __syncthreads();
   elem_face_terms<DIM, T>(md, dF, sB, e);
+  if (block_in_global) return;
   T* dst = diag + (size_t)e * n * n;
   for (int t = threadIdx.x; t < n * n; t += blockDim.x) dst[t] = sB[t];
 }
@@ -380,27 +388,29 @@ int launch_jac(eg_lo* lo, const double* q) {
   T* cpl = reinterpret_cast<T*>(lo->cpl);
   const int nslot = (m->I + m->B) * m->Nf;
   const int n = m->Np * m->nv;
-  const size_t smem = sizeof(T) * ((size_t)m->dim * m->Np * m->nv * m->nv + (size_t)n * n +
-                                   (size_t)m->dim * m->Np * m->Np);
+  // the block in shared memory when it fits, else accumulated in place
+  const size_t fixed = sizeof(T) * ((size_t)m->dim * m->Np * m->nv * m->nv + (size_t)m->dim * m->Np * m->Np);
+  const int gblk = fixed + sizeof(T) * (size_t)n * n > 200 * 1024 ? 1 : 0;
+  const size_t smem = fixed + (gblk ? 0 : sizeof(T) * (size_t)n * n);
   eg_phase_begin(m, EG_PHASE_OTHER);
   const bool split = m->params.volume_integral_type == 2;
   if (m->dim == 2) {
     k_face_jac<2, T><<<(nslot + 127) / 128, 128, 0, m->stream>>>(md, q, dF);
     if (split) {
       cudaFuncSetAttribute(k_elem_jac_split<2, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-      k_elem_jac_split<2, T><<<m->E, 256, smem, m->stream>>>(md, q, dF, diag);
+      k_elem_jac_split<2, T><<<m->E, 256, smem, m->stream>>>(md, q, dF, diag, gblk);
     } else {
       cudaFuncSetAttribute(k_elem_jac<2, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-      k_elem_jac<2, T><<<m->E, 256, smem, m->stream>>>(md, q, dF, diag);
+      k_elem_jac<2, T><<<m->E, 256, smem, m->stream>>>(md, q, dF, diag, gblk);
     }
   } else {
     k_face_jac<3, T><<<(nslot + 127) / 128, 128, 0, m->stream>>>(md, q, dF);
     if (split) {
       cudaFuncSetAttribute(k_elem_jac_split<3, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-      k_elem_jac_split<3, T><<<m->E, 256, smem, m->stream>>>(md, q, dF, diag);
+      k_elem_jac_split<3, T><<<m->E, 256, smem, m->stream>>>(md, q, dF, diag, gblk);
     } else {
       cudaFuncSetAttribute(k_elem_jac<3, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-      k_elem_jac<3, T><<<m->E, 256, smem, m->stream>>>(md, q, dF, diag);
+      k_elem_jac<3, T><<<m->E, 256, smem, m->stream>>>(md, q, dF, diag, gblk);
     }
   }
   const int64_t ncpl = (int64_t)eg_lo_coupling_size(lo);
@@ -426,10 +436,9 @@ int launch_jac(eg_lo* lo, const double* q) {
 int eg_jacobian_launch(eg_lo* lo, const double* q) {
   const size_t smem_needed = (lo->prec == EG_F64 ? 8 : 4) *
                              ((size_t)lo->mesh->dim * lo->mesh->Np * lo->mesh->nv * lo->mesh->nv +
-                              (size_t)lo->mesh->dim * lo->mesh->Np * lo->mesh->Np +
-                              (size_t)lo->n * lo->n);
+                              (size_t)lo->mesh->dim * lo->mesh->Np * lo->mesh->Np);
   if (smem_needed > 200 * 1024) {
-    eg_set_error("evalJacobian: element block of %d unknowns exceeds shared memory", lo->n);
+    eg_set_error("evalJacobian: element tables of %d nodes exceed shared memory", lo->mesh->Np);
     return EG_ERR_UNSUPPORTED;
   }
   return lo->prec == EG_F64 ? launch_jac<double>(lo, q) : launch_jac<float>(lo, q);

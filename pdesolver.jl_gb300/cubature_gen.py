@@ -13,7 +13,8 @@ solve the moment equations exactly (Hicken, Del Rey Fernandez & Zingg,
 
 Node counts follow src/dofcount.jl:21-88 of the reference (tri Omega p=1..4:
 3, 6, 10, 15; tri Gamma p=1..4: 3, 7, 12, 18).  The tet diagonal-E node sets
-are this project's own (the reference does not tabulate them).
+(p=1..3: 6, 23 and 45 nodes) are this project's own (the reference does not
+tabulate them).
 
 Reference elements: triangle (-1,-1), (1,-1), (-1,1); tetrahedron
 (-1,-1,-1), (1,-1,-1), (-1,1,-1), (-1,-1,1).
@@ -300,8 +301,10 @@ def build_tet_diage(p):
         face_orbits, face_q = ["vert", "mid", "S21"], 4
         tet_face_kinds = ["vert", "mid", "face21"]
         interior = ["S4"]
+    elif p == 3:
+        return _build_tet_diage3()
     else:
-        raise ValueError("tet diagonal-E rules are built for p = 1, 2")
+        raise ValueError("tet diagonal-E rules are built for p = 1, 2, 3")
     # face rule on the reference triangle
     if all(NFREE[o] == 0 for o in face_orbits):
         fpts = [tri_orbit(o, []) @ TRI_VERTS for o in face_orbits]
@@ -339,6 +342,42 @@ def build_tet_diage(p):
     return pts, wts, fpts_all, fwts, max(fres, vres)
 
 
+def _s21_param(b):
+    """the repeated barycentric coordinate of an S21 point (a, a, 1 - 2a)."""
+    srt = np.sort(b)
+    return float(srt[0]) if np.isclose(srt[0], srt[1]) else float(srt[2])
+
+
+def _build_tet_diage3():
+    """p = 3: on every face a degree-6 triangle rule with the vertices, two
+    points per edge (a, 1 - a) and two S21 orbits (15 face nodes, found by
+    solve_rule); in the volume those 40 boundary nodes plus the centroid and
+    an S31 orbit (c, c, c, 1 - 3c), with weights exact to degree 5 = 2p - 1.
+    The moment equations fix the weights for each c; c is chosen on a grid
+    of step 1e-3 in [0.01, 0.24] to maximise the smallest weight (45 nodes)."""
+    face_orbits = ["vert", "edge", "S21", "S21"]
+    fpts_all, fwts, fres = solve_rule(2, face_orbits, 6, seed=7, tries=60)
+    bary = _tri_bary(fpts_all)
+    edge = bary[3:9]
+    a = float(np.min(edge[edge > 1e-9]))
+    b1, b2 = _s21_param(bary[9]), _s21_param(bary[12])
+    fixed = [tet_orbit("vert", []) @ TET_VERTS, tet_orbit("edge2", [a]) @ TET_VERTS,
+             tet_orbit("face21", [b1]) @ TET_VERTS, tet_orbit("face21", [b2]) @ TET_VERTS,
+             tet_orbit("S4", []) @ TET_VERTS]
+    best = None
+    for c in np.round(np.arange(0.01, 0.2405, 0.001), 6):
+        tet_pts = fixed + [tet_orbit("S31", [float(c)]) @ TET_VERTS]
+        w, vres = solve_linear_weights(3, tet_pts, 5)
+        if vres < 1e-13 and np.all(w > 0) and (best is None or w.min() > best[0]):
+            best = (w.min(), tet_pts, w, vres)
+    if best is None:
+        raise RuntimeError("no positive degree-5 tet rule on the p = 3 face nodes")
+    _, tet_pts, w, vres = best
+    pts = np.concatenate(tet_pts)
+    wts = np.concatenate([np.full(len(pt), wi) for pt, wi in zip(tet_pts, w)])
+    return pts, wts, fpts_all, fwts, max(fres, vres)
+
+
 def _tri_bary(pts):
     # x = -1 + 2 l2, y = -1 + 2 l3 for the reference triangle
     l2 = (pts[:, 0] + 1) / 2
@@ -365,7 +404,7 @@ def main(out_path):
     lines.append('}')
     lines.append('')
     lines.append('TET_DIAGE = {')
-    for p in (1, 2):
+    for p in (1, 2, 3):
         pts, wts, fpts, fwts, res = build_tet_diage(p)
         lines.append(f'    {p}: {{"n": {len(wts)}, "points": {_fmt(pts)},')
         lines.append(f'        "weights": {_fmt(wts)},')

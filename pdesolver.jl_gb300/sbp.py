@@ -26,6 +26,7 @@ not claimed (that package is absent).
 from __future__ import annotations
 
 import dataclasses
+import functools
 import itertools
 
 import numpy as np
@@ -201,6 +202,7 @@ def _finish(dim, p, family, x, w, face_ref, wface, R, perm, interp, sparse):
                        interp=interp, normals=normals, face_xi=face_xi, sparse_face=sparse)
 
 
+@functools.lru_cache(maxsize=None)
 def tri_operator(family: str, p: int) -> SBPOperator:
     """Triangle SBP-Omega (all nodes interior) or SBP-Gamma (p+1 nodes on
     every edge) operator of degree p (reference: getTriSBPOmega /
@@ -244,6 +246,7 @@ def tri_operator(family: str, p: int) -> SBPOperator:
     return _finish(2, p, family, x, w, t[:, None], wface, R, perm, interp, False)
 
 
+@functools.lru_cache(maxsize=None)
 def tet_operator_diage(p: int) -> SBPOperator:
     """Tetrahedral diagonal-E SBP operator (face nodes are volume nodes), the
     kind the reference gets from getTetSBPDiagE (src/solver/common.jl:276-390)."""

@@ -46,7 +46,8 @@ def test_residual_tri_operators(gpu_lib, oracle, fam, p):
     assert rel_err(res, ref) <= TOL
 
 
-@pytest.mark.parametrize("p,flux", [(1, "IRFlux"), (2, "IRFlux"), (2, "RoeFlux")])
+@pytest.mark.parametrize("p,flux", [(1, "IRFlux"), (2, "IRFlux"), (2, "RoeFlux"), (3, "IRFlux"),
+                                    (3, "RoeFlux")])
 def test_residual_tet_split_form(gpu_lib, oracle, p, flux):
     ms, opts, q = problems.config3(n=3, p=p, seed=20 + p)
     opts = dict(opts, Flux_name=flux)

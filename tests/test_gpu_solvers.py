@@ -36,7 +36,7 @@ def test_jacobian_blocks_fp64(gpu_lib, oracle, fam, p, flux):
     assert np.abs(c - rc).max() <= 1e-10 * scale
 
 
-@pytest.mark.parametrize("p,flux", [(1, "RoeFlux"), (2, "RoeFlux"), (2, "IRFlux")])
+@pytest.mark.parametrize("p,flux", [(1, "RoeFlux"), (2, "RoeFlux"), (2, "IRFlux"), (3, "RoeFlux")])
 def test_jacobian_blocks_tet(gpu_lib, oracle, p, flux):
     """warped cube (2^3 x 6 tets), diagonal-E tets (face nodes are volume
     nodes: the element face terms and coupling blocks take the one-term path),
@@ -340,12 +340,13 @@ def test_transposed_operator_and_preconditioner(gpu_lib, oracle, case):
         assert np.abs(z - x).max() <= (1e-11 if prec == 0 else 1e-4) * np.abs(x).max()
 
 
-@pytest.mark.parametrize("case", ["tet1", "tet2", "gamma2"])
+@pytest.mark.parametrize("case", ["tet1", "tet2", "tet3", "gamma2"])
 def test_split_form_jacobian_blocks(gpu_lib, oracle, case):
     """element blocks of the entropy-stable split form (Hadamard pair terms
     differentiated pair by pair) with IR faces against the oracle: FP64 1e-10,
     FP32 1e-5 relative to the largest entry; the operator apply equals the
-    residual's directional derivative."""
+    residual's directional derivative.  tet3 (diagonal-E p=3, 45 nodes, 225
+    unknowns per element) accumulates its blocks in place in device memory."""
     if case.startswith("tet"):
         ms, opts, q = problems.config3(n=2, p=int(case[-1]), seed=91)
     else:

@@ -279,10 +279,11 @@ def test_freestream_residual_roundoff_tri_split_form(oracle, fam, p):
     assert np.abs(res).max() < 1e-12
 
 
-def test_freestream_residual_roundoff_tet_split_form(oracle):
+@pytest.mark.parametrize("p", [2, 3])
+def test_freestream_residual_roundoff_tet_split_form(oracle, p):
     """Free-stream preservation of the Ismail-Roe split form on warped
     (curvilinear) tetrahedra: the discrete metric identities hold."""
-    op = sbp.get_operator(3, "diage", 2)
+    op = sbp.get_operator(3, "diage", p)
     ms = mesh.cube(op, 2, warp=0.05, seed=3, bc=mesh.BC_FREESTREAM)
     desc = abi.MeshDesc(ms)
     P = _p(Ma=0.5, aoa_deg=5.0, face_flux=abi.EG_FLUX_IR, volume_integral_type=2)
@@ -299,8 +300,14 @@ def test_split_form_entropy_conservation_whole_residual(oracle):
     tetrahedra with the Ismail-Roe volume and face fluxes, the entropy
     production of the whole residual is the boundary term alone,
     sum_nodes w . R = sum_boundary nodes wface (psi . n - w . F_bc), psi =
-    rho u, at 1e-12 relative, for a non-uniform state."""
-    op = sbp.get_operator(3, "diage", 2)
+    rho u, at 1e-12 relative, for a non-uniform state (diagonal-E p=2 and
+    p=3)."""
+    for p in (2, 3):
+        _entropy_production_case(oracle, p)
+
+
+def _entropy_production_case(oracle, p):
+    op = sbp.get_operator(3, "diage", p)
     ms = mesh.cube(op, 2, warp=0.05, seed=3, bc=mesh.BC_FREESTREAM)
     P = _p(Ma=0.5, face_flux=abi.EG_FLUX_IR, volume_integral_type=2)
     x = ms.coords
@@ -447,7 +454,7 @@ def test_explicit_jacobian_vs_dual_jvp(oracle, fam, p, flux):
         assert np.abs(b1 - b2).max() < 1e-11 * max(1.0, np.abs(b2).max())
 
 
-@pytest.mark.parametrize("p", [1, 2])
+@pytest.mark.parametrize("p", [1, 2, 3])
 def test_split_form_jacobian_vs_dual_jvp(oracle, p):
     """the entropy-stable split-form volume Jacobian (pair by pair, as
     calcVolumeIntegralsSplitFormCurvilinear_diff, euler_funcs_diff.jl:330-430)

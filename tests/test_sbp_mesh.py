@@ -6,7 +6,7 @@ import pytest
 from pdesolver_gb300 import cubature_tables, mesh, sbp
 
 OPS = [(2, "omega", p) for p in (1, 2, 3, 4)] + [(2, "gamma", p) for p in (1, 2, 3, 4)] + \
-      [(3, "diage", p) for p in (1, 2)]
+      [(3, "diage", p) for p in (1, 2, 3)]
 
 
 @pytest.mark.parametrize("dim,fam,p", OPS)
