@@ -26,7 +26,18 @@ state) as they arrive and keeps up to `slots` of them on the device at once:
   recently used first, when an admission needs their memory;
 * each request's arithmetic does not depend on what else runs: its kernels
   see only its own arrays, and the block counts of its launches depend only
-  on its own sizes, so a result is the same alone and in the mix.
+  on its own sizes, so a result is the same alone and in the mix;
+* preemption (the serving counterpart of the reference's checkpoint/restart,
+  src/Utils/checkpoint.jl): `preempt(rid)` stops a running request at its
+  next continuation-level boundary.  Its state at that point (the converged
+  state of the finished level, the Newton options of the current attempt, the
+  statistics so far) is copied to host memory as a RequestSnapshot, its
+  device slot and memory budget are released (its meshes, with their Newton
+  work objects, go to the idle pool like a finished request's, where an
+  admission that needs the memory evicts them), and the request goes to the
+  back of the queue.  When it is admitted again it resumes from the snapshot
+  on any slot: the prolongation and the next level's Newton solve start from
+  the same bits, so the result is bitwise the one of an uninterrupted solve.
 
 `SteadySolveServer.serve(requests)` replays the requests' arrival times in
 real time and returns one result per request with its latency (completion
@@ -40,6 +51,19 @@ import time
 from dataclasses import dataclass, field
 
 import numpy as np
+
+
+@dataclass
+class RequestSnapshot:
+    """Host copy of a request's progress at a continuation-level boundary:
+    `level` is the next level to solve, q the converged state of level
+    `level - 1`, opts the Newton options of the current attempt (the
+    pseudo-time step after retries), stats the finished levels' statistics."""
+    level: int
+    q: np.ndarray
+    opts: dict
+    attempt: int
+    stats: list
 
 
 @dataclass
@@ -57,6 +81,7 @@ class SolveRequest:
     level_tol: float | None = None
     functional_group: int | None = 0
     footprint: int = 0
+    snapshot: RequestSnapshot | None = None   # set when the request was preempted
 
 
 @dataclass
@@ -71,6 +96,7 @@ class RequestResult:
     footprint: int = 0
     retries: int = 0
     launches: int = 0                # library kernel launches of the request
+    preemptions: int = 0             # times the request was stopped and resumed
     error: str | None = None
 
     @property
@@ -171,6 +197,7 @@ class SteadySolveServer:
         self._head_bypassed = 0
         self._closed = False
         self._results = {}
+        self._preempt = set()        # rids to stop at their next level boundary
         self._threads = []
         self.peak_bytes = 0
         self.peak_running = 0
@@ -193,33 +220,68 @@ class SteadySolveServer:
             g.close()
 
     def _gpu_run_request(self, req, meshes, stream, res):
+        """Run (or resume) a request; returns a RequestSnapshot when it was
+        preempted at a level boundary, else None."""
         for g, (_, opts) in zip(meshes, req.levels):
             g.set_stream(stream.cuda_stream)
             if g.opts != opts:
                 g.set_params(opts)
         l0 = sum(g.timings().launches for g in meshes)
         try:
-            self._gpu_solve(req, meshes, stream, res)
+            return self._gpu_solve(req, meshes, stream, res)
         finally:
-            res.launches = sum(g.timings().launches for g in meshes) - l0
+            res.launches += sum(g.timings().launches for g in meshes) - l0
 
     def _gpu_solve(self, req, meshes, stream, res):
+        """The p-continuation solve of eulergpu.solve_steady level by level,
+        with the retry rule of batch.solve_one (from the initial state, the
+        initial pseudo-time step divided by 4), resumable from a snapshot and
+        stoppable at a level boundary."""
         import torch
 
-        from .batch import SteadyProblem, solve_one
+        from .eulergpu import EulerGPUError, prolong
+        snap = req.snapshot
+        attempt = snap.attempt if snap else 0
+        opts = dict(snap.opts) if snap else dict(req.opts)
         with torch.cuda.stream(stream):
-            q0 = torch.from_numpy(np.ascontiguousarray(req.q0)).to("cuda", non_blocking=False)
-            pr = SteadyProblem(levels=meshes, q0=q0, opts=req.opts, level_tol=req.level_tol,
-                               tag=req.rid)
-            out = solve_one(pr, precision=self.precision, retries=self.retries, stream=stream)
-            res.retries = out.retries
-            res.stats = [s.asdict() for s in out.stats]
-            if out.error is not None:
-                res.error = out.error
-                return
+            while True:
+                try:
+                    if snap is not None:
+                        start, stats = snap.level, list(snap.stats)
+                        q = torch.from_numpy(np.ascontiguousarray(snap.q)).to("cuda")
+                    else:
+                        start, stats = 0, []
+                        q = torch.from_numpy(np.ascontiguousarray(req.q0)).to("cuda")
+                    snap = None
+                    for k in range(start, len(meshes)):
+                        g = meshes[k]
+                        if k > 0:
+                            ms = g.mesh
+                            qn = q.new_zeros((ms.numEl, ms.numNodesPerElement, ms.numDofPerNode))
+                            prolong(meshes[k - 1], q, g, qn)
+                            q = qn
+                        o = dict(opts)
+                        if k < len(meshes) - 1 and req.level_tol is not None:
+                            o["res_abstol"] = req.level_tol
+                        stats.append(g.newton(q, o, precision=self.precision).asdict())
+                        if k < len(meshes) - 1 and req.rid in self._preempt:
+                            self._preempt.discard(req.rid)
+                            return RequestSnapshot(level=k + 1, q=q.cpu().numpy(), opts=opts,
+                                                   attempt=attempt, stats=stats)
+                    break
+                except EulerGPUError as e:
+                    attempt += 1
+                    res.retries = attempt
+                    if attempt > self.retries:
+                        res.error = str(e)
+                        res.stats = stats
+                        return None
+                    opts["euler_tau"] = opts.get("euler_tau", 1.0) * 0.25
+            res.stats = stats
             if req.functional_group is not None:
-                res.functional = meshes[-1].functional_pressure(out.q, req.functional_group)
-            res.q = out.q.cpu().numpy()
+                res.functional = meshes[-1].functional_pressure(q, req.functional_group)
+            res.q = q.cpu().numpy()
+        return None
 
     # ---- scheduling ------------------------------------------------------
     def _pick(self):
@@ -277,18 +339,31 @@ class SteadySolveServer:
             for m in evicted:
                 self._close_meshes(m)
             res = self._results[req.rid]
-            res.admitted = self.clock()
+            if req.snapshot is None:
+                res.admitted = self.clock()
             res.footprint = req.footprint
+            snap = None
             try:
                 if meshes is None:
                     meshes = self._make_meshes(req)
-                self._run_request(req, meshes, stream, res)
+                snap = self._run_request(req, meshes, stream, res)
             except Exception as e:  # reported per request
                 res.error = f"{type(e).__name__}: {e}"
-            res.done = self.clock()
+            stopped = isinstance(snap, RequestSnapshot) and res.error is None
+            if not stopped:
+                res.done = self.clock()
             with self._cv:
                 self._in_flight -= req.footprint
                 self._running -= 1
+                if stopped:
+                    # the request leaves the device: state on the host, back
+                    # of the queue, resumed from the snapshot when admitted
+                    req.snapshot = snap
+                    res.preemptions += 1
+                    self._pending.append(req)
+                else:
+                    req.snapshot = None
+                    self._preempt.discard(req.rid)
                 if meshes is not None and req.key is not None and res.error is None:
                     self.pool.give(req.key, meshes, req.footprint)
                     meshes = None
@@ -305,6 +380,14 @@ class SteadySolveServer:
                          for _ in range(self.slots)]
         for t in self._threads:
             t.start()
+
+    def preempt(self, rid):
+        """Stop request `rid` at its next continuation-level boundary (see the
+        module docstring): its state moves to host memory, its slot and
+        memory are released, and it resumes later from there.  A request
+        that has no level boundary left finishes normally."""
+        with self._cv:
+            self._preempt.add(rid)
 
     def submit(self, req: SolveRequest):
         """queue a request now (its arrival is the current clock)."""

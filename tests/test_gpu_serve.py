@@ -165,3 +165,28 @@ def test_batched_gmres_gives_the_same_bits_as_alone(gpu_lib):
         assert a.error is None and b.error is None, (a.error, b.error)
         assert [s.krylov_iters for s in a.stats] == [s.krylov_iters for s in b.stats]
         assert torch.equal(a.q, b.q)
+
+
+def test_preempted_request_resumes_bitwise(gpu_lib):
+    """preemption at a continuation-level boundary: request 0 (2-D, p=1 then
+    p=3) is stopped after its p=1 level, its state goes to host memory, the
+    other requests run on the single slot, and it resumes from the snapshot;
+    its final state and functional are bitwise those of the same request
+    solved without interruption."""
+    reqs = _requests()[:3]
+    srv = serve.SteadySolveServer(8 << 30, slots=1, precision=1)
+    srv.preempt(0)
+    out = srv.serve(reqs)
+    srv.close()
+    assert all(r.error is None for r in out), [r.error for r in out]
+    assert out[0].preemptions == 1 and len(out[0].stats) == 2
+    assert out[0].done > out[1].done
+    ref_srv = serve.SteadySolveServer(8 << 30, slots=1, precision=1)
+    r0 = _requests()[0]
+    ref = ref_srv.serve([serve.SolveRequest(rid=0, levels=r0.levels, q0=r0.q0, opts=r0.opts,
+                                            key=r0.key, level_tol=r0.level_tol)])[0]
+    ref_srv.close()
+    assert ref.preemptions == 0
+    assert np.array_equal(out[0].q, ref.q)
+    assert out[0].functional == ref.functional
+    assert [s["krylov_iters"] for s in out[0].stats] == [s["krylov_iters"] for s in ref.stats]

@@ -142,6 +142,32 @@ def test_failed_request_is_reported_and_not_pooled():
     assert [("mesh", 1)] in dev.closed
 
 
+def test_preempted_request_leaves_the_device_and_resumes_last():
+    """preempt(rid): the request stops at its level boundary (the fake device
+    returns a snapshot), releases its slot and memory, goes to the back of
+    the queue, later resumes from its snapshot once, and completes with one
+    result; the request waiting behind it runs in between."""
+    dev = FakeDevice(seconds=0.03)
+    seen = []
+
+    def run(req, meshes, stream, res):
+        seen.append((req.rid, None if req.snapshot is None else req.snapshot.level))
+        dev.run(req, meshes, stream, res)
+        if req.rid == 0 and req.snapshot is None:
+            return serve.RequestSnapshot(level=1, q=np.zeros(3), opts={}, attempt=0, stats=[])
+        assert req.rid != 0 or req.snapshot.level == 1
+        return None
+
+    srv = serve.SteadySolveServer(100, slots=1, run_request=run, make_meshes=dev.make_meshes,
+                                  close_meshes=dev.close_meshes, make_stream=lambda: None)
+    out = srv.serve([req(0, 50), req(1, 50, arrival=0.005)])
+    assert [r.error for r in out] == [None, None]
+    assert seen == [(0, None), (1, None), (0, 1)]
+    assert out[0].preemptions == 1 and out[1].preemptions == 0
+    assert out[0].done > out[1].done
+    assert srv._in_flight == 0 and srv._running == 0
+
+
 def test_estimate_mem_counts_the_newton_objects(gpu_lib):
     """eg_estimate_mem (loads the library, no device work): the Jacobian,
     inverse blocks and Krylov basis have the sizes the solver allocates."""
