@@ -650,6 +650,20 @@ def run_c3(args, rank, world):
     tc = time.perf_counter()
     lib.oracle_eval_residual(C.byref(desc.desc), C.byref(P), abi.dptr(q), abi.dptr(res))
     t_cpu_res = time.perf_counter() - tc
+    # errors against the oracle on the same inputs: the residual at the start
+    # state, and 5 RK4 steps (the oracle on all host threads)
+    rg = np.zeros_like(q)
+    g.eval_residual(q, rg)
+    qg5 = q.copy()
+    g.rk4(qg5, h, 5 * h)
+    steady = _oracle_steady()
+    olib = steady.load()
+    olib.oracle_set_threads(os.cpu_count() or 1)
+    qo5 = q.copy()
+    steady.rk4(olib, ms, opts, qo5, h, 5)
+    err = {"residual": float(np.abs(rg - res).max() / np.abs(res).max()),
+           "rk4_5_steps_state": float(np.abs(qg5 - qo5).max() / np.abs(qo5).max()),
+           "what": "max-norm relative errors against the CPU oracle on the same inputs (full mesh)"}
     line = {
         "metric": "RK4 steps/s", "value": value, "unit": "steps/s", "n_gpus": world,
         "steps": st.steps, "warmup": args.warmup, "ms_per_step": total_ms / max(st.steps, 1),
@@ -674,6 +688,7 @@ def run_c3(args, rank, world):
                                                    "(%.1f s), 4 per RK4 step" % t_cpu_res},
         "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": int(q.nbytes / nsteps),
                 "d2h_bytes_per_step": int(q.nbytes / nsteps)},
+        "error_vs_oracle": err,
         "gpu_launches": int(n_launch),
         "clocks": clk.summary(),
     }
@@ -747,11 +762,22 @@ def run_c1(args, rank, world):
     desc = abi.MeshDesc(ms)
     P = eulergpu.params_from_opts(opts)
     res = np.zeros_like(q)
+    lib.oracle_eval_residual(C.byref(desc.desc), C.byref(P), abi.dptr(q), abi.dptr(res))
+    # the CPU baseline: the oracle's own RK4, the same 100 steps, timed (1 core)
+    steady = _oracle_steady()
+    olib = steady.load()
+    olib.oracle_set_threads(1)
+    qo = q.copy()
     tc = time.perf_counter()
-    nr = 50
-    for _ in range(nr):
-        lib.oracle_eval_residual(C.byref(desc.desc), C.byref(P), abi.dptr(q), abi.dptr(res))
-    t_cpu = (time.perf_counter() - tc) / nr
+    sto = steady.rk4(olib, ms, opts, qo, h, nsteps)
+    t_cpu_steps = time.perf_counter() - tc
+    qg = q.copy()
+    g.rk4(qg, h, nsteps * h)
+    rg = np.zeros_like(q)
+    g.eval_residual(q, rg)
+    err = {"residual": float(np.abs(rg - res).max() / np.abs(res).max()),
+           "rk4_100_steps_state": float(np.abs(qg - qo).max() / np.abs(qo).max()),
+           "what": "max-norm relative errors against the CPU oracle on the same inputs"}
     rbytes, rflops = residual_model(ms)
     peaks, src = measured_peaks()
     line = {
@@ -771,11 +797,13 @@ def run_c1(args, rank, world):
                      "traffic": None,
                      "kernel": "residual (k_face_flux + k_element): 0.35 MB per evaluation, far "
                                "below the launch floor; the fraction is not meaningful"},
-        "cpu_baseline": {"value": 1.0 / (4 * t_cpu), "unit": "steps/s", "cores": used,
+        "cpu_baseline": {"value": sto.steps / t_cpu_steps, "unit": "steps/s", "cores": 1,
                          "kind": "port",
-                         "sample": f"{nr} oracle residual evaluations on 1 core (4 per RK4 step)"},
+                         "sample": "the oracle's RK4, %d steps of this workload on 1 core, timed "
+                                   "(%.3f s)" % (sto.steps, t_cpu_steps)},
         "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": int(q.nbytes / nsteps),
                 "d2h_bytes_per_step": int(q.nbytes / nsteps)},
+        "error_vs_oracle": err,
         "gpu_launches": int(n_launch),
         "clocks": clk.summary(),
     }

@@ -35,27 +35,30 @@ constexpr size_t kRingBudget = 160 * 1024;
 constexpr size_t kSlotTarget = 12 * 1024;
 
 // Operator ring of the Arnoldi apply: the block's elements are cut into units
-// of `eps` consecutive elements; unit u goes through slot u % nstage, which
-// belongs to consumer group u % nstage (wpg warps).  One thread of the group
-// issues the bulk copies of a unit (its inverse blocks, one contiguous range,
-// and, for 2-D dense coupling, the neighbours' coupling blocks of its faces)
-// on the slot's mbarrier; the group computes z = D^-1 v for the unit from
-// the slot, pushes the coupling products C z to the neighbours' face sides,
-// and issues the next unit into the slot.  After its last unit a group
-// issues its first unit again: the copies of the next Arnoldi iteration's
-// first units are in flight during the grid barriers and vector passes.
+// of `eps` consecutive elements, each unit's operator data (its inverse
+// blocks, one contiguous range, and for 2-D dense coupling the neighbours'
+// coupling blocks of its faces) is one set of bulk copies into a slot of a
+// ring of nslot slots.  One producer thread keeps the slots filled (full /
+// empty mbarrier pairs) and runs ahead into the next Arnoldi iteration's
+// first units, so those copies are in flight during the grid barriers and
+// vector passes; ngroup consumer groups of wpg warps compute z = D^-1 v and
+// push C z from the slots.  When all of a block's units fit in the ring it is
+// resident: loaded once for the whole solve.
 struct RingCfg {
   int on;          // 1: the Arnoldi apply runs through the ring
-  int nstage;      // slots = consumer groups
+  int nslot;       // slots of the ring
+  int resident;    // 1: every unit has its own slot, loaded once
   int eps;         // elements per unit
+  int ngroup;      // consumer groups
   int wpg;         // warps per consumer group
   int cpl_tma;     // coupling blocks arrive in the slot (2-D dense coupling)
   int slot_bytes;  // bytes of one slot (multiple of 128)
   int inv_cap;     // bytes of a slot's inverse-block region (multiple of 16)
   int cpl_bytes;   // bytes of one coupling block
   int fside_smem;  // the block's [epb][F] face-side table is staged in shared memory
+  int vj_smem;     // the block's rows of v_j are staged in shared memory per apply
   // dynamic shared memory offsets (bytes)
-  int off_ring, off_bar, off_z, off_v, off_red, off_fside, off_sz;
+  int off_ring, off_bar, off_z, off_v, off_vj, off_red, off_fside, off_sz;
 };
 
 template <typename T>
@@ -228,8 +231,8 @@ __device__ void block_reduce_all(const T* __restrict__ part, int nblk, int cnt, 
 
 // y = (x - sum_{k<cnt} V[k] h[k]) * s on the block's rows, by threads
 // t0 .. NT-1 (x and y may alias).  The basis loads of a row are issued in
-// batches of 4 before their updates, so 4 loads per thread are in flight;
-// the sum runs over k in order.
+// batches of 16 before their updates (one round trip to L2 per batch); the
+// sum runs over k in order.
 template <typename T>
 __device__ void block_sub_scale(const T* __restrict__ V, const T* __restrict__ h, int cnt, int64_t N,
                                 const T* x, T s, T* y, int64_t r0, int nrow, bool vec, int t0) {
@@ -254,13 +257,13 @@ __device__ void block_sub_scale(const T* __restrict__ V, const T* __restrict__ h
     for (int i = threadIdx.x - t0; i < nrow; i += NT - t0) {
       const int64_t row = r0 + i;
       T a = x[row];
-      for (int k0 = 0; k0 < cnt; k0 += 8) {
-        T v[8];
+      for (int k0 = 0; k0 < cnt; k0 += 16) {
+        T v[16];
 #pragma unroll
-        for (int q = 0; q < 8; ++q)
+        for (int q = 0; q < 16; ++q)
           if (k0 + q < cnt) v[q] = V[(size_t)(k0 + q) * N + row];
 #pragma unroll
-        for (int q = 0; q < 8; ++q)
+        for (int q = 0; q < 16; ++q)
           if (k0 + q < cnt) a -= v[q] * h[k0 + q];
       }
       y[row] = a * s;
@@ -317,9 +320,10 @@ __device__ __forceinline__ void stp(T* p, const Pack<T, W>& r) {
   }
 }
 
-// Sum of v[k] over the 32 lanes for each of the KC slots, as a transposed
-// butterfly (KC - 1 shuffles for KC = 32): afterwards lane l holds the sum
-// of slot l * KC / 32 (lanes 2i and 2i+1 both hold slot i when KC = 16).
+// Sum of v[k] over the 32 lanes for each of the KC slots (KC a power of two,
+// at most 32), as a transposed butterfly (KC - 1 shuffles for KC = 32):
+// afterwards lane l holds the sum of slot l * KC / 32 (the 32 / KC lanes
+// l with equal l * KC / 32 hold the same sum).
 template <typename T, int KC>
 __device__ __forceinline__ void transpose_reduce(T (&v)[KC], int lane) {
   int o = 16;
@@ -350,7 +354,7 @@ __device__ void gs_dots_w(const CoopArgs<T>& a, const T* __restrict__ vj, bool g
                           int nrow, int e0, const int* __restrict__ sSpos, const int* __restrict__ sFside,
                           T* __restrict__ sRed, T* __restrict__ pb) {
   constexpr int NV = DIM + 2;
-  constexpr int KC = 16;
+  constexpr int KC = 8;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nu = nrow / W, n = a.n, F = a.F, Np = a.md.Np, nb = a.nb;
   const int64_t N = a.N;
@@ -404,29 +408,25 @@ __device__ void gs_dots_w(const CoopArgs<T>& a, const T* __restrict__ vj, bool g
 #pragma unroll
         for (int q = 0; q < W; ++q) accw += wv.v[q] * wv.v[q];
       }
-      // basis loads in batches of 4 (in flight together), then their dots
+      // every basis load of the chunk issued before the first dot (one
+      // round trip to L2 per chunk and row)
+      Pack<T, W> v[KC];
 #pragma unroll
-      for (int kb = 0; kb < KC; kb += 4) {
-        if (kb < nk) {
-          Pack<T, W> v[4];
+      for (int k = 0; k < KC; ++k)
+        if (k < nk) v[k] = ldp<T, W>(a.V + (size_t)(k0 + k) * N + row);
 #pragma unroll
-          for (int q = 0; q < 4; ++q)
-            if (kb + q < nk) v[q] = ldp<T, W>(a.V + (size_t)(k0 + kb + q) * N + row);
+      for (int k = 0; k < KC; ++k) {
+        if (k < nk) {
+          T d = T(0);
 #pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            if (kb + q < nk) {
-              T d = T(0);
-#pragma unroll
-              for (int c = 0; c < W; ++c) d += v[q].v[c] * wv.v[c];
-              acc[kb + q] += d;
-            }
-          }
+          for (int c = 0; c < W; ++c) d += v[k].v[c] * wv.v[c];
+          acc[k] += d;
         }
       }
     }
     transpose_reduce<T, KC>(acc, lane);
-    if (KC == 32) sRed[warp * 33 + lane] = acc[0];
-    else if ((lane & 1) == 0) sRed[warp * 33 + (lane >> 1)] = acc[0];
+    constexpr int LPS = 32 / KC;  // lanes holding each slot's sum
+    if (lane % LPS == 0) sRed[warp * 33 + lane / LPS] = acc[0];
     if (k0 == 0) {
       const T ww = wsum(accw);
       if (lane == 0) sRed[warp * 33 + 32] = ww;
@@ -457,18 +457,28 @@ __device__ void gs_dots(const CoopArgs<T>& a, const T* __restrict__ vj, bool gat
 }
 
 // ---- operator ring (see RingCfg) -----------------------------------------
+// Unit u of Arnoldi iteration `it` has the sequence number s = it * nunits +
+// u (s = u for a resident ring, loaded once) and travels through slot
+// s % nslot, on the slot's n-th use with n = s / nslot: its full barrier
+// completes phase n (parity n & 1) when the copies land, and its empty
+// barrier completes phase n when the consumer group has released it.
 struct RingState {
-  uint32_t parity;  // phase of the group's slot barrier the next wait expects
-  int pending;      // a unit's copies were issued into the group's slot and not waited for
-  int failed;       // a wait of this thread gave up: no further waits
+  int it;           // Arnoldi operator applies done by this block
+  long long issued; // producer thread: sequence numbers issued so far
+  int failed;       // a bounded wait of this thread gave up: no further waits
 };
 
-// one thread: issue the copies of unit u into `slot`, armed on `bar`
+// the producer thread: issue the copies of unit u (sequence s) into its slot,
+// armed on the slot's full barrier
 template <typename T>
-__device__ void ring_issue(const CoopArgs<T>& a, int u, int e0, int e1, unsigned char* slot, uint64_t* bar,
-                           const int* __restrict__ sFside) {
+__device__ void ring_issue(const CoopArgs<T>& a, long long s, int nunits, int e0, int e1,
+                           unsigned char* dsm, const int* __restrict__ sFside) {
   const RingCfg& rc = a.rc;
   const int n = a.n, F = a.F;
+  const int u = (int)(s % nunits);
+  const int slot_id = (int)(s % rc.nslot);
+  unsigned char* slot = dsm + rc.off_ring + (size_t)slot_id * rc.slot_bytes;
+  uint64_t* full = reinterpret_cast<uint64_t*>(dsm + rc.off_bar) + slot_id;
   const int c0 = e0 + u * rc.eps, nl = min(rc.eps, e1 - c0);
   const size_t nn = (size_t)n * n * sizeof(T);
   const char* src = reinterpret_cast<const char*>(a.inv) + (size_t)c0 * nn;
@@ -484,8 +494,8 @@ __device__ void ring_issue(const CoopArgs<T>& a, int u, int e0, int e1, unsigned
         if (fs >= 0) total += (uint32_t)rc.cpl_bytes;
       }
   }
-  mbar_arrive_expect_tx(bar, total);
-  bulk_g2s(slot, src - delta, binv, bar);
+  mbar_arrive_expect_tx(full, total);
+  bulk_g2s(slot, src - delta, binv, full);
   if (rc.cpl_tma) {
     const char* cb = reinterpret_cast<const char*>(a.cpl);
     for (int le = 0; le < nl; ++le)
@@ -493,15 +503,20 @@ __device__ void ring_issue(const CoopArgs<T>& a, int u, int e0, int e1, unsigned
         const int fs = rc.fside_smem ? sFside[(c0 - e0 + le) * F + f] : a.fside[(size_t)(c0 + le) * F + f];
         if (fs < 0) continue;
         bulk_g2s(slot + rc.inv_cap + (size_t)(le * F + f) * rc.cpl_bytes,
-                 cb + (size_t)(fs ^ 1) * rc.cpl_bytes, (uint32_t)rc.cpl_bytes, bar);
+                 cb + (size_t)(fs ^ 1) * rc.cpl_bytes, (uint32_t)rc.cpl_bytes, full);
       }
   }
 }
 
-// The Arnoldi operator apply of iteration j through the ring: for every
-// unit of the block, z = D^-1 v_j per element (inverse blocks from the slot,
-// v from the unit's own rows staged in shared memory), then the push of the
-// coupling products C z to the neighbours' face sides (cfs).
+// The Arnoldi operator apply of iteration `it` through the ring: the
+// producer (lane 0 of the last warp) keeps up to nslot units in flight and
+// runs ahead into the first units of the next iteration (the operator is the
+// same in every iteration) as slots free up; consumer group g takes units g,
+// g + ngroup, ...: z = D^-1 v_j per element (inverse blocks from the slot, v
+// from the unit's own rows staged in shared memory), then the push of the
+// coupling products C z to the neighbours' face sides (cfs), then releases
+// the slot.  A resident ring (all units fit in the slots) is loaded once for
+// the whole solve.
 template <int DIM, int NB, typename T>
 __device__ void ring_apply_push(const CoopArgs<T>& a, const T* __restrict__ vj, int e0, int e1,
                                 unsigned char* dsm, const int* __restrict__ sPerm,
@@ -510,36 +525,77 @@ __device__ void ring_apply_push(const CoopArgs<T>& a, const T* __restrict__ vj, 
   const RingCfg& rc = a.rc;
   const int n = NB > 0 ? NB : a.n;
   const int F = a.F, S = a.S, nb = a.nb;
-  const int g = (threadIdx.x >> 5) / rc.wpg;
+  const int warp = threadIdx.x >> 5;
   const int nunits = (e1 - e0 + rc.eps - 1) / rc.eps;
-  if (g >= rc.nstage || g >= nunits) return;
+  const int it = rs.it++;
+  if (nunits <= 0) return;
+  uint64_t* fullb = reinterpret_cast<uint64_t*>(dsm + rc.off_bar);
+  uint64_t* emptyb = fullb + rc.nslot;
+  // the block's rows of v_j in shared memory (when they fit): the consumer
+  // groups read them there instead of one round trip to L2 per unit
+  T* sVj = reinterpret_cast<T*>(dsm + rc.off_vj);
+  if (rc.vj_smem) {
+    for (int t = threadIdx.x; t < (e1 - e0) * n; t += NT) sVj[t] = vj[(size_t)e0 * n + t];
+    __syncthreads();
+  }
+  if (warp == NW - 1) {
+    // producer: the whole warp runs the loop and waits (converged); lane 0
+    // issues the copies
+    const int lane = threadIdx.x & 31;
+    const long long upto = rc.resident ? (long long)nunits
+                                       : (long long)(it + 1) * nunits + min(rc.nslot, nunits);
+    for (long long s = rs.issued; s < upto; ++s) {
+      if (s >= rc.nslot && !rs.failed) {
+        // the slot's previous use (sequence s - nslot) must be released
+        const uint32_t par = (uint32_t)(((s / rc.nslot) - 1) & 1);
+        if (!mbar_wait(emptyb + (s % rc.nslot), par)) {
+          rs.failed = 1;
+          if (lane == 0) atomicOr(a.flags + F_TMO, 1);
+        }
+      }
+      __syncwarp();
+      if (lane == 0) {
+        fence_proxy_async_smem();
+        ring_issue<T>(a, s, nunits, e0, e1, dsm, sFside);
+      }
+      __syncwarp();
+    }
+    if (upto > rs.issued) rs.issued = upto;
+    return;
+  }
+  const int g = warp / rc.wpg;
+  if (g >= rc.ngroup || g >= nunits) return;
   const int GT = rc.wpg * 32, gt = threadIdx.x - g * GT;
-  unsigned char* slot = dsm + rc.off_ring + (size_t)g * rc.slot_bytes;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(dsm + rc.off_bar) + g;
   T* zb = reinterpret_cast<T*>(dsm + rc.off_z) + (size_t)g * rc.eps * n;
   T* vb = reinterpret_cast<T*>(dsm + rc.off_v) + (size_t)g * rc.eps * n;
-  if (!rs.pending && gt == 0) ring_issue<T>(a, g, e0, e1, slot, bar, sFside);
-  for (int u = g; u < nunits; u += rc.nstage) {
+  for (int u = g; u < nunits; u += rc.ngroup) {
+    const long long sq = rc.resident ? (long long)u : (long long)it * nunits + u;
+    const int slot_id = (int)(sq % rc.nslot);
+    const uint32_t par = rc.resident ? 0u : (uint32_t)((sq / rc.nslot) & 1);
+    const unsigned char* slot = dsm + rc.off_ring + (size_t)slot_id * rc.slot_bytes;
     const int c0 = e0 + u * rc.eps, nl = min(rc.eps, e1 - c0);
-    for (int t = gt; t < nl * n; t += GT) vb[t] = vj[(size_t)c0 * n + t];
-    // after a wait that gave up, the group stops waiting (its results are
+    const T* vu = vb;
+    if (rc.vj_smem)
+      vu = sVj + (size_t)(c0 - e0) * n;
+    else
+      for (int t = gt; t < nl * n; t += GT) vb[t] = vj[(size_t)c0 * n + t];
+    // after a wait that gave up, the thread stops waiting (the results are
     // void and the host reports EG_ERR_TIMEOUT)
-    if (!rs.failed && !mbar_wait(bar, rs.parity)) {
+    if (!rs.failed && !mbar_wait(fullb + slot_id, par)) {
       rs.failed = 1;
       atomicOr(a.flags + F_TMO, 1);
     }
-    rs.parity ^= 1u;
     named_sync(1 + g, GT);
     const T* inv = reinterpret_cast<const T*>(slot + (((size_t)c0 * n * n * sizeof(T)) & 15));
     for (int t = gt; t < nl * n; t += GT) {
       const int le = t / n, r = t - le * n;
-      zb[t] = block_row<NB, T>(inv + (size_t)le * n * n, vb + (size_t)le * n, r, n);
+      zb[t] = block_row<NB, T>(inv + (size_t)le * n * n, vu + (size_t)le * n, r, n);
     }
     named_sync(1 + g, GT);
     // push: row i of the neighbour's coupling block on face f of element le
     const int nitem = nl * F * nb;
-    for (int it = gt; it < nitem; it += GT) {
-      const int le = it / (F * nb), rem = it - le * (F * nb);
+    for (int itm = gt; itm < nitem; itm += GT) {
+      const int le = itm / (F * nb), rem = itm - le * (F * nb);
       const int f = rem / nb, i = rem - f * nb;
       const int fs = rc.fside_smem ? sFside[(c0 - e0 + le) * F + f] : a.fside[(size_t)(c0 + le) * F + f];
       if (fs < 0) continue;
@@ -557,12 +613,18 @@ __device__ void ring_apply_push(const CoopArgs<T>& a, const T* __restrict__ vj, 
 #pragma unroll
         for (int b = 0; b < NV; ++b) acc += c[b] * zz[b];
       } else if (rc.cpl_tma) {
+        // the row's NV-wide pieces in a rotated order (piece (k + i) % S at
+        // step k): neighbouring rows start in different banks
         const T* Cr = reinterpret_cast<const T*>(slot + rc.inv_cap + (size_t)(le * F + f) * rc.cpl_bytes) +
                       (size_t)i * nb;
-        for (int sp = 0; sp < S; ++sp) {
+        for (int k = 0; k < S; ++k) {
+          int sp = k + i;
+          sp = sp % S;
+          T c[NV];
+          load_row_piece<NV, T>(Cr + sp * NV, c);
           const T* zz = zs + pf[sp] * NV;
 #pragma unroll
-          for (int b = 0; b < NV; ++b) acc += Cr[sp * NV + b] * zz[b];
+          for (int b = 0; b < NV; ++b) acc += c[b] * zz[b];
         }
       } else {
         const T* Cr = a.cpl + ((size_t)tgt * nb + i) * nb;
@@ -577,28 +639,30 @@ __device__ void ring_apply_push(const CoopArgs<T>& a, const T* __restrict__ vj, 
       a.cfs[(size_t)tgt * nb + i] = acc;
     }
     named_sync(1 + g, GT);
-    if (gt == 0) {
-      // the next unit of this group, or (after the last) its first unit for
-      // the next Arnoldi iteration
-      const int nx = u + rc.nstage < nunits ? u + rc.nstage : g;
-      fence_proxy_async_smem();
-      ring_issue<T>(a, nx, e0, e1, slot, bar, sFside);
-    }
+    // release the slot to the producer (a resident ring keeps its units)
+    if (gt == 0 && !rc.resident) mbar_arrive(emptyb + slot_id);
   }
-  rs.pending = 1;
 }
 
-// before the block exits: wait (bounded) for the copies still in flight into
-// the group's slot
+// before the block exits: the producer waits (bounded) for the copies still
+// in flight into the ring (the next iteration's units it issued ahead)
 template <typename T>
-__device__ void ring_drain(const CoopArgs<T>& a, unsigned char* dsm, RingState& rs) {
-  if (!a.rc.on || !rs.pending || rs.failed) return;
-  const int g = (threadIdx.x >> 5) / a.rc.wpg;
-  if (g >= a.rc.nstage) return;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(dsm + a.rc.off_bar) + g;
-  if (!mbar_wait(bar, rs.parity)) atomicOr(a.flags + F_TMO, 1);
-  rs.parity ^= 1u;
-  rs.pending = 0;
+__device__ void ring_drain(const CoopArgs<T>& a, unsigned char* dsm, RingState& rs, int e0, int e1) {
+  // every issued copy is waited for (bounded), also after an earlier wait
+  // gave up: the block must not end with copies into its shared memory
+  if (!a.rc.on || (threadIdx.x >> 5) != NW - 1) return;
+  const int nunits = (e1 - e0 + a.rc.eps - 1) / a.rc.eps;
+  if (nunits <= 0) return;
+  uint64_t* fullb = reinterpret_cast<uint64_t*>(dsm + a.rc.off_bar);
+  // sequences consumed: it * nunits (nunits when resident and used once)
+  const long long consumed = a.rc.resident ? (rs.it > 0 ? nunits : 0) : (long long)rs.it * nunits;
+  for (long long s = consumed; s < rs.issued; ++s) {
+    const uint32_t par = a.rc.resident ? 0u : (uint32_t)((s / a.rc.nslot) & 1);
+    if (!mbar_wait(fullb + (s % a.rc.nslot), par)) {
+      if ((threadIdx.x & 31) == 0) atomicOr(a.flags + F_TMO, 1);
+      return;
+    }
+  }
 }
 
 // Element block times a vector held per element (z_e = A_e x_e) for a chunk
@@ -719,8 +783,9 @@ __device__ void gmres_solve(const CoopArgs<T>& a, const int b, const int nblk, B
   if (a.rc.fside_smem)
     for (int k = tid; k < (e1 - e0) * a.F; k += NT) sFside[k] = a.fside[(size_t)e0 * a.F + k];
   if (a.rc.on && tid == 0) {
+    // full[nslot] (armed by the producer), empty[nslot] (one consumer arrival)
     uint64_t* bars = reinterpret_cast<uint64_t*>(dsmem + a.rc.off_bar);
-    for (int g = 0; g < a.rc.nstage; ++g) mbar_init(bars + g, 1);
+    for (int k = 0; k < 2 * a.rc.nslot; ++k) mbar_init(bars + k, 1);
     fence_mbar_init();
   }
   for (int k = tid; k < a.F * a.md.Np; k += NT) sSpos[k] = a.spos[k];
@@ -909,9 +974,11 @@ template <int DIM, int NB, typename T, class Bar>
 __device__ void gmres_body(const CoopArgs<T>& a, const int b, const int nblk, Bar& grid,
                            GmresShared<T>& sm) {
   extern __shared__ __align__(128) unsigned char dsmem[];
-  RingState rs{0u, 0, 0};
+  RingState rs{0, 0, 0};
   gmres_solve<DIM, NB, T, Bar>(a, b, nblk, grid, sm, rs);
-  ring_drain<T>(a, dsmem, rs);
+  const int epb = (a.E + nblk - 1) / nblk;
+  const int e0 = min(a.E, b * epb), e1 = min(a.E, e0 + epb);
+  ring_drain<T>(a, dsmem, rs, e0, e1);
 }
 
 // kernel arguments of a solver's GMRES solve (chunk size a->ec set by the
@@ -970,25 +1037,56 @@ size_t coop_layout(CoopArgs<T>* a, int dim, int nblk) {
   const size_t inv_cap = align_up((size_t)eps * nn + 32, 16);
   const size_t slot = align_up(inv_cap + (cpl_tma ? (size_t)eps * F * cb : 0), 128);
   const int nunits = (epb + eps - 1) / eps;
-  const int nstage = (int)std::min<size_t>(std::min<size_t>(8, kRingBudget / slot), (size_t)nunits);
+  const int cap = (int)std::min<size_t>(16, kRingBudget / slot);
+  // Consumer groups: the last warp is the producer.  A streaming ring needs
+  // nslot to be a multiple of ngroup: then every use of a slot belongs to one
+  // group, which has waited for the slot's previous use before it waits for
+  // the next, so a parity wait never sees a phase two uses old (the
+  // mbarrier's parity tells only the current phase from the one before).
+  // The most groups (of at least two warps) whose multiple keeps three
+  // quarters of the slots that fit.
+  int nslot = 0, ngroup = 1;
+  for (int g = (NW - 1) / 2; g >= 1; --g) {
+    const int ns = (cap / g) * g;
+    if (ns >= 2 && 4 * ns >= 3 * cap) {
+      nslot = ns;
+      ngroup = g;
+      break;
+    }
+  }
   size_t off = 0;
-  if (ring_ok && nstage >= 2) {
+  if (ring_ok && nslot >= 2) {
     rc.on = 1;
-    rc.nstage = nstage;
+    rc.resident = nunits <= cap ? 1 : 0;
+    if (rc.resident) {
+      // every unit has its slot, used once: any grouping is safe
+      nslot = nunits;
+      ngroup = (NW - 1) / 2;
+    }
+    rc.nslot = nslot;
     rc.eps = eps;
-    rc.wpg = NW / nstage;
+    rc.ngroup = ngroup;
+    rc.wpg = (NW - 1) / ngroup;
     rc.cpl_tma = cpl_tma;
     rc.slot_bytes = (int)slot;
     rc.inv_cap = (int)inv_cap;
     rc.cpl_bytes = (int)cb;
     rc.off_ring = 0;
-    off = (size_t)nstage * slot;
+    off = (size_t)rc.nslot * slot;
     rc.off_bar = (int)off;
-    off += align_up((size_t)nstage * 8, 16);
+    off += align_up((size_t)2 * rc.nslot * 8, 16);
     rc.off_z = (int)off;
-    off += align_up((size_t)nstage * eps * n * es, 16);
-    rc.off_v = (int)off;
-    off += align_up((size_t)nstage * eps * n * es, 16);
+    off += align_up((size_t)rc.ngroup * eps * n * es, 16);
+    const size_t vj_bytes = align_up((size_t)epb * n * es, 16);
+    if (vj_bytes <= 24 * 1024) {
+      rc.vj_smem = 1;
+      rc.off_vj = (int)off;
+      off += vj_bytes;
+      rc.off_v = rc.off_vj;  // per-unit staging not used
+    } else {
+      rc.off_v = (int)off;
+      off += align_up((size_t)rc.ngroup * eps * n * es, 16);
+    }
   }
   rc.off_red = (int)off;
   off += align_up((size_t)NW * 33 * es, 16);
