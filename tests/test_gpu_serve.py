@@ -172,8 +172,11 @@ def test_preempted_request_resumes_bitwise(gpu_lib):
     p=3) is stopped after its p=1 level, its state goes to host memory, the
     other requests run on the single slot, and it resumes from the snapshot;
     its final state and functional are bitwise those of the same request
-    solved without interruption."""
+    solved without interruption.  All three arrive at once, so request 0
+    re-enters the queue behind the other two and finishes last."""
     reqs = _requests()[:3]
+    for r in reqs:
+        r.arrival = 0.0    # all queued when request 0 stops
     srv = serve.SteadySolveServer(8 << 30, slots=1, precision=1)
     srv.preempt(0)
     out = srv.serve(reqs)
