@@ -59,16 +59,21 @@ int launch_T(eg_ls* ls) {
   // grid: one block for a small system (a one-block grid is resident or not
   // at all, so several run side by side on other streams); otherwise up to
   // one block per SM with at least 32 elements each, one such grid at a time
+  const size_t elem_bytes = (size_t)a.n * sizeof(T);
   const size_t op_bytes = (size_t)m->E * a.n * a.n * sizeof(T);
   int nblk = op_bytes <= kSmallOperatorBytes ? 1 : std::max(2, std::min(sms, (m->E + 31) / 32));
   if (ls->coop_grid > 0) nblk = std::min(ls->coop_grid, sms);
   if (nblk > m->E) nblk = m->E;
   if (nblk > EG_COOP_MAX_BLOCKS) nblk = EG_COOP_MAX_BLOCKS;
-  const size_t smem = coop_layout<T>(&a, m->dim, nblk);
-  // the limit above the default 48 KB of dynamic shared memory: one value for
-  // every launch (threads of other meshes launch this kernel concurrently,
-  // and the attribute is shared by all of them)
-  EG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax));
+  const int epb = (m->E + nblk - 1) / nblk;
+  int ec = (int)((40 * 1024) / elem_bytes);
+  if (ec < 1) ec = 1;
+  if (ec > epb) ec = epb;
+  a.ec = ec;
+  const size_t smem = (size_t)ec * elem_bytes;
+  // the default dynamic limit is 48 KB minus the kernel's static shared
+  // memory (11.6 KB in FP64), below the chunk size above
+  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, NT, smem);
   if (per_sm < 1 || nblk <= 0) {
     eg_set_error("persistent GMRES kernel cannot be resident");
@@ -99,7 +104,7 @@ int eg_gmres_coop(eg_ls* ls) {
 
 bool eg_coop_usable(const eg_ls* ls) {
   const eg_mesh* m = ls->lo->mesh;
-  return ls->lo->nb <= NB_MAX && m->F * m->S <= 64 && m->F * m->Np <= 128 && m->I > 0 &&
+  return ls->lo->nb <= NB_MAX && m->F == m->dim + 1 && m->F * m->S <= 64 && m->F * m->Np <= 128 && m->I > 0 &&
          eg_coop_supported();
 }
 

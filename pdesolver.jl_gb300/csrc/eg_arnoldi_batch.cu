@@ -211,16 +211,16 @@ int launch_batch(Batcher& B, const std::vector<Submission*>& batch, int dev) {
     const eg_ls* ls = batch[i]->ls;
     const eg_mesh* m = ls->lo->mesh;
     const int n = ls->lo->n;
-    // the layout the staged arguments carry (stage_args, same block count)
-    CoopArgs<T> tmp;
-    coop_args<T>(ls, &tmp);
-    smem = std::max(smem, coop_layout<T>(&tmp, m->dim, nb[i]));
-    list.e[i] = BatchEntry{ls->dargs, b0, nb[i], kind_of(m->dim, n), tmp.ec};
+    const int epb = (m->E + nb[i] - 1) / nb[i];
+    const size_t elem_bytes = (size_t)n * sizeof(T);
+    int ec = (int)((40 * 1024) / elem_bytes);
+    ec = std::max(1, std::min(ec, epb));
+    smem = std::max(smem, (size_t)ec * elem_bytes);
+    list.e[i] = BatchEntry{ls->dargs, b0, nb[i], kind_of(m->dim, n), ec};
     b0 += nb[i];
   }
   const void* fn = (const void*)k_gmres_batch<T>;
-  // one limit for every launch (several leader threads launch this kernel)
-  EG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax));
+  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, NT, smem);
   if (per_sm < 1 || b0 > sms * per_sm) {
@@ -254,9 +254,7 @@ int stage_args(eg_ls* ls) {
   }
   // the staging buffer is the solver's own and its previous copy has
   // completed (every Newton iteration synchronises the mesh stream)
-  CoopArgs<T>* ha = reinterpret_cast<CoopArgs<T>*>(ls->hargs);
-  coop_args<T>(ls, ha);
-  coop_layout<T>(ha, m->dim, eg_gmres_wanted_blocks(ls));
+  coop_args<T>(ls, reinterpret_cast<CoopArgs<T>*>(ls->hargs));
   EG_CUDA(cudaMemcpyAsync(ls->dargs, ls->hargs, sizeof(CoopArgs<T>), cudaMemcpyHostToDevice, m->stream));
   EG_CUDA(cudaEventRecord(ls->ev_in, m->stream));
   return EG_OK;

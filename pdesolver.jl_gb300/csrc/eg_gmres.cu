@@ -636,10 +636,6 @@ int gmres_T(eg_ls* ls, eg_ls_stats* st, int transpose) {
     EG_CUDA(cudaStreamSynchronize(m->stream));
     std::memcpy(scal, ls->hh, sizeof(scal));
     std::memcpy(flags, ls->hh + 8, sizeof(flags));
-    if (flags[F_TMO]) {
-      eg_set_error("GMRES: a bounded wait on the operator copies gave up");
-      return EG_ERR_TIMEOUT;
-    }
     if (!std::isfinite(scal[S_BETA])) {
       eg_set_error("GMRES: non-finite residual");
       return EG_ERR_NONFINITE;

@@ -911,9 +911,7 @@ extern "C" int eg_pc_create(eg_lo* lo, eg_pc** out) {
   pc->lo = lo;
   pc->valid = false;
   const size_t es = lo->prec == EG_F64 ? 8 : 4;
-  // 256 bytes beyond the blocks: the persistent GMRES kernel copies the
-  // inverse blocks in 16-byte aligned ranges that may round past the last one
-  cudaError_t e = cudaMalloc(&pc->inv, es * (size_t)lo->mesh->E * lo->n * lo->n + 256);
+  cudaError_t e = cudaMalloc(&pc->inv, es * (size_t)lo->mesh->E * lo->n * lo->n);
   if (e != cudaSuccess) {
     delete pc;
     return eg_cuda_fail(e, "eg_pc_create");

@@ -393,11 +393,6 @@ IterOut newton_graph_iteration(eg_mesh* m, eg_newton_ws* w, double tau_l) {
   std::memcpy(flags, ls->hh + 8, sizeof(flags));
   r.kits = flags[F_ITS];
   r.kconv = flags[F_CONV];
-  if (flags[F_TMO]) {
-    eg_set_error("GMRES: a bounded wait on the operator copies gave up");
-    r.st = EG_ERR_TIMEOUT;
-    return r;
-  }
   r.step = m->h_red[1];
   r.norm = m->h_red[0];
   const unsigned int status = *m->h_status;
