@@ -258,7 +258,7 @@ typedef struct {
   int32_t iters;        /* total Krylov iterations                          */
   int32_t restarts;
   int32_t converged;    /* 1 if ||b - A x|| <= max(reltol ||b||, abstol)     */
-  int32_t reserved;
+  int32_t reorth;       /* Arnoldi steps that took a second Gram-Schmidt pass */
   double res0;          /* ||b - A x0||                                     */
   double res_final;     /* final (estimated) residual norm                  */
 } eg_ls_stats;

@@ -387,7 +387,7 @@ struct GmresShared {
   T scs[32], ssn[32], sg[33], sHc[33], syT[33];
   T sR[32 * 33];  // rotated Hessenberg columns: sR[j * (m+1) + k]
   double sy[33], sdi[33];
-  int s_done, s_its, s_reorth, s_jdone, s_conv, s_cycles;
+  int s_done, s_its, s_reorth, s_jdone, s_conv, s_cycles, s_nreorth;
   T s_beta;
   double s_tol, s_bnorm;
 };
@@ -408,7 +408,12 @@ struct GridBarrier {
 //   * cycle start: r = b - J x (element blocks D and the face push), beta =
 //     |r|, converged when beta <= max(reltol |b|, abstol) (the true residual),
 //     v_0 = r / beta;
-//   * Arnoldi on J M^-1 = I + C D^-1: classical Gram-Schmidt with the norm of
+//   * Arnoldi on K = C D^-1 (the coupling part of J M^-1 = I + K): the Krylov
+//     spaces of K and I + K are the same, and K V_j = V_{j+1} H_K gives
+//     (I + K) V_j = V_{j+1} (H_K + I), so the vectors are orthogonalised
+//     without the v_j term that I adds (which would only be subtracted again,
+//     with its cancellation) and the identity is added to the Hessenberg
+//     column's diagonal; classical Gram-Schmidt with the norm of
 //     the orthogonalised vector from the same reduction (|w'|^2 = w.w -
 //     |h|^2) and a second classical pass (its reduction also yields w'.w')
 //     when |w'|^2 < |w|^2 / 2 (DGKS with eta = 1/sqrt 2); Givens rotations in
@@ -456,6 +461,7 @@ __device__ void gmres_body(const CoopArgs<T>& a, const int b, const int nblk, Ba
   int& s_jdone = sm.s_jdone;
   int& s_conv = sm.s_conv;
   int& s_cycles = sm.s_cycles;
+  int& s_nreorth = sm.s_nreorth;
   T& s_beta = sm.s_beta;
   double& s_tol = sm.s_tol;
   double& s_bnorm = sm.s_bnorm;
@@ -471,6 +477,7 @@ __device__ void gmres_body(const CoopArgs<T>& a, const int b, const int nblk, Ba
     s_tol = fmax(a.scal[S_RELTOL] * s_bnorm, a.scal[S_ABSTOL]);
     s_its = 0;
     s_cycles = 0;
+    s_nreorth = 0;
   }
   __syncthreads();
   for (;;) {
@@ -519,13 +526,13 @@ __device__ void gmres_body(const CoopArgs<T>& a, const int b, const int nblk, Ba
         chunk_apply_push<DIM, NB, T>(a, a.inv, vj, true, sZ, sPerm, c0, nl, nullptr);
       }
       if (!grid.sync()) return;
-      // (2) w = v_j + the pushed products of the faces holding the row's node
+      // (2) w = K v_j: the pushed products of the faces holding the row's node
       for (int t = tid; t < nrow; t += NT) {
         const int le = t / n, r = t - le * n;
         const int jn = r / NV, av = r - jn * NV;
         const int e = e0 + le;
         const int64_t row = (int64_t)e * n + r;
-        a.w[row] = gather_pushed<DIM, NV, T>(a, sSpos, e, jn, av, vj[row]);
+        a.w[row] = gather_pushed<DIM, NV, T>(a, sSpos, e, jn, av, T(0));
       }
       __syncthreads();
       // (3) first pass: h1 = V^T w and w.w in one reduction
@@ -539,6 +546,7 @@ __device__ void gmres_body(const CoopArgs<T>& a, const int b, const int nblk, Ba
         const T ww = sh1[j + 1];
         const T n2 = ww - hh;
         s_reorth = n2 < T(0.5) * ww;
+        s_nreorth += s_reorth;
         sh2[32] = n2;  // |w'|^2
       }
       __syncthreads();
@@ -564,6 +572,7 @@ __device__ void gmres_body(const CoopArgs<T>& a, const int b, const int nblk, Ba
       //     every block); warps 1.. : v_{j+1} = (w - V h) / hn
       if (tid == 0) {
         for (int k = 0; k <= j; ++k) sHc[k] = s_reorth ? sh1[k] + sh2[k] : sh1[k];
+        sHc[j] += T(1);  // column j of H_K + I, the Hessenberg matrix of I + K
         sHc[j + 1] = hn;
         for (int k = 0; k < j; ++k) {
           const T t0 = scs[k] * sHc[k] + ssn[k] * sHc[k + 1];
@@ -628,6 +637,7 @@ __device__ void gmres_body(const CoopArgs<T>& a, const int b, const int nblk, Ba
     a.flags[F_DONE] = 1;
     a.flags[F_CONV] = s_conv;
     a.flags[F_CYCLES] = s_cycles;
+    a.flags[F_NREORTH] = s_nreorth;
     a.scal[S_BETA] = double(s_beta);
     a.scal[S_RESID] = double(s_beta);
     a.scal[S_BNORM] = s_bnorm;

@@ -197,6 +197,7 @@ __global__ void k_gm_reorth_check(int j, const T* __restrict__ h1, const T* __re
   for (int k = 0; k <= j; ++k) before += double(h1[k]) * double(h1[k]);
   const int need = double(hn[0]) * double(hn[0]) < 0.5 * before;
   flags[F_REORTH] = need;
+  flags[F_NREORTH] += need;
   if (!need)
     for (int k = 0; k <= j; ++k) h2[k] = T(0);
 }
@@ -432,6 +433,7 @@ __global__ void __launch_bounds__(256) k_gm_sub2(const T* __restrict__ V, const 
       if (pass == 1) {
         const int need2 = n2 < 0.5 * double(ww[0]);
         flags[F_REORTH] = need2;
+        flags[F_NREORTH] += need2;
         if (!need2) gm_givens_core<T>(j, m, h1, nullptr, sqrt(n2), dH, flags, scal);
       } else {
         gm_givens_core<T>(j, m, h1, h2, sqrt(n2), dH, flags, scal);
@@ -644,6 +646,7 @@ int gmres_T(eg_ls* ls, eg_ls_stats* st, int transpose) {
       st->iters = flags[F_ITS];
       st->restarts = flags[F_CYCLES];
       st->converged = flags[F_CONV];
+      st->reorth = flags[F_NREORTH];
       st->res0 = scal[S_BETA0];
       st->res_final = scal[S_BETA];
     }
@@ -715,6 +718,7 @@ int gmres_T(eg_ls* ls, eg_ls_stats* st, int transpose) {
     st->iters = flags[F_ITS];
     st->restarts = restarts;
     st->converged = flags[F_CONV];
+    st->reorth = flags[F_NREORTH];
     st->res0 = res0;
     st->res_final = scal[S_BETA];
   }

@@ -75,7 +75,7 @@ struct eg_ls {
 };
 void eg_gmres_release(eg_ls* ls);
 // slots of the device GMRES state: dflags[] and dscal[]
-enum { F_DONE = 0, F_JDONE = 1, F_ITS = 2, F_CONV = 3, F_ITERMAX = 4, F_REORTH = 5, F_CYCLES = 6 };
+enum { F_DONE = 0, F_JDONE = 1, F_ITS = 2, F_CONV = 3, F_ITERMAX = 4, F_REORTH = 5, F_CYCLES = 6, F_NREORTH = 7 };
 enum { S_TOL = 0, S_RESID = 1, S_BETA = 2, S_BNORM = 3, S_RELTOL = 4, S_ABSTOL = 5, S_BETA0 = 6 };
 // the whole GMRES solve as one persistent cooperative kernel (eg_arnoldi.cu)
 #define EG_COOP_MAX_BLOCKS 1024

@@ -98,7 +98,7 @@ def _declare(lib):
 
 class LsStats(C.Structure):
     _fields_ = [("iters", C.c_int32), ("restarts", C.c_int32), ("converged", C.c_int32),
-                ("reserved", C.c_int32), ("res0", C.c_double), ("res_final", C.c_double)]
+                ("reorth", C.c_int32), ("res0", C.c_double), ("res_final", C.c_double)]
 
 
 class NewtonOpts(C.Structure):

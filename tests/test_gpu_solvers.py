@@ -136,6 +136,7 @@ def test_gmres_solves(gpu_lib, precision, tol):
     x = np.zeros_like(b)
     st = ls.solve(b, x)
     assert st.converged == 1
+    assert 0 <= st.reorth <= st.iters
     lo64 = eulergpu.LinearOperator(g, precision=0)
     lo64.calc(q)
     r = b - lo64.apply(x, np.zeros_like(x))
