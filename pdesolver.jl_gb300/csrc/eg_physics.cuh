@@ -126,6 +126,20 @@ __host__ __device__ __forceinline__ float val(float a) { return a; }
 using ::sqrt;
 using ::log;
 
+// 1/sqrt(x): CUDA's rsqrt (double) / rsqrtf (float); for a derivative
+// carrier d(x^-1/2) = -x^-3/2 dx / 2
+__device__ __forceinline__ double rsqrt_(double a) { return ::rsqrt(a); }
+__device__ __forceinline__ float rsqrt_(float a) { return ::rsqrtf(a); }
+template <typename R, int N>
+__device__ __forceinline__ Fwd<R, N> rsqrt_(const Fwd<R, N>& a) {
+  Fwd<R, N> r;
+  r.v = rsqrt_(a.v);
+  const R dr = R(-0.5) * r.v * r.v * r.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * dr;
+  return r;
+}
+
 // real (non-derivative) type of a scalar
 template <typename T> struct RealOf { using type = T; };
 template <typename R, int N> struct RealOf<Fwd<R, N>> { using type = R; };
@@ -171,9 +185,13 @@ __device__ __forceinline__ void euler_flux(const Gas& g, const T* q, const Tn* d
 }
 
 // Roe flux: F(qL).n + 0.5 (|A_hat| - A_hat)(qL - qR), eigenvalue floors 0.025.
-// Arranged to spend few divisions (FP64 is the scarce resource on GB300): one
-// reciprocal per state density, 1/(sqL+sqR), 1/(n.n), 1/(H - phi) (= gami/a^2)
-// and 1/(dA a); the Euler flux of qL reuses 1/rho_L.
+// Arranged to spend one division (FP64 is the scarce resource on GB300):
+// 1/(sqL + sqR).  Four reciprocal square roots give the rest:
+//   s = rho^-1/2 of each state: sqrt(rho) = rho s and 1/rho = s^2;
+//   rn = |n|^-1: |n| = n.n rn and 1/|n|^2 = rn^2;
+//   ia = 1/a with a^2 = gami (H - phi): a = a^2 ia, 1/(H - phi) = gami ia^2
+//   and 1/(|n| a) = rn ia.
+// The Euler flux of qL reuses 1/rho_L.
 template <int DIM, typename T, typename Tn>
 __device__ __forceinline__ void roe_flux(const Gas& g, const T* q, const T* qg, const Tn* nrm, T* flux) {
   using R = typename RealOf<T>::type;
@@ -181,18 +199,20 @@ __device__ __forceinline__ void roe_flux(const Gas& g, const T* q, const T* qg, 
   const R gamma = R(g.gamma), gami = R(g.gamma_1), h = R(0.5), one = R(1);
   const R sat_V = R(0.025);
   // Roe averages
-  const T rL = one / q[0];
+  const T isL = rsqrt_(q[0]);
+  const T rL = isL * isL;
   T uL = q[1] * rL, vL = q[2] * rL;
   T wL = (DIM == 3) ? q[3] * rL : T(R(0));
   T phiL = h * (uL * uL + vL * vL + wL * wL);
   T HL = gamma * q[NV - 1] * rL - gami * phiL;
-  const T rR = one / qg[0];
+  const T isR = rsqrt_(qg[0]);
+  const T rR = isR * isR;
   T uR = qg[1] * rR, vR = qg[2] * rR;
   T wR = (DIM == 3) ? qg[3] * rR : T(R(0));
   T phiR = h * (uR * uR + vR * vR + wR * wR);
   T HR = gamma * qg[NV - 1] * rR - gami * phiR;
-  T sqL = sqrt(q[0]);
-  T sqR = sqrt(qg[0]);
+  T sqL = q[0] * isL;
+  T sqR = qg[0] * isR;
   T fac = one / (sqL + sqR);
   T u = (sqL * uL + sqR * uR) * fac;
   T v = (sqL * vL + sqR * vR) * fac;
@@ -205,11 +225,14 @@ __device__ __forceinline__ void roe_flux(const Gas& g, const T* q, const T* qg, 
   Tn nx = nrm[0], ny = nrm[1];
   Tn nz = (DIM == 3) ? nrm[2] : Tn(0);
   Tn n2 = nx * nx + ny * ny + nz * nz;
-  Tn dA = sqrt(n2);
+  Tn rn = rsqrt_(n2);
+  Tn dA = n2 * rn;
   T Un = u * nx + v * ny + w * nz;
   T phi = h * (u * u + v * v + w * w);
   T Hp = H - phi;
-  T a = sqrt(gami * Hp);
+  T a2 = gami * Hp;
+  T ia = rsqrt_(a2);
+  T a = a2 * ia;
   T dAa = dA * a;
   T lambda1 = Un + dAa;
   T lambda2 = Un - dAa;
@@ -227,9 +250,9 @@ __device__ __forceinline__ void roe_flux(const Gas& g, const T* q, const T* qg, 
     dqN = -Un * dq[0] + nx * dq[1] + ny * dq[2] + nz * dq[3];
   }
   T t1 = h * (lambda1 + lambda2) - lambda3;
-  T t2 = one / Hp;                 // gami / a^2
-  Tn t3 = Tn(1) / n2;              // 1 / dA^2
-  T t4 = h * (lambda1 - lambda2) / dAa;
+  T t2 = gami * ia * ia;           // 1 / (H - phi) = gami / a^2
+  Tn t3 = rn * rn;                 // 1 / dA^2
+  T t4 = h * (lambda1 - lambda2) * (rn * ia);  // / (dA a)
   // sat = l3 dq + t1 (t2 E1dq + t3 E2dq) + t4 (E3dq + gami E4dq)
   T c1 = t1 * t2 * dqE + t4 * dqN;        // coefficient of (1, u, v, w, H)
   T c2 = t1 * t3 * dqN + t4 * gami * dqE; // coefficient of (0, nx, ny, nz, Un)
@@ -343,15 +366,21 @@ struct IRNode {
   double z1, zp, lz1, lzp, u, v, w;
 };
 
-template <int DIM>
+template <int DIM, bool LOGS = true>
 __device__ __forceinline__ IRNode<DIM> ir_node(const Gas& g, const double* q) {
   IRNode<DIM> r;
   const double p = pressure<DIM>(g, q);
-  const double rinv = 1.0 / q[0];
-  r.z1 = sqrt(q[0] / p);
-  r.zp = sqrt(q[0] * p);
-  r.lz1 = log(r.z1);
-  r.lzp = log(r.zp);
+  // t = (rho p)^-1/2: sqrt(rho/p) = rho t, sqrt(rho p) = rho p t, 1/rho = p t^2
+  const double t = rsqrt_(q[0] * p);
+  const double rinv = p * t * t;
+  r.z1 = q[0] * t;
+  r.zp = q[0] * p * t;
+  if (LOGS) {
+    r.lz1 = log(r.z1);
+    r.lzp = log(r.zp);
+  } else {
+    r.lz1 = r.lzp = 0.0;
+  }
   r.u = q[1] * rinv;
   r.v = q[2] * rinv;
   r.w = (DIM == 3) ? q[3] * rinv : 0.0;
@@ -368,7 +397,8 @@ __device__ __forceinline__ IRNode<DIM> ir_node(const Gas& g, const double* q) {
 // with G = 1/F as its series 1 - u/3 - 4u^2/45 - 44u^3/945 - 428u^4/14175
 // (|G F - 1| < 5e-16 for u < 1e-3), and in the logarithmic branch
 //   1/L = (lL - lR)/d,  L = d^2 x and 1/L = (lL - lR)^2 x with x = 1/(d (lL - lR)).
-// A pair then costs two divisions on the series branch (1/s_1, 1/s_p).
+// A pair costs one division on the series branch: x = 1/(s_1 s_p) gives
+// 1/s_1 = s_p x and 1/s_p = s_1 x.
 __device__ __forceinline__ double logmean_F(double u) {
   return 1.0 + u * (1.0 / 3.0 + u * (1.0 / 5.0 + u * (1.0 / 7.0 + u * (1.0 / 9.0))));
 }
@@ -376,32 +406,37 @@ __device__ __forceinline__ double logmean_G(double u) {
   return 1.0 - u * (1.0 / 3.0 + u * (4.0 / 45.0 + u * (44.0 / 945.0 + u * (428.0 / 14175.0))));
 }
 
-// Ismail-Roe averages of two nodes from their precomputed quantities
-template <int DIM>
+// Ismail-Roe averages of two nodes from their per-node quantities.  PRE: the
+// nodes carry their logarithms (computed once per node, for the pairs of an
+// element); otherwise the logarithm of the ratio is taken on the log-mean
+// branch only (a face node pairs each state once).
+template <int DIM, bool PRE = true>
 __device__ __forceinline__ IRAvg<DIM, double> ir_average_pre(const Gas& g, const IRNode<DIM>& L,
                                                              const IRNode<DIM>& R) {
   const double gamma = g.gamma, gamma_1 = g.gamma_1;
   IRAvg<DIM, double> r;
-  // sqrt(rho/p): r1 = 1/(z1L + z1R) is also the weight of the velocity averages
+  // sqrt(rho/p): r1 = 1/(z1L + z1R) is also the weight of the velocity averages;
+  // one division for 1/s1 and 1/sp
   const double s1 = L.z1 + R.z1, d1 = L.z1 - R.z1;
-  const double r1 = 1.0 / s1;
+  const double sp = L.zp + R.zp, dp = L.zp - R.zp;
+  const double x1p = 1.0 / (s1 * sp);
+  const double r1 = sp * x1p;
   double inv_l1;
   if (d1 * d1 < 1e-3 * (s1 * s1)) {
     const double f = d1 * r1;
     inv_l1 = 2.0 * logmean_F(f * f) * r1;
   } else {
-    inv_l1 = (L.lz1 - R.lz1) / d1;
+    inv_l1 = (PRE ? L.lz1 - R.lz1 : log(L.z1 / R.z1)) / d1;
   }
   // sqrt(rho p)
-  const double sp = L.zp + R.zp, dp = L.zp - R.zp;
   double lp, inv_lp;
   if (dp * dp < 1e-3 * (sp * sp)) {
-    const double rp = 1.0 / sp;
+    const double rp = s1 * x1p;
     const double f = dp * rp, u = f * f;
     lp = 0.5 * sp * logmean_G(u);
     inv_lp = 2.0 * logmean_F(u) * rp;
   } else {
-    const double dl = L.lzp - R.lzp;
+    const double dl = PRE ? L.lzp - R.lzp : log(L.zp / R.zp);
     const double x = 1.0 / (dp * dl);
     lp = dp * dp * x;
     inv_lp = dl * dl * x;

@@ -63,7 +63,11 @@ __global__ void k_face_flux(DevMesh md, const double* __restrict__ q, double* __
     if (md.face_flux == EG_FLUX_ROE) {
       eg::roe_flux<DIM>(g, qL, qR, nrm, fl);
     } else {
-      auto av = eg::ir_average<DIM>(g, qL, qR);
+      // per-side square roots from one rsqrt each, logarithms only on the
+      // log-mean branch
+      const auto nL = eg::ir_node<DIM, false>(g, qL);
+      const auto nR = eg::ir_node<DIM, false>(g, qR);
+      const auto av = eg::ir_average_pre<DIM, false>(g, nL, nR);
       eg::ir_dir<DIM>(av, nrm, fl);
     }
   } else {
