@@ -1272,6 +1272,22 @@ def run_kernels_only(args, which):
         out["launches_each"] = args.steps
         print(json.dumps(out), flush=True)
         return
+    if which == "flux":
+        # the flux kernels' instruction counts: a small C2 weak-form case
+        # (Roe, 32 x 32 annulus, SBP-Gamma p=3) and a small C3 split-form case
+        # (IR, 8^3 x 6 warped tets, diagonal-E p=2), default launch shapes
+        for ms_k, opts_k, q_k in (problems.config2(n=32, p=3), problems.config3(n=8)):
+            gk = eulergpu.GPUMesh(ms_k, opts_k)
+            gk.set_stream(stream.cuda_stream)
+            qd = torch.from_numpy(q_k).cuda()
+            rd = torch.zeros_like(qd)
+            for _ in range(args.steps):
+                gk.eval_residual_async(qd, rd)
+            torch.cuda.synchronize()
+        out["kernels"] = ["k_face_flux<2>", "k_element<2,0>", "k_face_flux<3>", "k_split_element<3>"]
+        out["launches_each"] = args.steps
+        print(json.dumps(out), flush=True)
+        return
     if which == "blockinv":
         # block-Jacobi inverses: the C2 p=3 operator (48 unknowns per block) and
         # the warped 8^3 x 6 cube with diagonal-E p=2 tets (115 unknowns)
@@ -1348,7 +1364,8 @@ def main():
     ap.add_argument("--probe", type=int, default=32, help="c5: requests of the capacity probe")
     ap.add_argument("--fp64-stream", default="auto", choices=["auto", "on", "off"],
                     help="c5: also serve the stream with the FP64 server (auto: up to 300 requests)")
-    ap.add_argument("--only", default=None, choices=["krylov", "residual", "gmres", "split", "blockinv"],
+    ap.add_argument("--only", default=None, choices=["krylov", "residual", "gmres", "split", "blockinv",
+                                                     "flux"],
                     help="run only the isolated kernels (for profiler captures)")
     args = ap.parse_args()
     if args.only:
