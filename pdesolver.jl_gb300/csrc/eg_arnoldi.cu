@@ -23,7 +23,8 @@
 // Per Arnoldi iteration: 2 grid barriers (3 with the second Gram-Schmidt
 // pass); per restart: 2 more (residual push, residual norm).
 // The operator is the right-preconditioned J M^-1 = I + C D^-1 (element blocks
-// cancel with their inverses).
+// cancel with their inverses); the Arnoldi vectors are built from K = C D^-1
+// and the identity is added to the Hessenberg diagonal.
 #include <algorithm>
 #include <cmath>
 #include <mutex>

@@ -238,6 +238,7 @@ __device__ void gm_givens_core(int j, int m, const T* h1, const T* h2, double hn
   double* g = sn + m;
   double* Hc = H + (size_t)j * (m + 1);
   for (int k = 0; k <= j; ++k) Hc[k] = double(h1[k]) + (h2 ? double(h2[k]) : 0.0);
+  Hc[j] += 1.0;  // column j of H_K + I: the Arnoldi vectors come from K = C D^-1
   Hc[j + 1] = hn;
   for (int k = 0; k < j; ++k) {
     const double t0 = cs[k] * Hc[k] + sn[k] * Hc[k + 1];
@@ -537,15 +538,17 @@ void enqueue_arnoldi(eg_ls* ls) {
   const int* fl = ls->dflags;
   for (int j = 0; j < mm; ++j) {
     T* vj = V + (size_t)j * N;
-    // w = J M^-1 v_j = v_j + C (D^-1 v_j): the element blocks cancel with
-    // their inverses, so only the coupling blocks are read here (transposed:
-    // w = J^T M^-T v_j = v_j + C^T (D^-T v_j))
+    // J M^-1 = I + K with K = C D^-1: the element blocks cancel with their
+    // inverses.  Arnoldi runs on K (same Krylov space; (I + K) V_j =
+    // V_{j+1} (H_K + I), the identity added in the Givens step), so
+    // w = K v_j = C (D^-1 v_j) without the v_j term (transposed:
+    // w = C^T (D^-T v_j))
     if (ls->trans) {
       eg_pc_apply_t_T(ls->pc, vj, z, fl);
-      eg_cpl_apply_t_T(ls->lo, vj, z, w, fl);
+      eg_cpl_apply_t_T(ls->lo, nullptr, z, w, fl);
     } else {
       eg_pc_apply_T(ls->pc, vj, z, fl);
-      eg_cpl_apply_T(ls->lo, vj, z, w, fl);
+      eg_cpl_apply_T(ls->lo, nullptr, z, w, fl);
     }
     // classical Gram-Schmidt (with |w|^2 before, for the DGKS test), a second
     // pass only when the test asks, Givens on the device

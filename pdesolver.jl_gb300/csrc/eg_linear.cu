@@ -49,6 +49,7 @@ __global__ void k_spmv(DevMesh md, const T* __restrict__ diag, const T* __restri
 // Right-preconditioned operator without the element blocks:
 // (D + C) D^-1 v = v + C z with z = D^-1 v (z computed by k_block_apply).
 // Inside the Arnoldi loop this replaces k_spmv + the diagonal-block read.
+// v == nullptr: w = C z alone (the coupling part K v of I + K).
 template <int DIM, typename T>
 __global__ void k_cpl_apply(DevMesh md, const T* __restrict__ cpl, const int* __restrict__ spos,
                             const T* __restrict__ v, const T* __restrict__ z, T* __restrict__ w,
@@ -60,7 +61,7 @@ __global__ void k_cpl_apply(DevMesh md, const T* __restrict__ cpl, const int* __
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N;
        t += (int64_t)gridDim.x * blockDim.x) {
     const int e = (int)(t / n), r = (int)(t - (int64_t)e * n);
-    w[t] = v[t] + coupling_row<DIM, T>(md, cpl, spos, z, e, r, n);
+    w[t] = (v ? v[t] : T(0)) + coupling_row<DIM, T>(md, cpl, spos, z, e, r, n);
   }
 }
 
@@ -398,7 +399,8 @@ __global__ void k_spmv_t(DevMesh md, const T* __restrict__ diag, const T* __rest
 
 // w = v + C^T z: the transposed right-preconditioned operator
 // J^T M^-T v = (M^-1 J)^T v = v + C^T D^-T v with z = D^-T v (the element
-// blocks cancel with their inverses), coupling blocks only
+// blocks cancel with their inverses), coupling blocks only; v == nullptr:
+// w = C^T z alone
 template <int DIM, typename T>
 __global__ void k_cpl_apply_t(DevMesh md, const T* __restrict__ cpl, const int* __restrict__ spos,
                               const T* __restrict__ v, const T* __restrict__ z, T* __restrict__ w, int n,
@@ -407,7 +409,7 @@ __global__ void k_cpl_apply_t(DevMesh md, const T* __restrict__ cpl, const int* 
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= (int64_t)md.E * n) return;
   const int e = (int)(t / n), r = (int)(t - (int64_t)e * n);
-  w[t] = v[t] + coupling_col<DIM, T>(md, cpl, spos, z, e, r, n);
+  w[t] = (v ? v[t] : T(0)) + coupling_col<DIM, T>(md, cpl, spos, z, e, r, n);
 }
 
 // y = M^-T x (applyPCTranspose, LinearSolvers.jl:277): the transposed element
