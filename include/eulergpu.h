@@ -271,11 +271,13 @@ int eg_ls_create(eg_lo* lo, eg_pc* pc, int32_t restart, eg_ls** out);
 int eg_ls_destroy(eg_ls* ls);
 /* setTolerances (ls_standard.jl); negative values leave a field unchanged */
 int eg_ls_set_tolerances(eg_ls* ls, double reltol, double abstol, double dtol, int32_t itermax);
-/* Blocks of the persistent GMRES kernel (one per SM at most; 0 restores the
-   automatic choice: one block for operators of at most 2 MB, else up to one
-   block per SM with at least 32 elements each).  A tuning knob with no
-   reference counterpart; the result does not depend on it beyond the order of
-   the FP reductions. */
+/* Blocks of the persistent GMRES kernel (one per SM at most, as a
+   cooperative grid; 0 restores the automatic choice: one thread-block
+   cluster of 16 blocks (8 where 16 cannot be placed) for operators of at
+   most 2 MB or systems of at most 16 x 32 elements, else up to one block per
+   SM with at least 32 elements each).  A tuning knob with no reference
+   counterpart; the result does not depend on it beyond the order of the FP
+   reductions. */
 int eg_ls_set_grid(eg_ls* ls, int32_t blocks);
 /* Batched persistent GMRES (process-wide switch; no reference counterpart).
    When enabled, the multi-block Krylov solves that threads reach within

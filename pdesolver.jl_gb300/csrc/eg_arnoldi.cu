@@ -21,7 +21,9 @@
 //     no broadcast is needed and all blocks take the same branches (no
 //     barrier can be missed).
 // Per Arnoldi iteration: 2 grid barriers (3 with the second Gram-Schmidt
-// pass); per restart: 2 more (residual push, residual norm).
+// pass); per restart: 2 more (residual push, residual norm).  A system whose
+// element blocks take at most 2 MB, or whose grid would have at most 16
+// blocks, runs on one thread-block cluster instead (eg_arnoldi_cluster.cu).
 // The operator is the right-preconditioned J M^-1 = I + C D^-1 (element blocks
 // cancel with their inverses); the Arnoldi vectors are built from K = C D^-1
 // and the identity is added to the Hessenberg diagonal.
@@ -57,11 +59,28 @@ int launch_T(eg_ls* ls) {
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  // grid: one block for a small system (a one-block grid is resident or not
-  // at all, so several run side by side on other streams); otherwise up to
-  // one block per SM with at least 32 elements each, one such grid at a time
+  // grid: one cluster for a small system (its blocks are co-scheduled, so
+  // several run side by side on other streams; one block when no cluster can
+  // be placed); otherwise up to one block per SM with at least 32 elements
+  // each, one such grid at a time
   const size_t elem_bytes = (size_t)a.n * sizeof(T);
   const size_t op_bytes = (size_t)m->E * a.n * a.n * sizeof(T);
+  if (ls->coop_grid <= 0) {
+    // a cluster for a small system, and for one whose grid would have no
+    // more blocks than a cluster holds (no device-wide lock needed)
+    const int grid_blocks = std::max(2, std::min(sms, (m->E + 31) / 32));
+    int C = 0;
+    if (op_bytes <= kSmallOperatorBytes)
+      C = EG_GMRES_CLUSTER_BLOCKS;
+    else if (grid_blocks <= EG_GMRES_CLUSTER_BLOCKS)
+      C = grid_blocks;
+    while (C > 1 && C > m->E) C >>= 1;
+    if (C > 1) {
+      int rc = eg_gmres_cluster(ls, C);
+      if (rc == EG_ERR_UNSUPPORTED && C > 8) rc = eg_gmres_cluster(ls, 8);
+      if (rc != EG_ERR_UNSUPPORTED) return rc;
+    }
+  }
   int nblk = op_bytes <= kSmallOperatorBytes ? 1 : std::max(2, std::min(sms, (m->E + 31) / 32));
   if (ls->coop_grid > 0) nblk = std::min(ls->coop_grid, sms);
   if (nblk > m->E) nblk = m->E;

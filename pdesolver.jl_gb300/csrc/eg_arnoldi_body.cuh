@@ -689,4 +689,28 @@ __global__ void __launch_bounds__(NT, 1) k_gmres_coop(CoopArgs<T> a) {
   gmres_body<DIM, NB, T>(a, blockIdx.x, gridDim.x, bar, sm);
 }
 
+// barrier of a solve run by one thread-block cluster: the hardware cluster
+// barrier (arrive with release, wait with acquire semantics at cluster
+// scope, so the pushed products and partial sums written before it are seen
+// by every block of the cluster after it)
+struct ClusterBarrier {
+  cg::cluster_group c;
+  __device__ bool sync() {
+    c.sync();
+    return true;
+  }
+};
+
+// The same solve by the blocks of one cluster (a small system: one SM
+// would be latency-bound, a cooperative grid would need the device-wide
+// barrier); the cluster's blocks are co-scheduled by the hardware, so
+// several such solves run side by side on other streams.
+template <int DIM, int NB, typename T>
+__global__ void __launch_bounds__(NT, 1) k_gmres_cluster(CoopArgs<T> a) {
+  __shared__ GmresShared<T> sm;
+  cg::cluster_group cl = cg::this_cluster();
+  ClusterBarrier bar{cl};
+  gmres_body<DIM, NB, T>(a, (int)cl.block_rank(), (int)cl.num_blocks(), bar, sm);
+}
+
 }  // namespace

@@ -79,6 +79,12 @@ enum { F_DONE = 0, F_JDONE = 1, F_ITS = 2, F_CONV = 3, F_ITERMAX = 4, F_REORTH =
 enum { S_TOL = 0, S_RESID = 1, S_BETA = 2, S_BNORM = 3, S_RELTOL = 4, S_ABSTOL = 5, S_BETA0 = 6 };
 // the whole GMRES solve as one persistent cooperative kernel (eg_arnoldi.cu)
 #define EG_COOP_MAX_BLOCKS 1024
+// blocks of the thread-block cluster that runs a small system's GMRES solve
+// (16, a non-portable cluster size, measured faster than 8 on GB300; 8 is
+// taken where a 16-block cluster cannot be placed)
+#ifndef EG_GMRES_CLUSTER_BLOCKS
+#define EG_GMRES_CLUSTER_BLOCKS 16
+#endif
 // blocks of the stream GMRES path's reduction kernels (4 per SM)
 #define EG_GMRES_STREAM_BLOCKS 608
 // partial-sum slots of a GMRES(m) solver: the stream path's [blocks][m+2][2]
@@ -88,6 +94,9 @@ inline size_t eg_gmres_partials(int m) {
   return a > b ? a : b;
 }
 int eg_gmres_coop(eg_ls* ls);
+// the persistent solve of a small system by one cluster of C blocks
+// (EG_ERR_UNSUPPORTED when no such cluster can be placed)
+int eg_gmres_cluster(eg_ls* ls, int C);
 // one cooperative GMRES grid at a time per device (held across launch and
 // completion of multi-block grids, single or batched)
 std::mutex& eg_coop_mutex(int dev);
