@@ -1206,8 +1206,8 @@ def run_gmres_grid(args):
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     cases = [("c2 p1", (2, 64, 1)), ("c2 p3", (2, 64, 3)), ("n32 p3", (2, 32, 3)),
-             ("n16 p2", (2, 16, 2)), ("n96 p4", (2, 96, 4)), ("cube16 p2", (3, 16, 2)),
-             ("cube24 p2", (3, 24, 2))]
+             ("n16 p2", (2, 16, 2)), ("n24 p1", (2, 24, 1)), ("n96 p4", (2, 96, 4)),
+             ("cube4 p1", (3, 4, 1)), ("cube16 p2", (3, 16, 2)), ("cube24 p2", (3, 24, 2))]
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
     for name, key in cases:
         ms = problems.request_meshes(key)[-1]
@@ -1270,6 +1270,30 @@ def run_kernels_only(args, which):
         torch.cuda.synchronize()
         out["kernels"] = ["k_face_flux<3>", "k_split_element<3>"]
         out["launches_each"] = args.steps
+        print(json.dumps(out), flush=True)
+        return
+    if which == "cluster":
+        # a small system's GMRES (16 x 16 annulus, SBP-Gamma p=2, 1.6 MB of
+        # FP32 element blocks): one solve of `steps` iterations on the default
+        # launch, a thread-block cluster
+        ms_k = problems.request_meshes((2, 16, 2))[-1]
+        lv_k, q_k = problems.request_problem({"dim": 2, "n": 16, "p": 2, "M_in": 0.5, "seed": 1},
+                                             [ms_k])
+        gk = eulergpu.GPUMesh(ms_k, lv_k[0][1])
+        gk.set_stream(stream.cuda_stream)
+        lo = eulergpu.LinearOperator(gk, precision=1)
+        lo.calc(q_k)
+        pc = eulergpu.BlockJacobiPC(lo)
+        pc.calc()
+        ls = eulergpu.LinearSolver(pc, lo, restart=30)
+        ls.set_tolerances(reltol=1e-30, abstol=0.0, itermax=args.steps)
+        b = torch.randn(ms_k.numDof, dtype=torch.float64, device="cuda",
+                        generator=torch.Generator("cuda").manual_seed(1))
+        x = torch.zeros_like(b)
+        st = ls.solve(b, x)
+        torch.cuda.synchronize()
+        out["kernels"] = ["k_gmres_cluster<2,28,float>"]
+        out["iterations"] = st.iters
         print(json.dumps(out), flush=True)
         return
     if which == "flux":
@@ -1365,7 +1389,7 @@ def main():
     ap.add_argument("--fp64-stream", default="auto", choices=["auto", "on", "off"],
                     help="c5: also serve the stream with the FP64 server (auto: up to 300 requests)")
     ap.add_argument("--only", default=None, choices=["krylov", "residual", "gmres", "split", "blockinv",
-                                                     "flux"],
+                                                     "flux", "cluster"],
                     help="run only the isolated kernels (for profiler captures)")
     args = ap.parse_args()
     if args.only:

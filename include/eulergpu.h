@@ -274,8 +274,8 @@ int eg_ls_set_tolerances(eg_ls* ls, double reltol, double abstol, double dtol, i
 /* Blocks of the persistent GMRES kernel (one per SM at most, as a
    cooperative grid; 0 restores the automatic choice: one thread-block
    cluster of 16 blocks (8 where 16 cannot be placed) for operators of at
-   most 2 MB or systems of at most 16 x 32 elements, else up to one block per
-   SM with at least 32 elements each).  A tuning knob with no reference
+   most 2 MB or systems of at most 16 x 32 elements, else one block per SM,
+   at most one per element).  A tuning knob with no reference
    counterpart; the result does not depend on it beyond the order of the FP
    reductions. */
 int eg_ls_set_grid(eg_ls* ls, int32_t blocks);

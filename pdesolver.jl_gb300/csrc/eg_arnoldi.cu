@@ -61,19 +61,19 @@ int launch_T(eg_ls* ls) {
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   // grid: one cluster for a small system (its blocks are co-scheduled, so
   // several run side by side on other streams; one block when no cluster can
-  // be placed); otherwise up to one block per SM with at least 32 elements
-  // each, one such grid at a time
+  // be placed); otherwise one block per SM (at most one per element), one
+  // such grid at a time
   const size_t elem_bytes = (size_t)a.n * sizeof(T);
   const size_t op_bytes = (size_t)m->E * a.n * a.n * sizeof(T);
   if (ls->coop_grid <= 0) {
-    // a cluster for a small system, and for one whose grid would have no
-    // more blocks than a cluster holds (no device-wide lock needed)
-    const int grid_blocks = std::max(2, std::min(sms, (m->E + 31) / 32));
+    // a cluster for a small system, and for one with at most 32 elements
+    // per block of a cluster (no device-wide lock needed)
+    const int chunks = (m->E + 31) / 32;
     int C = 0;
     if (op_bytes <= kSmallOperatorBytes)
       C = EG_GMRES_CLUSTER_BLOCKS;
-    else if (grid_blocks <= EG_GMRES_CLUSTER_BLOCKS)
-      C = grid_blocks;
+    else if (chunks <= EG_GMRES_CLUSTER_BLOCKS)
+      C = std::max(2, chunks);
     while (C > 1 && C > m->E) C >>= 1;
     if (C > 1) {
       int rc = eg_gmres_cluster(ls, C);
@@ -81,7 +81,9 @@ int launch_T(eg_ls* ls) {
       if (rc != EG_ERR_UNSUPPORTED) return rc;
     }
   }
-  int nblk = op_bytes <= kSmallOperatorBytes ? 1 : std::max(2, std::min(sms, (m->E + 31) / 32));
+  // a lone multi-block grid (they run one at a time) takes every SM: the
+  // full grid was the fastest for every system above the cluster sizes
+  int nblk = op_bytes <= kSmallOperatorBytes ? 1 : std::max(2, std::min(sms, m->E));
   if (ls->coop_grid > 0) nblk = std::min(ls->coop_grid, sms);
   if (nblk > m->E) nblk = m->E;
   if (nblk > EG_COOP_MAX_BLOCKS) nblk = EG_COOP_MAX_BLOCKS;

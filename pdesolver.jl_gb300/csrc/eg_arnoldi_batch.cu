@@ -192,7 +192,14 @@ int wanted_blocks_sms(const eg_ls* ls, int sms) {
   const eg_mesh* m = ls->lo->mesh;
   const size_t es = ls->lo->prec == EG_F64 ? 8 : 4;
   const size_t op = (size_t)m->E * ls->lo->n * ls->lo->n * es;
-  int nb = op <= (size_t(2) << 20) ? 1 : std::max(2, std::min(sms, (m->E + 31) / 32));
+  // the block count of the same solve alone (eg_arnoldi.cu), so a batched
+  // solve keeps its partition and gives the same bits: one (a small system,
+  // solved by a cluster and never batched), the cluster's blocks for at most
+  // 16 x 32 elements, else one block per SM
+  const int chunks = (m->E + 31) / 32;
+  int nb = op <= (size_t(2) << 20) ? 1
+           : chunks <= EG_GMRES_CLUSTER_BLOCKS ? std::max(2, chunks)
+                                               : std::max(2, std::min(sms, m->E));
   nb = std::min(nb, m->E);
   return std::min(nb, EG_COOP_MAX_BLOCKS);
 }

@@ -144,6 +144,39 @@ def test_gmres_solves(gpu_lib, precision, tol):
 
 
 @pytest.mark.parametrize("precision,tol", [(0, 1e-10), (1, 1e-5)])
+def test_gmres_cluster_matches_grid_solves(gpu_lib, precision, tol):
+    """A small system (operator well under 2 MB) is solved by one 16-block
+    thread-block cluster by default; the same system on a one-block and on a
+    12-block cooperative grid (eg_ls_set_grid) reaches the same true residual
+    tolerance in about the same number of Krylov iterations (the block
+    partition changes only the order of the reductions).  Two default solves
+    give the same bits."""
+    ms, opts, q, g = setup(n=8, p=2, fam="gamma")
+    lo = eulergpu.LinearOperator(g, precision=precision)
+    lo.calc(q)
+    pc = eulergpu.BlockJacobiPC(lo)
+    pc.calc()
+    ls = eulergpu.LinearSolver(pc, lo, restart=30)
+    ls.set_tolerances(reltol=tol, abstol=0.0, itermax=3000)
+    b = np.random.default_rng(23).normal(size=q.shape)
+    lo64 = eulergpu.LinearOperator(g, precision=0)
+    lo64.calc(q)
+    xs, its = [], []
+    for grid in (0, 0, 1, 12):
+        ls.set_grid(grid)
+        x = np.zeros_like(b)
+        st = ls.solve(b, x)
+        assert st.converged == 1
+        r = b - lo64.apply(x, np.zeros_like(x))
+        assert np.linalg.norm(r) <= 3 * tol * np.linalg.norm(b), grid
+        xs.append(x)
+        its.append(st.iters)
+    ls.set_grid(0)
+    assert np.array_equal(xs[0], xs[1])          # the cluster solve is deterministic
+    assert max(its) <= 1.1 * min(its) + 3, its
+
+
+@pytest.mark.parametrize("precision,tol", [(0, 1e-10), (1, 1e-5)])
 def test_gmres_transpose_solves(gpu_lib, precision, tol):
     """linearSolveTranspose in the library (eg_ls_solve_transpose): J^T x = b
     against the dense solve of the transposed FP64 blocks (FP64 to 1e-10
