@@ -1327,7 +1327,7 @@ def run_kernels_only(args, which):
             for _ in range(args.steps):
                 pc.calc()
             torch.cuda.synchronize()
-        out["kernels"] = ["k_block_inverse_reg<float,2,8>", "k_block_inverse_reg<float,4,16>"]
+        out["kernels"] = ["k_block_inverse_reg<float,2,8,8>", "k_block_inverse_reg<float,4,8,16>"]
         out["launches_each"] = args.steps
         print(json.dumps(out), flush=True)
         return

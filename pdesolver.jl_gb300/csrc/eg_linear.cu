@@ -461,8 +461,8 @@ void launch_cpl_transpose(eg_lo* lo, const T* v, const T* z, T* w, const int* do
 }
 
 // Register-tiled Gauss-Jordan inversion for blocks of 33..128 unknowns, one
-// CTA of 256 threads (8 warps) per element block.  Thread (lane, warp) keeps
-// rows lane + 32 r (r < MR) and columns warp + 8 c (c < MC) in registers.
+// CTA of NW warps per element block.  Thread (lane, warp) keeps rows
+// lane + 32 r (r < MR) and columns warp + NW c (c < MC) in registers.
 // Partial pivoting is implicit: the pivot of column k is the unused row p of
 // largest |A[p][k]| (ties: lowest row), found by one warp with shuffles; row p
 // is scaled in place and eliminated from the others, so no rows move.  Row p
@@ -483,10 +483,10 @@ __device__ __forceinline__ void tile_row_shfl(const T (&a)[MR][MC], int r, int s
     }
 }
 
-template <typename T, int MR, int MC>
-__global__ void __launch_bounds__(256) k_block_inverse_reg(const T* __restrict__ blocks,
-                                                           T* __restrict__ inv, int n,
-                                                           unsigned int* __restrict__ status) {
+template <typename T, int MR, int MC, int NW>
+__global__ void __launch_bounds__(32 * NW) k_block_inverse_reg(const T* __restrict__ blocks,
+                                                                T* __restrict__ inv, int n,
+                                                                unsigned int* __restrict__ status) {
   extern __shared__ unsigned char smraw[];
   T* S = reinterpret_cast<T*>(smraw);                      // [n][n] column-major, at the end
   T* colk = S + (size_t)n * n;                             // [2][32 MR] column k
@@ -503,7 +503,7 @@ __global__ void __launch_bounds__(256) k_block_inverse_reg(const T* __restrict__
     if (i >= n) used |= 1u << r;
 #pragma unroll
     for (int c = 0; c < MC; ++c) {
-      const int col = warp + 8 * c;
+      const int col = warp + NW * c;
       a[r][c] = (i < n && col < n) ? src[(size_t)col * n + i] : T(0);
     }
   }
@@ -511,8 +511,8 @@ __global__ void __launch_bounds__(256) k_block_inverse_reg(const T* __restrict__
   for (int k = 0; k < n; ++k) {
     const int buf = k & 1;
     T* ck = colk + buf * 32 * MR;
-    const bool kwarp = warp == (k & 7);  // this warp holds column k, as its column kc
-    const int kc = k >> 3;
+    const bool kwarp = warp == (k % NW);  // this warp holds column k, as its column kc
+    const int kc = k / NW;
     if (kwarp) {
       T best = T(-1);
       int bi = n;
@@ -584,7 +584,7 @@ __global__ void __launch_bounds__(256) k_block_inverse_reg(const T* __restrict__
   for (int r = 0; r < MR; ++r)
 #pragma unroll
     for (int c = 0; c < MC; ++c) {
-      const int i = lane + 32 * r, col = warp + 8 * c;
+      const int i = lane + 32 * r, col = warp + NW * c;
       if (i < n && col < n) S[(size_t)col * n + i] = a[r][c];
     }
   __syncthreads();
@@ -612,23 +612,30 @@ int pccalc_T(eg_pc* pc) {
   eg_phase_begin(m, EG_PHASE_OTHER);
   const T* A = (const T*)lo->diag;
   T* X = (T*)pc->inv;
-#define EG_INV_REG(MR)                                                                          \
+  // MC x NW columns cover the block: 8 warps of 8 or 12 columns up to 96
+  // unknowns; up to 128, 16 warps of 8 columns in FP32 (4 x 8 values and 64
+  // registers per thread, two blocks per SM: 18 % faster than 8 warps of 16
+  // columns on 115-unknown blocks) and 8 warps of 16 columns in FP64 (the
+  // 16-warp tile measured 0.7 % slower there)
+#define EG_INV_REG(MR, MC, NW)                                                                  \
   {                                                                                           \
     const size_t smem = block_inverse_reg_smem<T, MR>(n);                                     \
-    cudaFuncSetAttribute(k_block_inverse_reg<T, MR, 4 * MR>,                                  \
+    cudaFuncSetAttribute(k_block_inverse_reg<T, MR, MC, NW>,                                  \
                          cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);            \
-    k_block_inverse_reg<T, MR, 4 * MR><<<m->E, 256, smem, m->stream>>>(A, X, n, m->status);   \
+    k_block_inverse_reg<T, MR, MC, NW><<<m->E, 32 * NW, smem, m->stream>>>(A, X, n, m->status); \
   }
   if (n <= 32) {
     const size_t smem = sizeof(T) * (size_t)n * n + sizeof(int) * n;
     cudaFuncSetAttribute(k_block_inverse<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     k_block_inverse<T><<<m->E, 256, smem, m->stream>>>(A, X, n, m->status);
   } else if (n <= 64) {
-    EG_INV_REG(2)
+    EG_INV_REG(2, 8, 8)
   } else if (n <= 96) {
-    EG_INV_REG(3)
+    EG_INV_REG(3, 12, 8)
+  } else if (sizeof(T) == 4) {
+    EG_INV_REG(4, 8, 16)
   } else {
-    EG_INV_REG(4)
+    EG_INV_REG(4, 16, 8)
   }
 #undef EG_INV_REG
   eg_phase_end(m, EG_PHASE_OTHER, 1);
