@@ -472,14 +472,19 @@ def run_ours(args, rank, world, dist):
     dom_name, dom_ms, dom_bytes = "k_gmres_coop", t_gm, b_gm
     achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
     traffic = None
+    traffic_source = None
     try:
         # DRAM bytes per Arnoldi iteration from an ncu capture of the same
         # kernel on the same system (profiles/), scaled to this launch
         with open(os.path.join(ROOT, "profiles", "krylov_c2_traffic.json")) as f:
-            per_it = json.load(f).get("k_gmres_coop_bytes_per_iteration")
+            rec = json.load(f)
+        per_it = rec.get("k_gmres_coop_bytes_per_iteration")
         if per_it:
             traffic = per_it * st_gm.iters
-    except (OSError, ValueError):
+            traffic_source = ("profiles/krylov_c2_traffic.json (captured %s): %s; DRAM bytes per "
+                              "iteration x %d iterations" % (rec.get("captured", "?"), rec.get("source", ""),
+                                                              st_gm.iters))
+    except (OSError, ValueError, AttributeError):
         pass
     # the CPU oracle: one complete solve on all host threads (the CPU
     # baseline, measured end to end), whose converged state and functional
@@ -530,7 +535,8 @@ def run_ours(args, rank, world, dist):
                    "functional_r1_mixed": f_mixed, "functional_r1_fp64": f64,
                    "functional_rel_diff": abs(f_mixed - f64) / abs(f64)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                     "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "peak_source": src,
+                     "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
+                     "traffic_source": traffic_source, "peak_source": src,
                      "kernel": dom_name + " (FP32: one launch = one GMRES(30) solve of the p=3 "
                                "Newton system at the converged state, %d iterations)" % st_gm.iters,
                      "algorithmic_bytes_per_launch": dom_bytes, "kernel_ms": dom_ms,
