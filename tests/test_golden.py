@@ -10,7 +10,7 @@ from conftest import oracle_residual
 from pdesolver_gb300 import abi, eulergpu
 
 HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-NAMES = ["c1", "gamma3", "tet2"]
+NAMES = ["c1", "gamma3", "tet2", "tet3", "wall3", "annwall"]
 
 
 def _gen():
@@ -25,9 +25,13 @@ GEN = _gen()
 
 @pytest.mark.parametrize("name", NAMES)
 def test_oracle_matches_golden(oracle, name):
+    """1e-12 relative to the largest entry, the GPU parity bar: the fixtures
+    were written on x86-64, and a compiler that contracts multiply-adds into
+    FMAs (gcc on aarch64 does by default) moves the oracle's result by about
+    1e-13 of it."""
     ms, opts, q, gold = GEN.load(name)
     res = oracle_residual(oracle, abi.MeshDesc(ms), eulergpu.params_from_opts(opts), q)
-    assert np.abs(res - gold).max() <= 1e-13 * np.abs(gold).max()
+    assert np.abs(res - gold).max() <= 1e-12 * np.abs(gold).max()
 
 
 @pytest.mark.parametrize("name", NAMES)

@@ -27,10 +27,11 @@ def gpu_residual(ms, opts, q):
     return res, g
 
 
-@pytest.mark.parametrize("name", ["c1", "gamma3", "tet2"])
+@pytest.mark.parametrize("name", ["c1", "gamma3", "tet2", "tet3", "wall3", "annwall"])
 def test_residual_matches_golden(gpu_lib, name):
     """GPU residual on the fixture's bit-exact inputs vs the committed oracle
-    residual."""
+    residual (weak and split forms, diagonal-E p=2 and p=3, and the
+    entropy-stable wall in 2-D and 3-D)."""
     from test_golden import GEN
     ms, opts, q, gold = GEN.load(name)
     res, _ = gpu_residual(ms, opts, np.ascontiguousarray(q))
