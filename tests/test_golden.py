@@ -37,12 +37,13 @@ def test_oracle_matches_golden(oracle, name):
 @pytest.mark.parametrize("name", NAMES)
 def test_setup_regenerates_fixture(name):
     """the seeded state and the operator/mesh set-up reproduce the fixture
-    (to round-off: numpy's linear algebra may differ in the last bits across
-    machines)."""
+    (to round-off: numpy's linear algebra and elementary functions may differ
+    in the last bits across machines; the vortex state differs by 1.4e-14
+    between x86-64 and Arm)."""
     cases = dict(GEN.cases())
     ms, opts, q = cases[name]
     gms, gopts, gq, _ = GEN.load(name)
     assert opts == gopts
-    np.testing.assert_allclose(q, gq, rtol=1e-14, atol=0)
+    np.testing.assert_allclose(q, gq, rtol=1e-13, atol=0)
     np.testing.assert_allclose(ms.sbp.Q, gms.sbp.Q, atol=1e-12)
     np.testing.assert_allclose(ms.dxidx, gms.dxidx, rtol=1e-12, atol=1e-14)
